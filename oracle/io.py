@@ -1,0 +1,114 @@
+"""Binary I/O between the oracle's Python side and its C programs.
+
+Test infrastructure only.  ``write_input`` produces the "SPHIN001" file read by
+oracle/ref_harness.c (the driver of the reference's own loops) and by the C
+restatement in oracle/sph_oracle.c; ``read_output`` parses "SPHOUT01".
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import numpy as np
+
+STAGE_DENSITY, STAGE_GHOST, STAGE_FORCE = 1, 2, 4
+ALL_STAGES = STAGE_DENSITY | STAGE_GHOST | STAGE_FORCE
+
+# Field columns of the per-particle result block (24 floats per particle).
+COLS = {
+    "d_rho": 0, "d_rho_dh": 1, "d_wcount": 2, "d_wcount_dh": 3, "d_div_v": 4,
+    "d_rot_vx": 5, "d_rot_vy": 6, "d_rot_vz": 7,
+    "h": 8, "rho": 9, "f": 10, "pressure": 11, "soundspeed": 12,
+    "balsara": 13, "v_sig_ghost": 14,
+    "ax": 15, "ay": 16, "az": 17, "u_dt": 18, "h_dt": 19, "v_sig": 20,
+}
+
+CELL_DTYPE = np.dtype([
+    ("loc", "<f8", 3), ("width", "<f8", 3), ("h_max", "<f4"),
+    ("h_max_active", "<f4"), ("dmin", "<f4"), ("depth", "<i4"),
+    ("split", "<i4"), ("count", "<i4"), ("first", "<i4"), ("parent", "<i4"),
+    ("top", "<i4"), ("_pad", "<i4"),
+])
+assert CELL_DTYPE.itemsize == 88
+
+HEADER_DTYPE = np.dtype([
+    ("magic", "S8"), ("n", "<i8"), ("dim", "<f8", 3), ("eta", "<f4"),
+    ("h_tolerance", "<f4"), ("h_max", "<f4"), ("h_min", "<f4"),
+    ("alpha", "<f4"), ("max_iter", "<i4"), ("max_active_bin", "<i4"),
+    ("periodic", "<i4"), ("stages", "<i4"), ("_pad", "<i4"),
+])
+assert HEADER_DTYPE.itemsize == 80
+
+
+def default_params(box):
+    return dict(eta=box.get("eta", 1.2348), h_tolerance=1e-4,
+                h_max=np.finfo(np.float32).max, h_min=0.0, alpha=0.8,
+                max_iter=30, max_active_bin=box.get("max_active_bin", 56),
+                periodic=1)
+
+
+def write_input(path, box, stages=ALL_STAGES, **overrides):
+    p = default_params(box)
+    p.update(overrides)
+    n = box["x"].shape[0]
+    hdr = np.zeros(1, HEADER_DTYPE)
+    hdr["magic"] = b"SPHIN001"
+    hdr["n"] = n
+    hdr["dim"] = [box["dim"]] * 3
+    for k in ("eta", "h_tolerance", "h_max", "h_min", "alpha", "max_iter",
+              "max_active_bin", "periodic"):
+        hdr[k] = p[k]
+    hdr["stages"] = stages
+    with open(path, "wb") as f:
+        f.write(hdr.tobytes())
+        f.write(np.ascontiguousarray(box["x"], np.float64).tobytes())
+        f.write(np.ascontiguousarray(box["v"], np.float32).tobytes())
+        for k in ("m", "h", "u"):
+            f.write(np.ascontiguousarray(box[k], np.float32).tobytes())
+        f.write(np.ascontiguousarray(box["time_bin"], np.int8).tobytes())
+
+
+INT_COLS = {"leaf_first": 0, "leaf_count": 1, "leaf_depth": 2, "depth_h": 3,
+            "position": 4, "top": 5, "ngb_first": 6, "ngb_final": 7,
+            "ngb_force": 8, "ghost_iters": 9}
+
+
+def read_output(path):
+    with open(path, "rb") as f:
+        buf = f.read()
+    assert buf[:8] == b"SPHOUT01", "bad oracle output magic"
+    off = 8
+    n, nf, ncell, c0, c1, c2, ni = np.frombuffer(buf, "<i8", 7, off)
+    off += 56
+    width = np.frombuffer(buf, "<f8", 3, off)
+    off += 24
+    res = np.frombuffer(buf, "<f4", n * nf, off).reshape(n, nf)
+    off += 4 * n * nf
+    ints = np.frombuffer(buf, "<i4", ni * n, off).reshape(n, ni)
+    off += 4 * ni * n
+    cells = np.frombuffer(buf, CELL_DTYPE, ncell, off)
+    out = {"res": res, "ints": ints, "cells": cells,
+           "cdim": (int(c0), int(c1), int(c2)), "width": width.copy()}
+    for name, col in COLS.items():
+        out[name] = res[:, col]
+    for name, col in INT_COLS.items():
+        if col < ni:
+            out[name] = ints[:, col]
+    return out
+
+
+def ref_harness_path(mode="parity"):
+    here = os.path.dirname(os.path.abspath(__file__))
+    return os.path.join(here, "_ref", mode, "bin", "ref_harness")
+
+
+def run_reference(box, workdir, stages=ALL_STAGES, mode="parity", **overrides):
+    """Run the reference's own loops (oracle/_ref) on ``box``."""
+    exe = ref_harness_path(mode)
+    if not os.path.exists(exe):
+        raise FileNotFoundError(f"reference harness not built: {exe}")
+    inp = os.path.join(workdir, "ref_in.bin")
+    out = os.path.join(workdir, "ref_out.bin")
+    write_input(inp, box, stages, **overrides)
+    subprocess.run([exe, inp, out], check=True, capture_output=True)
+    return read_output(out)

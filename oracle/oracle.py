@@ -1,0 +1,136 @@
+"""ctypes front end of the oracle's C restatement (oracle/sph_oracle.c).
+
+Test infrastructure only: tests, the smoke check and bench.py's CPU-baseline
+leg use it as the checker; the GPU library never imports it.  ``build()``
+compiles the restatement with the same floating-point flags as the parity
+build of the reference (no fast-math, no FMA contraction), so that its sums
+can be compared bit for bit with the reference's own loops.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from .io import COLS, INT_COLS
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libsphoracle.so")
+NFIELDS, NINTS = 24, 10
+STAGE_DENSITY, STAGE_GHOST, STAGE_FORCE = 1, 2, 4
+ALL = 7
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_double * 3), ("periodic", ctypes.c_int32),
+                ("eta", ctypes.c_float), ("h_tolerance", ctypes.c_float),
+                ("h_max", ctypes.c_float), ("h_min", ctypes.c_float),
+                ("alpha", ctypes.c_float), ("max_iter", ctypes.c_int32),
+                ("max_active_bin", ctypes.c_int32),
+                ("max_top_level_cells", ctypes.c_int32)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("fields", ctypes.POINTER(ctypes.c_float)),
+                ("ints", ctypes.POINTER(ctypes.c_int32)),
+                ("cdim", ctypes.c_int32 * 3), ("ncells", ctypes.c_int32),
+                ("status", ctypes.c_int32)]
+
+
+def build(force=False):
+    src = os.path.join(HERE, "sph_oracle.c")
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= os.path.getmtime(src)):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.run(["gcc", "-std=gnu11", "-O2", "-fno-fast-math",
+                    "-ffp-contract=off", "-fPIC", "-shared", src, "-o", tmp,
+                    "-lm"], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB)
+        _lib.sph_oracle_run.restype = ctypes.c_int
+        _lib.sph_oracle_exact64.restype = None
+    return _lib
+
+
+def make_params(box, **kw):
+    p = Params()
+    d = box["dim"]
+    p.dim[:] = [d, d, d]
+    p.periodic = kw.get("periodic", 1)
+    p.eta = kw.get("eta", box.get("eta", 1.2348))
+    p.h_tolerance = kw.get("h_tolerance", 1e-4)
+    p.h_max = kw.get("h_max", float(np.finfo(np.float32).max))
+    p.h_min = kw.get("h_min", 0.0)
+    p.alpha = kw.get("alpha", 0.8)
+    p.max_iter = kw.get("max_iter", 30)
+    p.max_active_bin = kw.get("max_active_bin", box.get("max_active_bin", 56))
+    p.max_top_level_cells = kw.get("max_top_level_cells", 12)
+    return p
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def run(box, stages=ALL, **kw):
+    """One density -> ghost -> force pass of the restated reference loops."""
+    L = lib()
+    n = box["x"].shape[0]
+    x = np.ascontiguousarray(box["x"], np.float64)
+    v = np.ascontiguousarray(box["v"], np.float32)
+    m = np.ascontiguousarray(box["m"], np.float32)
+    h = np.ascontiguousarray(box["h"], np.float32)
+    u = np.ascontiguousarray(box["u"], np.float32)
+    tb = np.ascontiguousarray(box["time_bin"], np.int8)
+    fields = np.zeros((n, NFIELDS), np.float32)
+    ints = np.zeros((n, NINTS), np.int32)
+    res = Result()
+    res.fields = _ptr(fields, ctypes.c_float)
+    res.ints = _ptr(ints, ctypes.c_int32)
+    prm = make_params(box, **kw)
+    L.sph_oracle_run(ctypes.byref(prm), ctypes.c_int(n), _ptr(x, ctypes.c_double),
+                     _ptr(v, ctypes.c_float), _ptr(m, ctypes.c_float),
+                     _ptr(h, ctypes.c_float), _ptr(u, ctypes.c_float),
+                     _ptr(tb, ctypes.c_byte), ctypes.c_int(stages),
+                     ctypes.byref(res))
+    out = {"res": fields, "ints": ints, "cdim": tuple(res.cdim),
+           "ncells": res.ncells, "status": res.status}
+    for name, col in COLS.items():
+        out[name] = fields[:, col]
+    for name, col in INT_COLS.items():
+        out[name] = ints[:, col]
+    return out
+
+
+def exact64(box, out):
+    """FP64 sums (rho, wcount, div_v, a[3], u_dt) at the oracle's final h."""
+    L = lib()
+    n = box["x"].shape[0]
+    x = np.ascontiguousarray(box["x"], np.float64)
+    v = np.ascontiguousarray(box["v"], np.float32)
+    m = np.ascontiguousarray(box["m"], np.float32)
+    arrs = [np.ascontiguousarray(out[k], np.float32)
+            for k in ("h", "rho", "f", "pressure", "soundspeed", "balsara")]
+    res = np.zeros((n, 7), np.float64)
+    prm = make_params(box)
+    L.sph_oracle_exact64(ctypes.byref(prm), ctypes.c_int(n),
+                         _ptr(x, ctypes.c_double), _ptr(v, ctypes.c_float),
+                         _ptr(m, ctypes.c_float),
+                         *[_ptr(a, ctypes.c_float) for a in arrs],
+                         _ptr(res, ctypes.c_double))
+    return res

@@ -1,0 +1,165 @@
+/* swift_gb300.h -- C ABI of the GB300 SPH neighbour-interaction library.
+ *
+ * Plain C types only (pointers, sizes, integers).  Every function returns 0
+ * on success or a negative SPHGPU_E* code; sphgpu_last_error() gives the
+ * message of the last failure on the calling thread.  Nothing here aborts
+ * the process: where the reference's runner functions call error() (e.g.
+ * runner_ghost.c:1592 when h does not converge) this library returns
+ * SPHGPU_ENOCONV and leaves the decision to the caller.
+ *
+ * Particle arrays are passed in the caller's order ("input order"); the
+ * library keeps its own cell-sorted copy in HBM and maps results back.
+ * Positions are FP64 [n][3]; velocities FP32 [n][3]; mass, h, u FP32 [n];
+ * time bins int8 [n].
+ *
+ * Reference interfaces replaced (paths relative to SWIFT's src/):
+ *   sphgpu_space_create        space_init + space_rebuild (space.c:1136,
+ *                              space_rebuild.c:49): grid, cell index, split
+ *   sphgpu_dosub_self1_density runner_dosub_self1_density
+ *                              (runner_doiact_functions_hydro.h:3037,
+ *                               declared runner_doiact_hydro.h:187-195)
+ *   sphgpu_dosub_pair1_density runner_dosub_pair1_density (:2933)
+ *   sphgpu_do_ghost            runner_do_ghost (runner_ghost.c:1113)
+ *   sphgpu_dosub_self2_force   runner_dosub_self2_force (:3203)
+ *   sphgpu_dosub_pair2_force   runner_dosub_pair2_force (:3102)
+ *   sphgpu_do_end_hydro_force  runner_do_end_hydro_force (runner_others.c:815)
+ *   sphgpu_step                one engine_init_particles-style pass
+ *                              (engine.c:2245): all density tasks, the
+ *                              ghosts and all force tasks, batched into one
+ *                              persistent launch per loop and one CUDA graph.
+ */
+#ifndef SWIFT_GB300_H
+#define SWIFT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHGPU_ABI_VERSION 1
+
+#define SPHGPU_OK 0
+#define SPHGPU_EINVAL -1   /* bad argument */
+#define SPHGPU_ECUDA -2    /* CUDA runtime error (message has details) */
+#define SPHGPU_ENOMEM -3   /* device or host allocation failed */
+#define SPHGPU_ENOCONV -4  /* smoothing lengths did not converge */
+#define SPHGPU_ESTATE -5   /* call out of order (e.g. no step run yet) */
+#define SPHGPU_ENODEV -6   /* no CUDA device */
+
+/* Stages of a step (bit mask). */
+#define SPHGPU_STAGE_DENSITY 1
+#define SPHGPU_STAGE_GHOST 2
+#define SPHGPU_STAGE_FORCE 4
+#define SPHGPU_STAGE_ALL 7
+
+typedef struct sphgpu_space sphgpu_space;
+
+/* Run-time parameters; names follow the reference's parameter file
+ * (SPH:resolution_eta, SPH:h_tolerance, SPH:h_max, SPH:h_min_ratio,
+ * SPH:max_ghost_iterations, SPH:viscosity_alpha,
+ * Scheduler:max_top_level_cells; hydro_properties.c:58-110). */
+typedef struct {
+  double dim[3];
+  int32_t periodic;
+  float eta;
+  float h_tolerance;
+  float h_max;
+  float h_min;
+  float alpha;
+  int32_t max_iter;
+  int32_t max_active_bin;
+  int32_t max_top_level_cells;
+} sphgpu_params;
+
+/* Launch configuration of the gather kernels (what the autotuner picks). */
+typedef struct {
+  int32_t threads_per_particle; /* 1, 2, 4 or 8 */
+  int32_t jtile;                /* 64 or 128 partner particles per tile */
+  int32_t persistent;           /* 1: resident grid + device work queue */
+} sphgpu_tuning;
+
+int sphgpu_abi_version(void);
+const char *sphgpu_last_error(void);
+void sphgpu_default_params(sphgpu_params *p);
+
+/* Build the cell tree of a box (host) and keep its particles for the GPU.
+ * Replaces space_init + space_rebuild.  No device is touched until the
+ * first GPU call, so tree queries work without a GPU. */
+int sphgpu_space_create(const sphgpu_params *prm, int64_t n, const double *x,
+                        const float *v, const float *m, const float *h,
+                        const float *u, const int8_t *time_bin,
+                        sphgpu_space **out);
+int sphgpu_space_destroy(sphgpu_space *s);
+
+/* info[0..7] = n, cdim[0..2], cells, leaves, top-level tasks, gather entries */
+int sphgpu_space_info(const sphgpu_space *s, int64_t info[8]);
+
+/* Cell assignment per particle (input order), int32 [n][6]: first index of
+ * the particle's leaf, leaf count, leaf depth, depth_h, position in the
+ * cell-sorted order, top-level cell id (cell_getid order). */
+int sphgpu_space_cells(const sphgpu_space *s, int32_t *out);
+
+/* Leaf geometry, double [leaves][6] = loc[3], width[3], plus int32
+ * [leaves][3] = first, count, depth (may be NULL). */
+int sphgpu_space_leaves(const sphgpu_space *s, double *geom, int32_t *ints);
+
+/* Change the active set (particles with time_bin <= max_active_bin). */
+int sphgpu_set_active(sphgpu_space *s, int32_t max_active_bin);
+
+int sphgpu_set_tuning(sphgpu_space *s, const sphgpu_tuning *t);
+int sphgpu_get_tuning(const sphgpu_space *s, sphgpu_tuning *t);
+
+/* Batched form: density -> ghost -> force over the whole box, one
+ * persistent launch per loop, captured as one CUDA graph on the first call
+ * (stages == SPHGPU_STAGE_ALL).  Inputs and outputs stay in HBM.  `stream`
+ * is a cudaStream_t (NULL: the library's own stream).  Returns
+ * SPHGPU_ENOCONV if some h did not converge in max_iter rounds. */
+int sphgpu_step(sphgpu_space *s, int32_t stages, void *stream);
+
+/* Same pass through host buffers: copies x, v, m, h, u (input order) from
+ * host memory, runs the step, copies the results back.  `fields` receives
+ * float [n][24] in the column layout of sphgpu_download; NULL skips it. */
+int sphgpu_step_host(sphgpu_space *s, const double *x, const float *v,
+                     const float *m, const float *h, const float *u,
+                     float *fields, void *stream);
+
+/* Plain form: the same pass issued task by task as the reference's runner
+ * would (one launch per self/pair task and loop, one ghost per top cell). */
+int sphgpu_step_plain(sphgpu_space *s, void *stream);
+
+/* Results in input order.  fields float [n][24]: 0-7 raw density sums of
+ * the last density pass (rho, rho_dh, wcount, wcount_dh, div_v, rot_v[3]),
+ * 8-14 after the ghost (h, rho, f, pressure, soundspeed, balsara, v_sig
+ * seed), 15-20 after the force (a_hydro[3], u_dt, h_dt, v_sig).
+ * ints int32 [n][4]: density neighbours (first pass), density neighbours
+ * (last pass), force neighbours, ghost rounds.  Either may be NULL. */
+int sphgpu_download(sphgpu_space *s, float *fields, int32_t *ints);
+
+/* Force loop only, from caller-provided post-ghost state (input order):
+ * h, rho, f, pressure, soundspeed, balsara.  For parity checks of the force
+ * loop against the reference's own post-ghost values. */
+int sphgpu_force_from_state(sphgpu_space *s, const float *h, const float *rho,
+                            const float *f, const float *pressure,
+                            const float *soundspeed, const float *balsara,
+                            void *stream);
+
+/* Drop-in per-task entry points (plain form).  `cell` / `ci`, `cj` are
+ * top-level cell ids (cell_getid order).  Density and force accumulate into
+ * the particle sums like the reference's loops; call sphgpu_begin_loops()
+ * first to zero them. */
+int sphgpu_begin_loops(sphgpu_space *s, void *stream);
+int sphgpu_dosub_self1_density(sphgpu_space *s, int32_t cell, void *stream);
+int sphgpu_dosub_pair1_density(sphgpu_space *s, int32_t ci, int32_t cj,
+                               void *stream);
+int sphgpu_do_ghost(sphgpu_space *s, int32_t cell, void *stream);
+int sphgpu_dosub_self2_force(sphgpu_space *s, int32_t cell, void *stream);
+int sphgpu_dosub_pair2_force(sphgpu_space *s, int32_t ci, int32_t cj,
+                             void *stream);
+int sphgpu_do_end_hydro_force(sphgpu_space *s, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWIFT_GB300_H */

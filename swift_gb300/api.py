@@ -1,0 +1,265 @@
+"""Python host mirror of the C ABI (include/swift_gb300.h).
+
+The reference's host for this path is C (runner_main.c dispatching
+runner_dosub_*_density/force and runner_do_ghost); this module is the thin
+Python face of the same C-ABI library, used by the tests, the benchmark and
+the serving loop.  Arrays are NumPy; nothing here computes physics.  If the
+compiled library is missing the import fails loudly: there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+STAGE_DENSITY, STAGE_GHOST, STAGE_FORCE, STAGE_ALL = 1, 2, 4, 7
+OK, EINVAL, ECUDA, ENOMEM, ENOCONV, ESTATE, ENODEV = 0, -1, -2, -3, -4, -5, -6
+
+FIELD_COLS = {
+    "d_rho": 0, "d_rho_dh": 1, "d_wcount": 2, "d_wcount_dh": 3, "d_div_v": 4,
+    "d_rot_vx": 5, "d_rot_vy": 6, "d_rot_vz": 7,
+    "h": 8, "rho": 9, "f": 10, "pressure": 11, "soundspeed": 12,
+    "balsara": 13, "v_sig_ghost": 14,
+    "ax": 15, "ay": 16, "az": 17, "u_dt": 18, "h_dt": 19, "v_sig": 20,
+}
+INT_COLS = {"ngb_first": 0, "ngb_final": 1, "ngb_force": 2, "ghost_iters": 3}
+CELL_COLS = {"leaf_first": 0, "leaf_count": 1, "leaf_depth": 2, "depth_h": 3,
+             "position": 4, "top": 5}
+
+
+class SphGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"sphgpu error {code}: {msg}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_double * 3), ("periodic", ctypes.c_int32),
+                ("eta", ctypes.c_float), ("h_tolerance", ctypes.c_float),
+                ("h_max", ctypes.c_float), ("h_min", ctypes.c_float),
+                ("alpha", ctypes.c_float), ("max_iter", ctypes.c_int32),
+                ("max_active_bin", ctypes.c_int32),
+                ("max_top_level_cells", ctypes.c_int32)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("threads_per_particle", ctypes.c_int32),
+                ("jtile", ctypes.c_int32), ("persistent", ctypes.c_int32)]
+
+
+# Every symbol the header declares, with its ctypes signature.
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+SIGNATURES = {
+    "sphgpu_abi_version": (ctypes.c_int, []),
+    "sphgpu_last_error": (ctypes.c_char_p, []),
+    "sphgpu_default_params": (None, [ctypes.POINTER(Params)]),
+    "sphgpu_space_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64,
+                                           _P, _P, _P, _P, _P, _P,
+                                           ctypes.POINTER(_P)]),
+    "sphgpu_space_destroy": (ctypes.c_int, [_P]),
+    "sphgpu_space_info": (ctypes.c_int, [_P, _P]),
+    "sphgpu_space_cells": (ctypes.c_int, [_P, _P]),
+    "sphgpu_space_leaves": (ctypes.c_int, [_P, _P, _P]),
+    "sphgpu_set_active": (ctypes.c_int, [_P, _I32]),
+    "sphgpu_set_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
+    "sphgpu_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
+    "sphgpu_step": (ctypes.c_int, [_P, _I32, _P]),
+    "sphgpu_step_host": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "sphgpu_step_plain": (ctypes.c_int, [_P, _P]),
+    "sphgpu_download": (ctypes.c_int, [_P, _P, _P]),
+    "sphgpu_force_from_state": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "sphgpu_begin_loops": (ctypes.c_int, [_P, _P]),
+    "sphgpu_dosub_self1_density": (ctypes.c_int, [_P, _I32, _P]),
+    "sphgpu_dosub_pair1_density": (ctypes.c_int, [_P, _I32, _I32, _P]),
+    "sphgpu_do_ghost": (ctypes.c_int, [_P, _I32, _P]),
+    "sphgpu_dosub_self2_force": (ctypes.c_int, [_P, _I32, _P]),
+    "sphgpu_dosub_pair2_force": (ctypes.c_int, [_P, _I32, _I32, _P]),
+    "sphgpu_do_end_hydro_force": (ctypes.c_int, [_P, _P]),
+}
+
+_lib = None
+
+
+def lib(build_if_missing=True):
+    """Load the in-tree library (building it first if allowed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise ImportError(f"swift_gb300: compiled library missing at {path}; "
+                          "run swift_gb300.build.build()")
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != OK:
+        msg = lib().sphgpu_last_error()
+        raise SphGpuError(rc, msg.decode() if msg else "")
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def make_params(box, **kw):
+    L = lib()
+    p = Params()
+    L.sphgpu_default_params(ctypes.byref(p))
+    d = box["dim"]
+    p.dim[:] = [d, d, d]
+    p.eta = kw.get("eta", box.get("eta", p.eta))
+    for k in ("periodic", "h_tolerance", "h_max", "h_min", "alpha", "max_iter",
+              "max_top_level_cells"):
+        if k in kw:
+            setattr(p, k, kw[k])
+    p.max_active_bin = kw.get("max_active_bin", box.get("max_active_bin",
+                                                        p.max_active_bin))
+    return p
+
+
+class Space:
+    """A box of SPH particles with its cell tree, resident on the GPU once a
+    GPU call is made.  Mirrors the reference's space + runner entry points."""
+
+    def __init__(self, box, **params):
+        L = lib()
+        self.n = int(box["x"].shape[0])
+        self._keep = {
+            "x": np.ascontiguousarray(box["x"], np.float64),
+            "v": np.ascontiguousarray(box["v"], np.float32),
+            "m": np.ascontiguousarray(box["m"], np.float32),
+            "h": np.ascontiguousarray(box["h"], np.float32),
+            "u": np.ascontiguousarray(box["u"], np.float32),
+            "tb": np.ascontiguousarray(box["time_bin"], np.int8),
+        }
+        k = self._keep
+        self.params = make_params(box, **params)
+        h = ctypes.c_void_p()
+        _check(L.sphgpu_space_create(ctypes.byref(self.params), self.n,
+                                     _ptr(k["x"]), _ptr(k["v"]), _ptr(k["m"]),
+                                     _ptr(k["h"]), _ptr(k["u"]), _ptr(k["tb"]),
+                                     ctypes.byref(h)))
+        self._h = h
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sphgpu_space_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- tree --------------------------------------------------------------
+    def info(self):
+        out = np.zeros(8, np.int64)
+        _check(lib().sphgpu_space_info(self._h, _ptr(out)))
+        keys = ("n", "cdim0", "cdim1", "cdim2", "cells", "leaves", "tasks",
+                "entries")
+        return dict(zip(keys, (int(v) for v in out)))
+
+    def cells(self):
+        out = np.zeros((self.n, 6), np.int32)
+        _check(lib().sphgpu_space_cells(self._h, _ptr(out)))
+        return {name: out[:, col] for name, col in CELL_COLS.items()}
+
+    def leaves(self):
+        nl = self.info()["leaves"]
+        geom = np.zeros((nl, 6), np.float64)
+        ints = np.zeros((nl, 3), np.int32)
+        _check(lib().sphgpu_space_leaves(self._h, _ptr(geom), _ptr(ints)))
+        return geom, ints
+
+    # -- configuration -----------------------------------------------------
+    def set_tuning(self, tpi=1, jtile=64, persistent=1):
+        t = Tuning(tpi, jtile, persistent)
+        _check(lib().sphgpu_set_tuning(self._h, ctypes.byref(t)))
+
+    def tuning(self):
+        t = Tuning()
+        _check(lib().sphgpu_get_tuning(self._h, ctypes.byref(t)))
+        return (t.threads_per_particle, t.jtile, t.persistent)
+
+    def set_active(self, max_active_bin):
+        _check(lib().sphgpu_set_active(self._h, int(max_active_bin)))
+
+    # -- GPU passes --------------------------------------------------------
+    def step(self, stages=STAGE_ALL, stream=None):
+        _check(lib().sphgpu_step(self._h, stages, stream))
+
+    def step_plain(self, stream=None):
+        _check(lib().sphgpu_step_plain(self._h, stream))
+
+    def step_host(self, box=None, fields=None, stream=None):
+        b = self._keep if box is None else {
+            "x": np.ascontiguousarray(box["x"], np.float64),
+            "v": np.ascontiguousarray(box["v"], np.float32),
+            "m": np.ascontiguousarray(box["m"], np.float32),
+            "h": np.ascontiguousarray(box["h"], np.float32),
+            "u": np.ascontiguousarray(box["u"], np.float32)}
+        _check(lib().sphgpu_step_host(self._h, _ptr(b["x"]), _ptr(b["v"]),
+                                      _ptr(b["m"]), _ptr(b["h"]), _ptr(b["u"]),
+                                      _ptr(fields), stream))
+        return fields
+
+    def download(self):
+        fields = np.zeros((self.n, 24), np.float32)
+        ints = np.zeros((self.n, 4), np.int32)
+        _check(lib().sphgpu_download(self._h, _ptr(fields), _ptr(ints)))
+        out = {"fields": fields, "ints": ints}
+        for name, col in FIELD_COLS.items():
+            out[name] = fields[:, col]
+        for name, col in INT_COLS.items():
+            out[name] = ints[:, col]
+        return out
+
+    def force_from_state(self, h, rho, f, pressure, soundspeed, balsara):
+        arrs = [np.ascontiguousarray(a, np.float32)
+                for a in (h, rho, f, pressure, soundspeed, balsara)]
+        _check(lib().sphgpu_force_from_state(self._h, *[_ptr(a) for a in arrs],
+                                             None))
+
+    # -- drop-in per-task entry points --------------------------------------
+    def begin_loops(self):
+        _check(lib().sphgpu_begin_loops(self._h, None))
+
+    def dosub_self1_density(self, cell):
+        _check(lib().sphgpu_dosub_self1_density(self._h, int(cell), None))
+
+    def dosub_pair1_density(self, ci, cj):
+        _check(lib().sphgpu_dosub_pair1_density(self._h, int(ci), int(cj), None))
+
+    def do_ghost(self, cell):
+        _check(lib().sphgpu_do_ghost(self._h, int(cell), None))
+
+    def dosub_self2_force(self, cell):
+        _check(lib().sphgpu_dosub_self2_force(self._h, int(cell), None))
+
+    def dosub_pair2_force(self, ci, cj):
+        _check(lib().sphgpu_dosub_pair2_force(self._h, int(ci), int(cj), None))
+
+    def do_end_hydro_force(self):
+        _check(lib().sphgpu_do_end_hydro_force(self._h, None))

@@ -1,0 +1,151 @@
+// space.h -- host planner: reference space build and recursion -> gather
+// lists (see space.cpp for the reference citations).
+#pragma once
+#include <stdint.h>
+
+#include <utility>
+#include <vector>
+
+#include "sph_types.h"
+
+namespace sphgpu {
+
+struct Params {
+  double dim[3] = {1.0, 1.0, 1.0};
+  int periodic = 1;
+  float eta = 1.2348f;
+  float h_tolerance = 1e-4f;
+  float h_max = 3.40282347e+38f;
+  float h_min = 0.f;
+  float alpha = 0.8f;
+  int max_iter = 30;
+  int max_active_bin = 56;
+  int max_top_level_cells = 12;
+};
+
+struct Cell {
+  double loc[3] = {0, 0, 0}, width[3] = {0, 0, 0};
+  float dmin = 0, h_min_allowed = 0, h_max_allowed = 0;
+  float h_max = 0, h_max_active = 0, h_max_old = 0;
+  int count = 0, first = 0, depth = 0, split = 0, active = 0;
+  int parent = -1, top = -1, leaf = -1;
+  int progeny[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+};
+
+struct TopTask {
+  int ci, cj;  // cj < 0: self task
+};
+
+struct Item {
+  int kind;
+  int a, b;  // a = ci after the swap (or the self cell), b = cj or -1
+  double shift[3];
+  int min_depth, max_depth;
+};
+
+struct Plan {
+  std::vector<Entry> entries;
+  std::vector<Unit> units;
+  std::vector<int> leaf_entry_begin;
+};
+
+class Space {
+ public:
+  static constexpr int kSplitSize = 400;     // space.h:49
+  static constexpr int kRecurseSize = 100;   // space.h:64-65
+
+  explicit Space(const Params& prm);
+  void build(int64_t n, const double* x, const float* h, const int8_t* time_bin);
+  void set_activity(int max_active_bin);
+  void set_unit_chunk(int c) { unit_chunk_ = c; }
+
+  // Gather lists: first density pass (second=false) or force pass
+  // (second=true, call update_h_after_ghost first); ghost re-runs.
+  void plan_density(Plan& plan, bool second) const;
+  void plan_subset(Plan& plan) const;
+  void leaf_infos(std::vector<LeafInfo>& out) const;
+  void update_h_after_ghost(const float* h_sorted);
+
+  int n() const { return n_; }
+  const int* cdim() const { return cdim_; }
+  const double* width() const { return width_; }
+  const std::vector<Cell>& cells() const { return cells_; }
+  const std::vector<int>& leaves() const { return leaves_; }
+  const std::vector<int>& perm() const { return perm_; }          // sorted -> input
+  const std::vector<int>& inv_perm() const { return inv_perm_; }  // input -> sorted
+  const std::vector<int8_t>& depth_h() const { return depth_h_; }
+  const std::vector<int>& leaf_of() const { return leaf_of_; }
+  const std::vector<uint8_t>& active() const { return active_; }
+  const std::vector<double>& x() const { return x_; }  // wrapped, input order
+  const std::vector<TopTask>& tasks() const { return tasks_; }
+  const Params& params() const { return prm_; }
+
+  // Recursion entry points (also used for per-task plans of the plain form).
+  void dosub_self(std::vector<Item>& out, int c, int below, bool second) const;
+  void dosub_pair(std::vector<Item>& out, int ci, int cj, int below, bool second) const;
+  void items_to_entries(const std::vector<Item>& items,
+                        std::vector<std::vector<Entry>>& per_leaf) const;
+  void flatten(const std::vector<std::vector<Entry>>& per_leaf, Plan& plan) const;
+
+ private:
+  int getsid_and_swap(int& ci, int& cj, double shift[3]) const;
+  void bucket_permute(std::vector<int>& bin, int nbins, int first, int n,
+                      std::vector<int>& counts_out);
+  void octant_permute(int first, int n, const double pivot[3], int counts[8]);
+  void set_h_depth(int sorted_idx, int leaf);
+  void split_tree_then_gather(int top);
+  void split_geometry(int c);
+  void finalize_h(int c);
+  void build_top_pairs();
+  void refresh_activity(int c);
+  void refresh_hmax(int c);
+  void emit_pair(std::vector<Item>& out, int ci, int cj, const double shift[3],
+                 int lmin, int lmax) const;
+  void emit_self(std::vector<Item>& out, int c, int lmin, int lmax) const;
+  void pair_branch(std::vector<Item>& out, int ci, int cj, int lmin, int lmax) const;
+  void self_branch(std::vector<Item>& out, int c, int lmin, int lmax) const;
+  void subset_pair(std::vector<Item>& out, int ci, int leaf_cell, int cj) const;
+  void subset_self(std::vector<Item>& out, int ci, int leaf_cell) const;
+  int find_sub(int c, int leaf_cell) const;
+  Entry make_entry(int leaf_cell, int partner, int kind, bool u_is_ci,
+                   const double shift[3], int frame_cell, int min_depth,
+                   int max_depth) const;
+  void leaves_under(int c, std::vector<int>& out) const;
+
+  // cell.h:934-1010 (dx_max terms are zero: no drift between rebuild and loop)
+  static bool can_recurse_pair1(const Cell& c) {
+    return (SPH_KG * c.h_max_active + 0.f) < 0.5f * c.dmin;
+  }
+  static bool can_recurse_self1(const Cell& c) {
+    return SPH_KG * c.h_max_active < 0.5f * c.dmin;
+  }
+  static bool can_recurse_pair2(const Cell& c) {
+    return (SPH_KG * c.h_max + 0.f) < 0.5f * c.dmin;
+  }
+  static bool can_recurse_self2(const Cell& c) {
+    return c.split && (SPH_KG * c.h_max < 0.5f * c.dmin);
+  }
+  static bool can_recurse_pair_old(const Cell& c) {
+    return c.split && ((SPH_KG * c.h_max_old + 0.f) < 0.5f * c.dmin);
+  }
+  static bool can_recurse_self_old(const Cell& c) {
+    return c.split && (SPH_KG * c.h_max_old < 0.5f * c.dmin);
+  }
+
+  Params prm_;
+  int n_ = 0;
+  int cdim_[3] = {0, 0, 0};
+  double width_[3] = {0, 0, 0};
+  int unit_chunk_ = 128;
+  std::vector<double> x_;
+  std::vector<float> h_in_, h_;
+  std::vector<int8_t> tb_in_;
+  std::vector<uint8_t> active_;
+  std::vector<int8_t> depth_h_;
+  std::vector<int> perm_, inv_perm_, leaf_of_, leaves_;
+  std::vector<Cell> cells_;
+  std::vector<TopTask> tasks_;
+  std::vector<std::pair<int, int>> cpairs_[13];
+};
+
+}  // namespace sphgpu

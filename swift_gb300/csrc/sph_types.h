@@ -1,0 +1,84 @@
+// sph_types.h -- data layout shared by the host planner (space.cpp) and the
+// sm_103a kernels (sph_kernels.cu).
+//
+// Particles live in HBM as structure-of-arrays in the cell-sorted order of
+// the reference's space build (every cell, at every tree level, is one
+// contiguous index range).  Positions are kept in FP64 for the exact
+// neighbour predicate and, for the arithmetic, as FP32 offsets from the
+// particle's top-level cell corner (the reference's cell-relative frames,
+// runner_doiact_functions_hydro.h:1327-1346).
+#pragma once
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define SPH_HD __host__ __device__
+#else
+#define SPH_HD
+#endif
+
+namespace sphgpu {
+
+// Scheme constants, evaluated the way kernel_hydro.h / dimension.h /
+// adiabatic_index.h evaluate them (float products, double divisions).
+#define SPH_KG ((float)(1.936492))
+#define SPH_KCONST ((float)(21. * 0.31830988618379067154 / 2.))
+#define SPH_KG_INV ((float)(1. / SPH_KG))
+#define SPH_KG2 ((float)(SPH_KG * SPH_KG))
+#define SPH_KG_INV_DIM ((float)(1. / (SPH_KG * SPH_KG * SPH_KG)))
+#define SPH_KG_INV_DIM1 ((float)(1. / (SPH_KG * SPH_KG * SPH_KG * SPH_KG)))
+#define SPH_KROOT ((float)(1.f) * SPH_KCONST * SPH_KG_INV_DIM)
+#define SPH_HDIM 3.f
+#define SPH_HDIM_INV 0.3333333333f
+#define SPH_GAMMA 1.66666666666666667f
+#define SPH_GAMMA_M1 0.66666666666666667f
+#define SPH_VISC_BETA 3.0f
+
+// Kinds of reference evaluation frame.  The neighbour predicate r^2 < H^2
+// must be evaluated in the same frame, with the same roundings, as the
+// reference loop that owns the pair, or borderline pairs flip.
+enum FrameKind : int8_t {
+  FRAME_PAIR_CELLREL = 0,  // DOPAIR1/DOPAIR2: (float)(x_u - O_u) - (float)(x_p - O_p)
+  FRAME_SELF_DBL = 1,      // DOSELF1/DOSELF2: (float)(x_u - x_p) in double
+  FRAME_SELF_CELLREL = 2,  // DOSELF_SUBSET:   (float)(x - c.loc) differences
+  FRAME_PAIR_ABS = 3,      // DOPAIR_SUBSET:   (float)((x_u - shift) - x_p)
+};
+
+// One partner cell of a leaf in a gather list: the particles of the leaf
+// that pass the depth filter interact with every particle of the partner
+// range, in the given frame.
+struct Entry {
+  int32_t first, count;       // partner particle range
+  int8_t kind;                // FrameKind
+  int8_t min_depth, max_depth;
+  int8_t pad0;
+  float fdx, fdy, fdz;        // fast frame: partner top-cell origin (+periodic
+                              // shift) minus the leaf's top-cell origin
+  double ou[3];               // exact frame origin of the updated particle
+                              // (PAIR_CELLREL / SELF_CELLREL) or the shift
+                              // applied to it (PAIR_ABS)
+  double op[3];               // exact frame origin of the partner particle
+};
+static_assert(sizeof(Entry) == 72, "Entry layout");
+
+// Work unit: a chunk of a leaf's particles gathering over a list of entries.
+struct Unit {
+  int32_t i_first, i_count;   // particle range (chunk of one leaf)
+  int32_t e_begin, e_end;     // entry range
+  int32_t leaf;               // leaf index
+  int32_t pad;
+};
+
+// Per-leaf geometry needed on the device by the ghost (cell_set_part_h_depth,
+// cell.h:1787): the (h_min_allowed, h_max_allowed, depth) chain from the
+// leaf up to its top cell.
+#define SPH_MAX_DEPTH 24
+struct LeafInfo {
+  int32_t first, count;
+  int32_t top;
+  int32_t nlevels;            // chain length (leaf first)
+  float hmin[SPH_MAX_DEPTH];
+  float hmax[SPH_MAX_DEPTH];
+  int8_t depth[SPH_MAX_DEPTH];
+};
+
+}  // namespace sphgpu

@@ -1,0 +1,101 @@
+"""GPU parity: the sm_103a path against the oracle (oracle/sph_oracle.c,
+itself bit-identical to the reference's loops), through the C ABI.
+
+Tolerances: neighbour counts and cell assignment are compared exactly.
+Positive sums (rho, wcount, P, c, v_sig) are compared at 1e-4 relative per
+particle.  Signed sums whose terms cancel (rho_dh, wcount_dh, div_v, rot_v,
+a, du/dt, dh/dt) are compared at 1e-4 of the field's scale (its largest
+magnitude in the box): their per-particle value is a residual of cancelling
+terms, so only an absolute tolerance is meaningful -- the same convention as
+the absolute-tolerance row of the reference's tests/difffloat.py.
+h is compared within the ghost's own tolerance: two runs that converge
+independently may each stop anywhere inside the 1e-4 window around the root
+(runner_ghost.c:1388), so they differ by up to 2e-4; quantities downstream
+of h in a full pass are then compared at 1e-3 of their scale, while the
+force loop fed with the oracle's own post-ghost state is held to 1e-4.
+"""
+import numpy as np
+import pytest
+
+from swift_gb300 import api, ics
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-4
+
+
+def scaled_err(a, b):
+    """|a - b| relative to the field's scale (max |b|)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.abs(a - b) / (np.max(np.abs(b)) + 1e-30)
+
+
+def rel_err(a, b, floor_frac=1e-3):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = np.maximum(np.abs(b), floor_frac * np.max(np.abs(b)) + 1e-30)
+    return np.abs(a - b) / scale
+
+
+@pytest.fixture(scope="module", params=["lattice:16", "lattice:32", "clustered:40"])
+def case(request, oracle_lib):
+    box = ics.make(request.param, seed=5)
+    ref = oracle_lib.run(box)
+    return request.param, box, ref
+
+
+def test_first_density_pass_counts_exact(case):
+    name, box, ref = case
+    with api.Space(box) as sp:
+        sp.step(api.STAGE_DENSITY)
+        out = sp.download()
+    assert np.array_equal(out["ngb_first"], ref["ngb_first"]), name
+    for k in ("d_rho", "d_wcount"):
+        assert rel_err(out[k], ref[k]).max() < REL, (name, k)
+    for k in ("d_rho_dh", "d_wcount_dh", "d_div_v", "d_rot_vx", "d_rot_vy",
+              "d_rot_vz"):
+        assert scaled_err(out[k], ref[k]).max() < REL, (name, k)
+
+
+def test_full_pass_matches_oracle(case):
+    name, box, ref = case
+    with api.Space(box) as sp:
+        sp.step(api.STAGE_ALL)
+        out = sp.download()
+    assert rel_err(out["h"], ref["h"]).max() < 2e-4, name
+    for k in ("rho", "pressure", "soundspeed", "v_sig"):
+        assert rel_err(out[k], ref[k]).max() < 3e-4, (name, k)
+    for k in ("ax", "ay", "az", "u_dt", "h_dt", "f", "balsara"):
+        assert scaled_err(out[k], ref[k]).max() < 1e-3, (name, k)
+    # neighbour counts after independent ghosts agree except where h differs
+    # inside the tolerance window
+    assert np.mean(out["ngb_final"] == ref["ngb_final"]) > 0.99, name
+
+
+def test_force_counts_exact_from_oracle_state(case):
+    name, box, ref = case
+    with api.Space(box) as sp:
+        sp.step(api.STAGE_ALL)
+        sp.force_from_state(ref["h"], ref["rho"], ref["f"], ref["pressure"],
+                            ref["soundspeed"], ref["balsara"])
+        out = sp.download()
+    assert np.array_equal(out["ngb_force"], ref["ngb_force"]), name
+    for k in ("ax", "ay", "az", "u_dt", "h_dt"):
+        assert scaled_err(out[k], ref[k]).max() < REL, (name, k)
+    assert rel_err(out["v_sig"], ref["v_sig"]).max() < 1e-6, name
+
+
+def test_plain_equals_batched(case):
+    name, box, ref = case
+    with api.Space(box) as sp:
+        sp.step(api.STAGE_ALL)
+        a = sp.download()
+        sp.step_plain()
+        b = sp.download()
+    assert np.array_equal(a["ngb_first"], b["ngb_first"])
+    assert rel_err(b["h"], a["h"]).max() < 2e-4, name
+    for k in ("rho", "v_sig"):
+        assert rel_err(b[k], a[k]).max() < 3e-4, (name, k)
+    for k in ("ax", "ay", "az", "u_dt", "h_dt"):
+        assert scaled_err(b[k], a[k]).max() < 1e-3, (name, k)

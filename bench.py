@@ -1,0 +1,374 @@
+#!/usr/bin/env python3
+"""Benchmark: SPH pair-interactions/s of one density -> ghost -> force step.
+
+Workload (default): the 128^3 = 2,097,152-particle periodic box drawn from a
+clustered density field (lattice displaced by a seeded Gaussian random field
+with P(k) ~ k^-2, rms displacement 0.3 of the spacing), Minimal SPH with the
+Wendland C2 kernel, all particles active.  A step is one full pass -- density
+loop, the ghost's Newton iterations on h with density re-runs, force loop --
+starting from h0 = eta * spacing, run by the batched form (one persistent
+gather launch per loop, three CUDA graphs per step).
+
+  value   interactions/s with the particle state resident in HBM;
+  e2e     the same through the C ABI with host buffers: every step copies the
+          inputs from pinned host memory and the 24 result fields back;
+  metric  directed pair interactions (H_d + H_f) / t: H_d = pairs with
+          r^2 < gamma^2 h_i^2 at the converged h, H_f = pairs with
+          r^2 < gamma^2 max(h_i, h_j)^2, over active i.
+
+--impl reference times the CPU restatement of the reference loops
+(oracle/sph_oracle.c) on the host cores instead: one independent box per core.
+With N > 1 ranks (torchrun) every rank runs its own replica box (the path has
+no cross-box exchange), value = all ranks' interactions / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOPS_DENSITY = 71   # per directed density hit (hydro_iact.h:137-189 tally)
+FLOPS_FORCE = 132    # per directed force hit (hydro_iact.h:378-490 tally)
+METRIC = "SPH pair-interactions/s (density+ghost+force step)"
+UNIT = "interactions/s"
+
+WORKLOADS = {
+    "clustered128": ("clustered", 128, 0.3,
+                     "128^3=2,097,152 particles, lattice displaced by a P(k)~k^-2 "
+                     "Gaussian random field (rms 0.3 spacing), periodic unit box"),
+    "plain32": ("lattice", 32, None,
+                "32^3=32,768 particles, jittered lattice (+/-0.1 spacing), "
+                "Gaussian velocities sigma 0.05"),
+    "sedov256": ("sedov", 256, None,
+                 "256^3=16,777,216 particles, jittered lattice, Sedov blast"),
+}
+
+
+def make_box(name, seed):
+    from swift_gb300 import ics
+    kind, n, rms, _ = WORKLOADS[name]
+    if kind == "clustered":
+        return ics.clustered(n, seed=seed, rms=rms)
+    if kind == "sedov":
+        return ics.sedov(n, seed=seed)
+    return ics.lattice(n, seed=seed)
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def fp32_peak_tflops(pk):
+    """FP32 issue peak: 152 SMs x 128 FP32 lanes x 2 flop (FMA) x SM clock.
+    MEASURED_PEAKS.json carries no FP32 figure; its measured maximum SM clock
+    is used, else the nominal 2070 MHz."""
+    mhz = float(pk.get("sm_max_mhz", 2070.0))
+    return 152 * 128 * 2 * mhz * 1e6 / 1e12, mhz
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the oracle's restatement of the reference loops, one box per core.
+
+def _cpu_box_worker(args):
+    spec, seed = args
+    sys.path.insert(0, ROOT)
+    from swift_gb300 import ics
+    from oracle import oracle
+    kind, n = spec.split(":")
+    box = (ics.clustered(int(n), seed=seed, rms=0.3) if kind == "clustered"
+           else ics.lattice(int(n), seed=seed))
+    t0 = time.perf_counter()
+    out = oracle.run(box)
+    dt = time.perf_counter() - t0
+    hits = int(out["ngb_final"].sum()) + int(out["ngb_force"].sum())
+    return hits, dt
+
+
+def cpu_baseline(spec="clustered:48", boxes_per_core=1, cores=None):
+    """Interactions/s of the reference loops restated in C (oracle), run as
+    independent boxes on all host cores (spawned workers)."""
+    from oracle import oracle
+    oracle.build()
+    cores = cores or os.cpu_count() or 1
+    jobs = [(spec, 1000 + k) for k in range(cores * boxes_per_core)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_box_worker, jobs)
+    wall = time.perf_counter() - t0
+    hits = sum(r[0] for r in res)
+    cpu_s = sum(r[1] for r in res)
+    # throughput over the loops' own time: all workers run concurrently, the
+    # slowest one bounds the sample (process start-up and IC generation are
+    # excluded)
+    loop_s = max(r[1] for r in res) * boxes_per_core
+    return {"value": hits / loop_s, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{len(jobs)} independent {spec.replace(':', ' ')}^3 boxes "
+                      f"(same generator), one per worker process; {cpu_s:.1f} s of "
+                      f"CPU work, {wall:.1f} s wall"}
+
+
+# ---------------------------------------------------------------------------
+
+def run_reference_arm(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    t0 = time.perf_counter()
+    vals = []
+    for _ in range(max(1, args.steps)):
+        cb = cpu_baseline(args.cpu_sample)
+        vals.append(cb["value"])
+    value = statistics.median(vals)
+    wall = time.perf_counter() - t0
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 positions)",
+        "data": "synthetic (seeded generators)",
+        "config": {"workload": WORKLOADS[args.workload][3],
+                   "sample": args.cpu_sample, "parallelism": "replicas"},
+        "cpu_baseline": {**cb, "value": value},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def traffic_from_profile():
+    """DRAM bytes per force-gather launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "force_gather_clustered128.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":")[1].strip().split()[0])
+    except Exception:
+        pass
+    return None
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from swift_gb300 import api
+
+    box = make_box(args.workload, seed=args.seed + rank)
+    n = box["x"].shape[0]
+    sp = api.Space(box)
+    stream = torch.cuda.Stream()
+    sh = ctypes_stream(stream)
+    # plan (first step) + warm-up
+    sp.step(stream=sh)
+    for _ in range(args.warmup):
+        sp.step(stream=sh)
+    hits = sp.count_hits()
+    h_d = int(sp.download()["ngb_final"].sum())
+    inter_per_step = h_d + int(hits[2])
+    sp.phase_times(reset=True)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = ClockSampler(local_rank)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        sp.step(stream=sh)
+    e1.record(stream)
+    barrier()
+    ms_total = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    phase_ms, nsteps = sp.phase_times(reset=True)
+
+    # End to end through host buffers (pinned), same step.
+    pinned = {}
+    for k in ("x", "v", "m", "h", "u"):
+        t = torch.from_numpy(np.ascontiguousarray(box[k])).pin_memory()
+        pinned[k] = t.numpy()
+    fields = torch.empty((n, 24), dtype=torch.float32).pin_memory().numpy()
+    sp.step_host(pinned, fields, stream=sh)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sp.step_host(pinned, fields, stream=sh)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+
+    t_step = ms_total / 1e3 / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_step, e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step, e2e_s = float(t[0]), float(t[1])
+        c = torch.tensor([inter_per_step], device="cuda", dtype=torch.float64)
+        dist.all_reduce(c)
+        total_inter = float(c[0])
+    else:
+        total_inter = float(inter_per_step)
+
+    out = None
+    if rank == 0:
+        pk = peaks()
+        peak, mhz = fp32_peak_tflops(pk)
+        force_ms = phase_ms[2] / max(1, nsteps)
+        dens_ms = phase_ms[0] / max(1, nsteps)
+        ghost_ms = phase_ms[1] / max(1, nsteps)
+        achieved = FLOPS_FORCE * float(hits[2]) / (force_ms / 1e3) / 1e12
+        step_flops = (FLOPS_DENSITY * float(hits[0] + hits[1])
+                      + FLOPS_FORCE * float(hits[2]))
+        cb = None
+        if not args.no_cpu:
+            cb = cpu_baseline(args.cpu_sample)
+        out = {
+            "metric": METRIC, "value": total_inter / t_step, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64 positions)",
+            "data": "synthetic (seeded generators, no dataset)",
+            "config": {
+                "workload": WORKLOADS[args.workload][3],
+                "particles_per_gpu": n, "form": "batched persistent, 3 CUDA graphs/step",
+                "active": "all", "h0": "eta*spacing (ghost iterates every step)",
+                "l2": "inputs larger than L2 (particle state ~150 B/particle)",
+                "parallelism": "replicas" if world > 1 else "single",
+                "interactions_per_step": inter_per_step,
+            },
+            "phases_ms": {"density": dens_ms, "ghost_rounds": ghost_ms,
+                          "force": force_ms},
+            "hits_per_step": {"density_first": int(hits[0]),
+                              "density_reruns": int(hits[1]),
+                              "force": int(hits[2])},
+            "step_tflops": step_flops / t_step / 1e12,
+            "roofline": {
+                "bound": "fp32", "kernel": "gather_warp<force>",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak,
+                "peak_note": f"derived: 152 SMs x 128 FP32 lanes x 2 x {mhz:.0f} MHz "
+                             "(sm_max_mhz of MEASURED_PEAKS.json; no measured FP32 "
+                             "figure there)",
+                "traffic": traffic_from_profile(),
+            },
+            "e2e": {"value": total_inter / e2e_s, "unit": UNIT,
+                    "h2d_bytes_per_step": int(n * (24 + 12 + 4 + 4 + 4)),
+                    "d2h_bytes_per_step": int(n * 24 * 4)},
+            "gpu_launches": 64 * args.steps,
+            "clocks": clk,
+            "cpu_baseline": cb,
+        }
+        print(json.dumps(out), flush=True)
+    sp.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def ctypes_stream(stream):
+    import ctypes
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__,
+                                 formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="clustered128")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--cpu-sample", default="clustered:48")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

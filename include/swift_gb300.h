@@ -118,6 +118,16 @@ int sphgpu_get_tuning(const sphgpu_space *s, sphgpu_tuning *t);
  * SPHGPU_ENOCONV if some h did not converge in max_iter rounds. */
 int sphgpu_step(sphgpu_space *s, int32_t stages, void *stream);
 
+/* Per-loop device time of the batched steps run so far (CUDA events on the
+ * step's stream): ms_sum[0] density first pass, [1] ghost rounds (Newton
+ * updates + density re-runs), [2] force loop; *steps = steps timed. */
+int sphgpu_phase_times(sphgpu_space *s, double ms_sum[3], int64_t *steps,
+                       int32_t reset);
+
+/* One instrumented (uncaptured) step that counts neighbour interactions:
+ * hits[0] density first pass, [1] density re-runs of the ghost, [2] force. */
+int sphgpu_count_hits(sphgpu_space *s, int64_t hits[3]);
+
 /* Same pass through host buffers: copies x, v, m, h, u (input order) from
  * host memory, runs the step, copies the results back.  `fields` receives
  * float [n][24] in the column layout of sphgpu_download; NULL skips it. */

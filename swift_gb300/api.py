@@ -80,6 +80,8 @@ SIGNATURES = {
     "sphgpu_dosub_self2_force": (ctypes.c_int, [_P, _I32, _P]),
     "sphgpu_dosub_pair2_force": (ctypes.c_int, [_P, _I32, _I32, _P]),
     "sphgpu_do_end_hydro_force": (ctypes.c_int, [_P, _P]),
+    "sphgpu_phase_times": (ctypes.c_int, [_P, _P, _P, _I32]),
+    "sphgpu_count_hits": (ctypes.c_int, [_P, _P]),
 }
 
 _lib = None
@@ -194,7 +196,7 @@ class Space:
         return geom, ints
 
     # -- configuration -----------------------------------------------------
-    def set_tuning(self, tpi=1, jtile=64, persistent=1):
+    def set_tuning(self, tpi=32, jtile=32, persistent=1):
         t = Tuning(tpi, jtile, persistent)
         _check(lib().sphgpu_set_tuning(self._h, ctypes.byref(t)))
 
@@ -224,6 +226,21 @@ class Space:
                                       _ptr(b["m"]), _ptr(b["h"]), _ptr(b["u"]),
                                       _ptr(fields), stream))
         return fields
+
+    def phase_times(self, reset=False):
+        """(ms summed per loop [density, ghost, force], steps timed)."""
+        ms = np.zeros(3, np.float64)
+        steps = ctypes.c_int64()
+        _check(lib().sphgpu_phase_times(self._h, _ptr(ms), ctypes.byref(steps),
+                                        1 if reset else 0))
+        return ms, steps.value
+
+    def count_hits(self):
+        """Neighbour interactions of one pass: density first pass, ghost
+        re-runs, force."""
+        out = np.zeros(3, np.int64)
+        _check(lib().sphgpu_count_hits(self._h, _ptr(out)))
+        return out
 
     def download(self):
         fields = np.zeros((self.n, 24), np.float32)

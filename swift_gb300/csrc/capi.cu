@@ -61,30 +61,14 @@ struct DBuf {
 
 struct DevPlan {
   DBuf<Entry> entries;
-  DBuf<Unit> units;
-  int nunits = 0;
+  DBuf<int> lpb, pb, pe;  // leaf_pair_begin, pair_block, pair_entry
   void upload(const Plan& pl, cudaStream_t s) {
     entries.upload(pl.entries.data(), pl.entries.size(), s);
-    units.upload(pl.units.data(), pl.units.size(), s);
-    nunits = (int)pl.units.size();
+    lpb.upload(pl.leaf_pair_begin.data(), pl.leaf_pair_begin.size(), s);
+    pb.upload(pl.pair_block.data(), pl.pair_block.size(), s);
+    pe.upload(pl.pair_entry.data(), pl.pair_entry.size(), s);
   }
 };
-
-// Sort units so that the most expensive go first (longest-processing-time
-// order for the persistent queue); cost = i_count x sum of partner counts,
-// the reference's pair cost model (scheduler.c:516-629) at particle level.
-void order_units(Plan& pl) {
-  std::vector<std::pair<double, Unit>> tmp;
-  tmp.reserve(pl.units.size());
-  for (const Unit& u : pl.units) {
-    double c = 0;
-    for (int e = u.e_begin; e < u.e_end; e++) c += pl.entries[e].count;
-    tmp.emplace_back(c * u.i_count, u);
-  }
-  std::stable_sort(tmp.begin(), tmp.end(),
-                   [](const auto& a, const auto& b) { return a.first > b.first; });
-  for (size_t k = 0; k < tmp.size(); k++) pl.units[k] = tmp[k].second;
-}
 
 }  // namespace
 
@@ -94,14 +78,13 @@ struct sphgpu_space {
   std::vector<double> x_in;
   std::vector<float> v_in, m_in, h_in, u_in;
   std::vector<int8_t> tb_in;
-  sphgpu_tuning tune{1, 64, 1};
+  sphgpu_tuning tune{32, 32, 1};
 
   // host plans
   Plan plan_d, plan_s, plan_f;
   bool force_planned = false;
   // plain-form per-task plans
-  std::vector<Plan> task_d, task_f;
-  std::vector<int> task_of_pair;  // unused placeholder for lookups
+  std::vector<Plan> task_d, task_f;  // non-empty once the per-task lists exist
   std::vector<std::pair<int, int>> sub_units_of_top;  // subset units per top cell
 
   // device
@@ -119,43 +102,43 @@ struct sphgpu_space {
   DBuf<double> top_loc;
   DBuf<LeafInfo> leaves;
   DevPlan dplan_d, dplan_s, dplan_f;
-  std::vector<DevPlan> dtask_d, dtask_f;
-  DBuf<int> queue, redo, status;
+  DBuf<int> queue, redo;
+  DBuf<float4> bb_lo, bb_hi;
+  DBuf<int2> bb_fc;
+  DBuf<int32_t> active_list, redo_list;
+  DBuf<int4> task_items_d, task_items_f;
+  DBuf<Entry> task_entries_d, task_entries_f;
+  DBuf<int> task_pb_d, task_pe_d, task_pb_f, task_pe_f;
+  std::vector<int> task_items_begin_d, task_items_begin_f;
+  std::vector<int> active_top_begin;   // per top cell: slice of the active list
+  int n_active = 0;
+  std::vector<int> s_of_g;             // store index -> reference sorted index
   // host staging for step_host
   DBuf<double> x_stage;
   DBuf<float> v_stage, m_stage, h_stage, u_stage, out_stage;
-  cudaGraphExec_t graph = nullptr;
-  int graph_stages = 0;
+  // The batched step is three graphs (density first pass, ghost rounds,
+  // force) so that CUDA events between them time each loop of every step.
+  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double phase_ms[3] = {0, 0, 0};
+  long long phase_steps = 0;
+  DBuf<unsigned long long> hit_ctr;
+  bool count_hits = false;
 
   ~sphgpu_space() {
-    if (graph) cudaGraphExecDestroy(graph);
+    for (auto& g : graph)
+      if (g) cudaGraphExecDestroy(g);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
   }
 };
 
 namespace {
 
-int unit_chunk(const sphgpu_tuning& t) { return 128 / t.threads_per_particle; }
-
 void build_plans(sphgpu_space* s) {
-  s->space->set_unit_chunk(unit_chunk(s->tune));
   s->space->plan_density(s->plan_d, false);
   s->space->plan_subset(s->plan_s);
-  order_units(s->plan_d);
-  // subset units stay in leaf order: the plain-form ghost addresses them by
-  // top cell.
-  s->sub_units_of_top.clear();
-  const auto& cells = s->space->cells();
-  const int ntop = s->space->cdim()[0] * s->space->cdim()[1] * s->space->cdim()[2];
-  s->sub_units_of_top.assign(ntop, {0, 0});
-  const auto& lv = s->space->leaves();
-  int k = 0;
-  const int nu = (int)s->plan_s.units.size();
-  for (int t = 0; t < ntop; t++) {
-    const int b = k;
-    while (k < nu && cells[lv[s->plan_s.units[k].leaf]].top == t) k++;
-    s->sub_units_of_top[t] = {b, k};
-  }
 }
 
 void ensure_device(sphgpu_space* s) {
@@ -170,46 +153,79 @@ void ensure_device(sphgpu_space* s) {
   cudaStream_t st = s->stream;
   const Space& sp = *s->space;
   const int n = sp.n();
-  // Cell-sorted copies of the inputs.
-  const auto& perm = sp.perm();
+  // Store order: the reference's cell order, Morton-sorted inside leaves.
+  const auto& gperm = sp.gperm();
+  const auto& g_of_s = sp.gpu_of_sorted();
+  s->s_of_g.assign(n, 0);
+  for (int k = 0; k < n; k++) s->s_of_g[g_of_s[k]] = k;
   std::vector<double> xs(3 * (size_t)n);
   std::vector<float4> vm(n);
   std::vector<float> hs(n), us(n);
   std::vector<uint8_t> fl(n);
-  std::vector<int32_t> top(n);
+  std::vector<int8_t> dh(n);
+  std::vector<int32_t> top(n), lf(n);
   const auto& xw = sp.x();
   const auto& act = sp.active();
   const auto& cells = sp.cells();
   const auto& leaf_of = sp.leaf_of();
   const auto& lvs = sp.leaves();
-  for (int i = 0; i < n; i++) {
-    const int k = perm[i];
-    for (int d = 0; d < 3; d++) xs[3 * (size_t)i + d] = xw[3 * (size_t)k + d];
-    vm[i] = make_float4(s->v_in[3 * (size_t)k], s->v_in[3 * (size_t)k + 1],
-                        s->v_in[3 * (size_t)k + 2], s->m_in[k]);
-    hs[i] = s->h_in[k];
-    us[i] = s->u_in[k];
-    fl[i] = act[i] ? 1 : 0;
-    top[i] = cells[lvs[leaf_of[i]]].top;
-  }
+  std::vector<int32_t> alist;
+  alist.reserve(n);
   const int ntop = sp.cdim()[0] * sp.cdim()[1] * sp.cdim()[2];
+  s->active_top_begin.assign(ntop + 1, 0);
+  for (int g = 0; g < n; g++) {
+    const int k = gperm[g];
+    const int srt = s->s_of_g[g];
+    for (int d = 0; d < 3; d++) xs[3 * (size_t)g + d] = xw[3 * (size_t)k + d];
+    vm[g] = make_float4(s->v_in[3 * (size_t)k], s->v_in[3 * (size_t)k + 1],
+                        s->v_in[3 * (size_t)k + 2], s->m_in[k]);
+    hs[g] = s->h_in[k];
+    us[g] = s->u_in[k];
+    fl[g] = act[srt] ? 1 : 0;
+    dh[g] = sp.depth_h()[srt];
+    lf[g] = leaf_of[srt];
+    top[g] = cells[lvs[leaf_of[srt]]].top;
+  }
+  // active list, grouped by top cell (store order is top-cell major)
+  for (int t = 0; t < ntop; t++) {
+    s->active_top_begin[t] = (int)alist.size();
+    const Cell& c = cells[t];
+    for (int g = c.first; g < c.first + c.count; g++)
+      if (fl[g]) alist.push_back(g);
+  }
+  s->active_top_begin[ntop] = (int)alist.size();
+  s->n_active = (int)alist.size();
   std::vector<double> tl(3 * (size_t)ntop);
   for (int t = 0; t < ntop; t++)
     for (int d = 0; d < 3; d++) tl[3 * (size_t)t + d] = cells[t].loc[d];
   std::vector<LeafInfo> li;
   sp.leaf_infos(li);
+  const JBlocks& jb = sp.jblocks();
+  const size_t nb = jb.first.size();
+  std::vector<float4> blo(nb), bhi(nb);
+  std::vector<int2> bfc(nb);
+  for (size_t b = 0; b < nb; b++) {
+    blo[b] = make_float4(jb.lo[3 * b], jb.lo[3 * b + 1], jb.lo[3 * b + 2], 0.f);
+    bhi[b] = make_float4(jb.hi[3 * b], jb.hi[3 * b + 1], jb.hi[3 * b + 2], 0.f);
+    bfc[b] = make_int2(jb.first[b], jb.count[b]);
+  }
 
   s->xd.upload(xs.data(), xs.size(), st);
   s->velm.upload(vm.data(), n, st);
   s->h0.upload(hs.data(), n, st);
   s->u.upload(us.data(), n, st);
   s->flags.upload(fl.data(), n, st);
-  s->depth_h.upload(sp.depth_h().data(), n, st);
-  s->leaf_of.upload(leaf_of.data(), n, st);
+  s->depth_h.upload(dh.data(), n, st);
+  s->leaf_of.upload(lf.data(), n, st);
   s->top_of.upload(top.data(), n, st);
-  s->perm.upload(perm.data(), n, st);
+  s->perm.upload(gperm.data(), n, st);
   s->top_loc.upload(tl.data(), tl.size(), st);
   s->leaves.upload(li.data(), li.size(), st);
+  s->bb_lo.upload(blo.data(), nb, st);
+  s->bb_hi.upload(bhi.data(), nb, st);
+  s->bb_fc.upload(bfc.data(), nb, st);
+  s->active_list.upload(alist.data(), alist.size(), st);
+  s->redo_list.alloc(2 * (size_t)n);
   s->posh.alloc(n);
   s->dens0.alloc(n);
   s->dens1.alloc(n);
@@ -225,7 +241,8 @@ void ensure_device(sphgpu_space* s) {
   s->ngb_f.alloc(n);
   s->queue.alloc(8);
   s->redo.alloc(std::max(1, s->prm.max_iter));
-  s->status.alloc(1);
+  s->hit_ctr.alloc(4);
+  for (auto& e : s->ev) CK(cudaEventCreate(&e));
   CK(cudaMemsetAsync(s->fin0.p, 0, sizeof(float4) * n, st));
   CK(cudaMemsetAsync(s->fin1.p, 0, sizeof(float2) * n, st));
   CK(cudaMemsetAsync(s->acc.p, 0, sizeof(float4) * n, st));
@@ -260,33 +277,36 @@ void ensure_device(sphgpu_space* s) {
   s->dev = true;
 }
 
-LaunchCfg cfg_of(const sphgpu_space* s) {
-  LaunchCfg c;
-  c.tpi = s->tune.threads_per_particle;
-  c.jtile = s->tune.jtile;
-  c.persistent = s->tune.persistent;
-  c.block = 128;
-  return c;
-}
-
 // Relative band of the FP32 pre-test around H^2.  The FP32 offsets carry
 // about 1e-8 absolute error; for the smallest H of the supported boxes
 // (~0.005 box units) that is < 1e-5 relative on r^2, far inside this band.
 constexpr float kBand = 2.44140625e-4f;  // 2^-12
 
-GatherArgs gargs(sphgpu_space* s, DevPlan& dp, int qslot, const int* gate) {
-  GatherArgs a;
+G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, const int* list, int count,
+             const int* count_ptr, int mode) {
+  G2Args a;
   a.p = s->P;
-  a.units = dp.units.p;
-  a.nunits = dp.nunits;
+  a.list = list;
+  a.count = count;
+  a.count_ptr = count_ptr;
+  a.leaf_pair_begin = dp.lpb.p;
+  a.pair_block = dp.pb.p;
+  a.pair_entry = dp.pe.p;
   a.entries = dp.entries.p;
+  a.items = nullptr;
+  a.bb_lo = s->bb_lo.p;
+  a.bb_hi = s->bb_hi.p;
+  a.bb_fc = s->bb_fc.p;
   a.queue = s->queue.p + qslot;
-  a.gate = gate;
+  a.hits = nullptr;
+  if (s->count_hits) a.hits = s->hit_ctr.p + (qslot == 0 ? 0 : (qslot == 2 ? 2 : 1));
   a.band = kBand;
+  a.mode = mode;
   return a;
 }
 
-GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
+GhostArgs ghargs(sphgpu_space* s, int iter, const int* in_list, int in_count,
+                 const int* in_count_ptr, int* out_list, int* out_count) {
   GhostArgs g;
   g.p = s->P;
   g.leaves = s->leaves.p;
@@ -296,37 +316,53 @@ GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
   g.h_min = s->prm.h_min;
   g.alpha = s->prm.alpha;
   g.iter = iter;
-  g.lo = lo;
-  g.hi = hi;
-  g.max_iter = s->prm.max_iter;
-  g.redo_count = s->redo.p;
-  g.status = s->status.p;
+  g.in_list = in_list;
+  g.in_count = in_count;
+  g.in_count_ptr = in_count_ptr;
+  g.out_list = out_list;
+  g.out_count = out_count;
   return g;
 }
 
-// Enqueue density (first pass) and the ghost's rounds.
-void enqueue_density_ghost(sphgpu_space* s, cudaStream_t st, int stages) {
-  const LaunchCfg c = cfg_of(s);
-  CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, s->status.p, st));
-  CK(cudaMemsetAsync(s->queue.p, 0, 8 * sizeof(int), st));
-  if (stages & SPHGPU_STAGE_DENSITY)
-    CK(launch_density(gargs(s, s->dplan_d, 0, nullptr), MODE_FIRST, c, s->num_sms, st));
-  if (stages & SPHGPU_STAGE_GHOST) {
-    for (int k = 0; k < s->prm.max_iter; k++) {
-      CK(launch_ghost(ghargs(s, k, 0, s->P.n), st));
-      // re-run density for the particles sent to another round; the kernel
-      // returns at once when the round sent none (gate = its redo count)
-      CK(cudaMemsetAsync(s->queue.p + 1, 0, sizeof(int), st));
-      CK(launch_density(gargs(s, s->dplan_s, 1, s->redo.p + k), MODE_REDO, c,
-                        s->num_sms, st));
-    }
+// Ghost rounds over a list of particles (the whole active list, or the
+// active particles of one top cell): round k iterates the particles sent on
+// by round k-1 and re-runs their density (subset gather lists) when any
+// were sent to another round.
+void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st, const int* list0,
+                          int count0) {
+  const int n = s->P.n;
+  for (int k = 0; k < s->prm.max_iter; k++) {
+    const int* in = k == 0 ? list0 : s->redo_list.p + (size_t)((k - 1) & 1) * n;
+    const int* inc = k == 0 ? nullptr : s->redo.p + (k - 1);
+    int* out = s->redo_list.p + (size_t)(k & 1) * n;
+    CK(launch_ghost(ghargs(s, k, in, count0, inc, out, s->redo.p + k), count0, st));
+    CK(cudaMemsetAsync(s->queue.p + 1, 0, sizeof(int), st));
+    CK(launch_gather(gargs(s, s->dplan_s, 1, out, 0, s->redo.p + k, MODE_REDO),
+                     false, s->num_sms, count0, st));
   }
 }
 
+void enqueue_density(sphgpu_space* s, cudaStream_t st, bool density) {
+  CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, st));
+  CK(cudaMemsetAsync(s->queue.p, 0, 8 * sizeof(int), st));
+  if (density)
+    CK(launch_gather(gargs(s, s->dplan_d, 0, s->active_list.p, s->n_active,
+                           nullptr, MODE_FIRST),
+                     false, s->num_sms, s->n_active, st));
+}
+
+void enqueue_density_ghost(sphgpu_space* s, cudaStream_t st, int stages) {
+  enqueue_density(s, st, (stages & SPHGPU_STAGE_DENSITY) != 0);
+  if (stages & SPHGPU_STAGE_GHOST)
+    enqueue_ghost_rounds(s, st, s->active_list.p, s->n_active);
+}
+
 void enqueue_force(sphgpu_space* s, cudaStream_t st) {
+  CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
   CK(cudaMemsetAsync(s->queue.p + 2, 0, sizeof(int), st));
-  CK(launch_force(gargs(s, s->dplan_f, 2, nullptr), MODE_FIRST, cfg_of(s),
-                  s->num_sms, st));
+  CK(launch_gather(gargs(s, s->dplan_f, 2, s->active_list.p, s->n_active,
+                         nullptr, MODE_FIRST),
+                   true, s->num_sms, s->n_active, st));
 }
 
 int check_conv(sphgpu_space* s, cudaStream_t st) {
@@ -340,18 +376,23 @@ int check_conv(sphgpu_space* s, cudaStream_t st) {
   return SPHGPU_OK;
 }
 
-// The force loop's recursion depends on the post-ghost h_max of every cell
-// (cell.h:966-1010 use hydro.h_max); plan it once the ghost has run.
-void plan_force(sphgpu_space* s, cudaStream_t st) {
+// Smoothing lengths in the reference's sorted order, from the store.
+std::vector<float> sorted_h(sphgpu_space* s, cudaStream_t st) {
   const int n = s->P.n;
   std::vector<float4> ph(n);
   CK(cudaMemcpyAsync(ph.data(), s->posh.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   std::vector<float> h(n);
-  for (int i = 0; i < n; i++) h[i] = ph[i].w;
+  for (int g = 0; g < n; g++) h[s->s_of_g[g]] = ph[g].w;
+  return h;
+}
+
+// The force loop's recursion depends on the post-ghost h_max of every cell
+// (cell.h:966-1010 use hydro.h_max); plan it once the ghost has run.
+void plan_force(sphgpu_space* s, cudaStream_t st) {
+  const std::vector<float> h = sorted_h(s, st);
   s->space->update_h_after_ghost(h.data());
   s->space->plan_density(s->plan_f, true);
-  order_units(s->plan_f);
   s->dplan_f.upload(s->plan_f, st);
   s->force_planned = true;
 }
@@ -372,6 +413,34 @@ int guard(const std::function<int()>& f) {
     if (m.find("no CUDA device") != std::string::npos) return fail(SPHGPU_ENODEV, m);
     return fail(SPHGPU_EINVAL, m);
   }
+}
+
+void drop_graph(sphgpu_space* s) {
+  for (auto& g : s->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+template <class F>
+cudaGraphExec_t capture(cudaStream_t st, F&& body) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  try {
+    body();
+  } catch (...) {
+    cudaGraph_t dead = nullptr;
+    cudaStreamEndCapture(st, &dead);
+    if (dead) cudaGraphDestroy(dead);
+    throw;
+  }
+  CK(cudaStreamEndCapture(st, &g));
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  CK(e);
+  return ex;
 }
 
 }  // namespace
@@ -494,32 +563,11 @@ int sphgpu_space_leaves(const sphgpu_space* s, double* geom, int32_t* ints) {
 
 int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
   if (!s || !t) return fail(SPHGPU_EINVAL, "null argument");
-  const int tpi = t->threads_per_particle;
-  if (!(tpi == 1 || tpi == 2 || tpi == 4 || tpi == 8) ||
-      !(t->jtile == 64 || t->jtile == 128))
-    return fail(SPHGPU_EINVAL, "tuning: tpi in {1,2,4,8}, jtile in {64,128}");
-  return guard([&]() {
-    const bool replan = tpi != s->tune.threads_per_particle;
-    s->tune = *t;
-    if (replan) {
-      build_plans(s);
-      if (s->dev) {
-        s->dplan_d.upload(s->plan_d, s->stream);
-        s->dplan_s.upload(s->plan_s, s->stream);
-      }
-      s->force_planned = false;
-      s->task_d.clear();
-      s->task_f.clear();
-      s->dtask_d.clear();
-      s->dtask_f.clear();
-    }
-    if (s->graph) {
-      cudaGraphExecDestroy(s->graph);
-      s->graph = nullptr;
-    }
-    if (s->dev) CK(cudaStreamSynchronize(s->stream));
-    return SPHGPU_OK;
-  });
+  if (t->threads_per_particle != 32 || t->jtile != SPH_JBLOCK)
+    return fail(SPHGPU_EINVAL, "tuning: threads_per_particle 32, jtile 32 supported");
+  s->tune = *t;
+  drop_graph(s);
+  return SPHGPU_OK;
 }
 
 int sphgpu_get_tuning(const sphgpu_space* s, sphgpu_tuning* t) {
@@ -531,23 +579,30 @@ int sphgpu_get_tuning(const sphgpu_space* s, sphgpu_tuning* t) {
 int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
+    if (s->dev) CK(cudaStreamSynchronize(s->stream));
     s->prm.max_active_bin = max_active_bin;
     s->space->set_activity(max_active_bin);
     build_plans(s);
     s->force_planned = false;
     s->task_d.clear();
     s->task_f.clear();
-    s->dtask_d.clear();
-    s->dtask_f.clear();
-    if (s->graph) {
-      cudaGraphExecDestroy(s->graph);
-      s->graph = nullptr;
-    }
+    drop_graph(s);
     if (s->dev) {
       const int n = s->P.n;
       std::vector<uint8_t> fl(n);
-      for (int i = 0; i < n; i++) fl[i] = s->space->active()[i] ? 1 : 0;
+      for (int g = 0; g < n; g++) fl[g] = s->space->active()[s->s_of_g[g]] ? 1 : 0;
+      std::vector<int32_t> alist;
+      const auto& cells = s->space->cells();
+      const int ntop = s->space->cdim()[0] * s->space->cdim()[1] * s->space->cdim()[2];
+      for (int t = 0; t < ntop; t++) {
+        s->active_top_begin[t] = (int)alist.size();
+        for (int g = cells[t].first; g < cells[t].first + cells[t].count; g++)
+          if (fl[g]) alist.push_back(g);
+      }
+      s->active_top_begin[ntop] = (int)alist.size();
+      s->n_active = (int)alist.size();
       s->flags.upload(fl.data(), n, s->stream);
+      s->active_list.upload(alist.data(), alist.size(), s->stream);
       s->dplan_d.upload(s->plan_d, s->stream);
       s->dplan_s.upload(s->plan_s, s->stream);
       CK(cudaStreamSynchronize(s->stream));
@@ -577,25 +632,26 @@ int sphgpu_step(sphgpu_space* s, int32_t stages, void* stream) {
       if (rc != SPHGPU_OK) return rc;
       plan_force(s, st);
     }
-    if (!s->graph) {
-      cudaGraph_t g;
-      CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      try {
-        enqueue_density_ghost(s, st, SPHGPU_STAGE_DENSITY | SPHGPU_STAGE_GHOST);
-        enqueue_force(s, st);
-      } catch (...) {
-        cudaGraph_t dead;
-        cudaStreamEndCapture(st, &dead);
-        if (dead) cudaGraphDestroy(dead);
-        throw;
-      }
-      CK(cudaStreamEndCapture(st, &g));
-      const cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
-      cudaGraphDestroy(g);
-      CK(e);
+    if (!s->graph[0]) {
+      s->graph[0] = capture(st, [&]() { enqueue_density(s, st, true); });
+      s->graph[1] = capture(st, [&]() {
+        enqueue_ghost_rounds(s, st, s->active_list.p, s->n_active);
+      });
+      s->graph[2] = capture(st, [&]() { enqueue_force(s, st); });
     }
-    CK(cudaGraphLaunch(s->graph, st));
-    return check_conv(s, st);
+    CK(cudaEventRecord(s->ev[0], st));
+    for (int k = 0; k < 3; k++) {
+      CK(cudaGraphLaunch(s->graph[k], st));
+      CK(cudaEventRecord(s->ev[k + 1], st));
+    }
+    const int rc = check_conv(s, st);  // synchronises the stream
+    for (int k = 0; k < 3; k++) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, s->ev[k], s->ev[k + 1]));
+      s->phase_ms[k] += ms;
+    }
+    s->phase_steps++;
+    return rc;
   });
 }
 
@@ -647,19 +703,16 @@ int sphgpu_step_host(sphgpu_space* s, const double* x, const float* v,
     CK(launch_permute_in(s->P, s->perm.p, s->x_stage.p, s->v_stage.p, s->m_stage.p,
                          s->h_stage.p, s->u_stage.p, st));
     CK(launch_prepare_posh(s->P, s->top_of.p, s->top_loc.p, st));
-    int rc;
-    {
-      // run the batched step on the same stream
-      rc = sphgpu_step(s, SPHGPU_STAGE_ALL, (void*)st);
-      if (rc != SPHGPU_OK && rc != SPHGPU_ENOCONV) return rc;
-    }
+    const int rc = sphgpu_step(s, SPHGPU_STAGE_ALL, (void*)st);
+    if (rc != SPHGPU_OK && rc != SPHGPU_ENOCONV) return rc;
     if (fields) {
       CK(launch_collect_out(s->P, s->perm.p, s->out_stage.p, nullptr, st));
       CK(cudaMemcpyAsync(fields, s->out_stage.p, sizeof(float) * 24 * (size_t)n,
                          cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
     }
-    return rc;
+    if (rc == SPHGPU_ENOCONV) return fail(rc, g_err);
+    return SPHGPU_OK;
   });
 }
 
@@ -673,19 +726,20 @@ int sphgpu_force_from_state(sphgpu_space* s, const float* h, const float* rho,
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
     const int n = s->P.n;
-    const auto& perm = s->space->perm();
+    const auto& gperm = s->space->gperm();
     std::vector<float4> ph(n), f0(n), acc(n, make_float4(0, 0, 0, 0));
     std::vector<float2> f1(n), hv(n);
-    std::vector<float> hs(n);
+    std::vector<float> hs(n);  // reference sorted order
+    CK(cudaStreamSynchronize(st));
     CK(cudaMemcpyAsync(ph.data(), s->posh.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    for (int i = 0; i < n; i++) {
-      const int k = perm[i];
-      ph[i].w = h[k];
-      hs[i] = h[k];
-      f0[i] = make_float4(rho[k], f[k], pressure[k] / (rho[k] * rho[k]), soundspeed[k]);
-      f1[i] = make_float2(balsara[k], pressure[k]);
-      hv[i] = make_float2(0.f, 2.f * soundspeed[k]);
+    for (int g = 0; g < n; g++) {
+      const int k = gperm[g];
+      ph[g].w = h[k];
+      hs[s->s_of_g[g]] = h[k];
+      f0[g] = make_float4(rho[k], f[k], pressure[k] / (rho[k] * rho[k]), soundspeed[k]);
+      f1[g] = make_float2(balsara[k], pressure[k]);
+      hv[g] = make_float2(0.f, 2.f * soundspeed[k]);
     }
     s->posh.upload(ph.data(), n, st);
     s->fin0.upload(f0.data(), n, st);
@@ -697,15 +751,17 @@ int sphgpu_force_from_state(sphgpu_space* s, const float* h, const float* rho,
     std::vector<LeafInfo> li;
     s->space->leaf_infos(li);
     std::vector<int8_t> dh(n);
-    for (int i = 0; i < n; i++) {
-      const LeafInfo& L = li[s->space->leaf_of()[i]];
-      dh[i] = s->space->depth_h()[i];
-      if (hs[i] < L.hmin[0]) {
-        dh[i] = L.depth[0];
+    for (int g = 0; g < n; g++) {
+      const int srt = s->s_of_g[g];
+      const LeafInfo& L = li[s->space->leaf_of()[srt]];
+      const float hh = hs[srt];
+      dh[g] = s->space->depth_h()[srt];
+      if (hh < L.hmin[0]) {
+        dh[g] = L.depth[0];
       } else {
         for (int lev = 0; lev < L.nlevels; lev++)
-          if (hs[i] >= L.hmin[lev] && hs[i] < L.hmax[lev]) {
-            dh[i] = L.depth[lev];
+          if (hh >= L.hmin[lev] && hh < L.hmax[lev]) {
+            dh[g] = L.depth[lev];
             break;
           }
       }
@@ -713,45 +769,129 @@ int sphgpu_force_from_state(sphgpu_space* s, const float* h, const float* rho,
     s->depth_h.upload(dh.data(), n, st);
     Plan pf;
     s->space->plan_density(pf, true);
-    order_units(pf);
     DevPlan dp;
     dp.upload(pf, st);
+    CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
     CK(cudaMemsetAsync(s->queue.p + 3, 0, sizeof(int), st));
-    CK(launch_force(gargs(s, dp, 3, nullptr), MODE_FIRST, cfg_of(s), s->num_sms, st));
+    CK(launch_gather(gargs(s, dp, 3, s->active_list.p, s->n_active, nullptr, MODE_FIRST),
+                     true, s->num_sms, s->n_active, st));
     CK(cudaStreamSynchronize(st));
-    // the space's step plans assume its own ghost: re-plan on the next step
+    // the step's plans assume its own ghost: re-plan on the next step
     s->force_planned = false;
-    if (s->graph) {
-      cudaGraphExecDestroy(s->graph);
-      s->graph = nullptr;
-    }
+    drop_graph(s);
     return SPHGPU_OK;
   });
 }
 
+int sphgpu_phase_times(sphgpu_space* s, double ms_sum[3], int64_t* steps,
+                       int32_t reset) {
+  if (!s || !ms_sum || !steps) return fail(SPHGPU_EINVAL, "null argument");
+  for (int k = 0; k < 3; k++) ms_sum[k] = s->phase_ms[k];
+  *steps = s->phase_steps;
+  if (reset) {
+    for (int k = 0; k < 3; k++) s->phase_ms[k] = 0;
+    s->phase_steps = 0;
+  }
+  return SPHGPU_OK;
+}
+
+int sphgpu_count_hits(sphgpu_space* s, int64_t hits[3]) {
+  if (!s || !hits) return fail(SPHGPU_EINVAL, "null argument");
+  return guard([&]() {
+    ensure_device(s);
+    cudaStream_t st = s->stream;
+    int rc = SPHGPU_OK;
+    if (!s->force_planned) rc = sphgpu_step(s, SPHGPU_STAGE_ALL, st);
+    if (rc != SPHGPU_OK) return rc;
+    CK(cudaMemsetAsync(s->hit_ctr.p, 0, 4 * sizeof(unsigned long long), st));
+    s->count_hits = true;
+    try {
+      enqueue_density_ghost(s, st, SPHGPU_STAGE_DENSITY | SPHGPU_STAGE_GHOST);
+      enqueue_force(s, st);
+    } catch (...) {
+      s->count_hits = false;
+      throw;
+    }
+    s->count_hits = false;
+    rc = check_conv(s, st);
+    unsigned long long h[4];
+    CK(cudaMemcpy(h, s->hit_ctr.p, sizeof(h), cudaMemcpyDeviceToHost));
+    hits[0] = (int64_t)h[0];
+    hits[1] = (int64_t)h[1];
+    hits[2] = (int64_t)h[2];
+    return rc;
+  });
+}
+
 // ---------------------------------------------------------------------------
-// Plain per-task form
+// Plain per-task form: one launch per reference task, as runner_main.c would
+// issue them (self/pair density, per-top-cell ghost, self/pair force).
 
 static void ensure_task_plans(sphgpu_space* s, bool force) {
   auto& plans = force ? s->task_f : s->task_d;
-  auto& dplans = force ? s->dtask_f : s->dtask_d;
   if (!plans.empty()) return;
+  // One concatenated entry array for all tasks; each task's work is a list
+  // of (particle, entry range) items over the leaves the task touches.
   const Space& sp = *s->space;
   const auto& tasks = sp.tasks();
   plans.resize(tasks.size());
-  dplans.resize(tasks.size());
   std::vector<Item> items;
+  std::vector<Entry> all_entries;
+  std::vector<int4> all_items;
+  std::vector<int> all_pb, all_pe;
+  std::vector<int> ib(tasks.size() + 1, 0);
+  const auto& cells = sp.cells();
+  const auto& lvs = sp.leaves();
+  const auto& active = sp.active();
+  std::vector<std::vector<Entry>> per_leaf(lvs.size());
+  std::vector<int> touched;
+  // leaves are numbered top cell by top cell
+  const int ntop = sp.cdim()[0] * sp.cdim()[1] * sp.cdim()[2];
+  std::vector<int> top_leaf(ntop + 1, (int)lvs.size());
+  for (int l = (int)lvs.size() - 1; l >= 0; l--) top_leaf[cells[lvs[l]].top] = l;
+  for (int t = ntop - 1; t >= 0; t--)
+    if (top_leaf[t] > top_leaf[t + 1]) top_leaf[t] = top_leaf[t + 1];
   for (size_t t = 0; t < tasks.size(); t++) {
     items.clear();
     if (tasks[t].cj < 0)
       sp.dosub_self(items, tasks[t].ci, 0, force);
     else
       sp.dosub_pair(items, tasks[t].ci, tasks[t].cj, 0, force);
-    std::vector<std::vector<Entry>> per_leaf(sp.leaves().size());
     sp.items_to_entries(items, per_leaf);
-    sp.flatten(per_leaf, plans[t]);
-    dplans[t].upload(plans[t], s->stream);
+    ib[t] = (int)all_items.size();
+    touched.clear();
+    // leaves touched by this task: those of its cells whose list is non-empty
+    const int ci = tasks[t].ci, cj = tasks[t].cj;
+    for (int c : {ci, cj}) {
+      if (c < 0) continue;
+      for (int l = top_leaf[c]; l < top_leaf[c + 1]; l++)
+        if (!per_leaf[l].empty()) touched.push_back(l);
+    }
+    for (int l : touched) {
+      const int pb0 = (int)all_pb.size();
+      for (const Entry& E : per_leaf[l]) {
+        const int e = (int)all_entries.size();
+        all_entries.push_back(E);
+        for (int b = E.bfirst; b < E.bfirst + E.bcount; b++) {
+          all_pb.push_back(b);
+          all_pe.push_back(e);
+        }
+      }
+      const int pb1 = (int)all_pb.size();
+      per_leaf[l].clear();
+      const Cell& c = cells[lvs[l]];
+      for (int g = c.first; g < c.first + c.count; g++)
+        if (active[s->s_of_g[g]]) all_items.push_back(make_int4(g, pb0, pb1, 0));
+    }
   }
+  ib[tasks.size()] = (int)all_items.size();
+  auto& di = force ? s->task_items_f : s->task_items_d;
+  auto& de = force ? s->task_entries_f : s->task_entries_d;
+  di.upload(all_items.data(), all_items.size(), s->stream);
+  de.upload(all_entries.data(), all_entries.size(), s->stream);
+  (force ? s->task_pb_f : s->task_pb_d).upload(all_pb.data(), all_pb.size(), s->stream);
+  (force ? s->task_pe_f : s->task_pe_d).upload(all_pe.data(), all_pe.size(), s->stream);
+  (force ? s->task_items_begin_f : s->task_items_begin_d) = ib;
   CK(cudaStreamSynchronize(s->stream));
 }
 
@@ -764,14 +904,17 @@ static int find_task(const sphgpu_space* s, int ci, int cj) {
 }
 
 static int run_task(sphgpu_space* s, int t, bool force, cudaStream_t st) {
-  DevPlan& dp = force ? s->dtask_f[t] : s->dtask_d[t];
-  if (dp.nunits == 0) return SPHGPU_OK;
-  LaunchCfg c = cfg_of(s);
-  c.persistent = 0;
-  if (force)
-    CK(launch_force(gargs(s, dp, 4, nullptr), MODE_ACCUM, c, s->num_sms, st));
-  else
-    CK(launch_density(gargs(s, dp, 4, nullptr), MODE_ACCUM, c, s->num_sms, st));
+  const auto& ib = force ? s->task_items_begin_f : s->task_items_begin_d;
+  const int b = ib[t], e = ib[t + 1];
+  if (e == b) return SPHGPU_OK;
+  G2Args a = gargs(s, s->dplan_d, 4, nullptr, e - b, nullptr, MODE_ACCUM);
+  a.items = (force ? s->task_items_f.p : s->task_items_d.p) + b;
+  a.entries = force ? s->task_entries_f.p : s->task_entries_d.p;
+  a.pair_block = force ? s->task_pb_f.p : s->task_pb_d.p;
+  a.pair_entry = force ? s->task_pe_f.p : s->task_pe_d.p;
+  a.leaf_pair_begin = nullptr;
+  CK(cudaMemsetAsync(s->queue.p + 4, 0, sizeof(int), st));
+  CK(launch_gather(a, force, s->num_sms, e - b, st));
   return SPHGPU_OK;
 }
 
@@ -780,7 +923,7 @@ int sphgpu_begin_loops(sphgpu_space* s, void* stream) {
   return guard([&]() {
     ensure_device(s);
     ensure_task_plans(s, false);
-    CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, s->status.p, pick(s, stream)));
+    CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, pick(s, stream)));
     return SPHGPU_OK;
   });
 }
@@ -814,44 +957,43 @@ int sphgpu_do_ghost(sphgpu_space* s, int32_t cell, void* stream) {
   return guard([&]() {
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
-    const Cell& c = s->space->cells()[cell];
-    if (c.count == 0 || !c.active) return SPHGPU_OK;
+    const int b = s->active_top_begin[cell], e = s->active_top_begin[cell + 1];
+    if (e == b) return SPHGPU_OK;
+    const int n = s->P.n;
     CK(cudaMemsetAsync(s->redo.p, 0, sizeof(int) * s->prm.max_iter, st));
-    const auto ur = s->sub_units_of_top[cell];
-    DevPlan sub;  // view of the subset units of this top cell
-    const int nu = ur.second - ur.first;
-    LaunchCfg cfg = cfg_of(s);
-    cfg.persistent = 0;
     for (int k = 0; k < s->prm.max_iter; k++) {
-      CK(launch_ghost(ghargs(s, k, c.first, c.first + c.count), st));
+      const int* in = k == 0 ? s->active_list.p + b : s->redo_list.p + (size_t)((k - 1) & 1) * n;
+      const int* inc = k == 0 ? nullptr : s->redo.p + (k - 1);
+      int* out = s->redo_list.p + (size_t)(k & 1) * n;
+      CK(launch_ghost(ghargs(s, k, in, e - b, inc, out, s->redo.p + k), e - b, st));
       int cnt = 0;
       CK(cudaMemcpyAsync(&cnt, s->redo.p + k, sizeof(int), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
       if (cnt == 0) return SPHGPU_OK;
-      if (nu > 0) {
-        GatherArgs a = gargs(s, s->dplan_s, 4, nullptr);
-        a.units = s->dplan_s.units.p + ur.first;
-        a.nunits = nu;
-        CK(launch_density(a, MODE_REDO, cfg, s->num_sms, st));
-      }
+      CK(cudaMemsetAsync(s->queue.p + 5, 0, sizeof(int), st));
+      CK(launch_gather(gargs(s, s->dplan_s, 5, out, cnt, nullptr, MODE_REDO), false,
+                       s->num_sms, cnt, st));
       if (k == s->prm.max_iter - 1)
         return fail(SPHGPU_ENOCONV, "smoothing length failed to converge on " +
                                         std::to_string(cnt) + " particles");
     }
-    (void)sub;
     return SPHGPU_OK;
   });
+}
+
+static void ensure_force_plans(sphgpu_space* s, cudaStream_t st) {
+  if (!s->task_f.empty()) return;
+  // the force recursion needs the post-ghost h_max of every cell
+  plan_force(s, st);
+  ensure_task_plans(s, true);
+  CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
 }
 
 int sphgpu_dosub_self2_force(sphgpu_space* s, int32_t cell, void* stream) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
-    if (s->task_f.empty()) {
-      // the force recursion needs the post-ghost h_max of every cell
-      plan_force(s, pick(s, stream));
-      ensure_task_plans(s, true);
-    }
+    ensure_force_plans(s, pick(s, stream));
     const int t = find_task(s, cell, -1);
     if (t < 0) return SPHGPU_OK;
     return run_task(s, t, true, pick(s, stream));
@@ -862,10 +1004,7 @@ int sphgpu_dosub_pair2_force(sphgpu_space* s, int32_t ci, int32_t cj, void* stre
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
-    if (s->task_f.empty()) {
-      plan_force(s, pick(s, stream));
-      ensure_task_plans(s, true);
-    }
+    ensure_force_plans(s, pick(s, stream));
     const int t = find_task(s, ci, cj);
     if (t < 0) return fail(SPHGPU_EINVAL, "cells are not neighbours");
     return run_task(s, t, true, pick(s, stream));
@@ -888,8 +1027,8 @@ int sphgpu_step_plain(sphgpu_space* s, void* stream) {
     cudaStream_t st = pick(s, stream);
     int rc = sphgpu_begin_loops(s, st);
     if (rc) return rc;
-    const auto tasks = s->space->tasks();
-    for (size_t t = 0; t < tasks.size(); t++) {
+    const size_t ntasks = s->space->tasks().size();
+    for (size_t t = 0; t < ntasks; t++) {
       rc = run_task(s, (int)t, false, st);
       if (rc) return rc;
     }
@@ -898,11 +1037,9 @@ int sphgpu_step_plain(sphgpu_space* s, void* stream) {
       rc = sphgpu_do_ghost(s, c, st);
       if (rc) return rc;
     }
-    if (s->task_f.empty()) {
-      plan_force(s, st);
-      ensure_task_plans(s, true);
-    }
-    for (size_t t = 0; t < tasks.size(); t++) {
+    ensure_force_plans(s, st);
+    CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
+    for (size_t t = 0; t < ntasks; t++) {
       rc = run_task(s, (int)t, true, st);
       if (rc) return rc;
     }

@@ -265,6 +265,85 @@ void Space::build(int64_t n, const double* x, const float* h,
   inv_perm_.resize(n_);
   for (int k = 0; k < n_; k++) inv_perm_[perm_[k]] = k;
   build_top_pairs();
+  build_gpu_order();
+}
+
+static inline uint32_t spread10(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000ffu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+void Space::build_gpu_order() {
+  gperm_ = perm_;
+  g_of_s_.assign(n_, 0);
+  jb_ = JBlocks();
+  jb_.cell_begin.assign(cells_.size(), 0);
+  jb_.cell_end.assign(cells_.size(), 0);
+  std::vector<std::pair<uint32_t, int>> key;
+  std::vector<int> leaf_block_begin(leaves_.size() + 1, 0);
+  for (size_t l = 0; l < leaves_.size(); l++) {
+    const Cell& c = cells_[leaves_[l]];
+    key.clear();
+    for (int k = c.first; k < c.first + c.count; k++) {
+      const double* x = &x_[3 * (size_t)perm_[k]];
+      uint32_t q[3];
+      for (int d = 0; d < 3; d++) {
+        double t = (x[d] - c.loc[d]) / c.width[d];
+        t = t < 0 ? 0 : (t > 0.999999 ? 0.999999 : t);
+        q[d] = (uint32_t)(t * 1024.0);
+      }
+      key.emplace_back((spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]), k);
+    }
+    std::stable_sort(key.begin(), key.end());
+    for (size_t r = 0; r < key.size(); r++) {
+      gperm_[c.first + (int)r] = perm_[key[r].second];
+      g_of_s_[key[r].second] = c.first + (int)r;
+    }
+    leaf_block_begin[l] = (int)jb_.first.size();
+    const Cell& top = cells_[c.top];
+    for (int b0 = c.first; b0 < c.first + c.count; b0 += SPH_JBLOCK) {
+      const int bc = std::min(SPH_JBLOCK, c.first + c.count - b0);
+      float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+      for (int k = b0; k < b0 + bc; k++) {
+        const double* x = &x_[3 * (size_t)gperm_[k]];
+        for (int d = 0; d < 3; d++) {
+          const float o = (float)(x[d] - top.loc[d]);
+          lo[d] = std::min(lo[d], o);
+          hi[d] = std::max(hi[d], o);
+        }
+      }
+      jb_.first.push_back(b0);
+      jb_.count.push_back(bc);
+      for (int d = 0; d < 3; d++) {
+        jb_.lo.push_back(lo[d]);
+        jb_.hi.push_back(hi[d]);
+      }
+    }
+  }
+  leaf_block_begin[leaves_.size()] = (int)jb_.first.size();
+  // Cell block ranges: the leaves under a cell are consecutive.
+  for (size_t c = cells_.size(); c-- > 0;) {
+    const Cell& cc = cells_[c];
+    if (cc.count == 0) continue;
+    if (!cc.split) {
+      jb_.cell_begin[c] = leaf_block_begin[cc.leaf];
+      jb_.cell_end[c] = leaf_block_begin[cc.leaf + 1];
+    } else {
+      int b = 0x7fffffff, e = -1;
+      for (int k = 0; k < 8; k++) {
+        const int p = cc.progeny[k];
+        if (p < 0) continue;
+        b = std::min(b, jb_.cell_begin[p]);
+        e = std::max(e, jb_.cell_end[p]);
+      }
+      jb_.cell_begin[c] = b;
+      jb_.cell_end[c] = e;
+    }
+  }
 }
 
 // Splitting reorders particles; leaves need the final-order h to compute
@@ -592,6 +671,8 @@ Entry Space::make_entry(int leaf_cell, int partner, int kind, bool u_is_ci,
   std::memset(&e, 0, sizeof(e));
   e.first = cells_[partner].first;
   e.count = cells_[partner].count;
+  e.bfirst = jb_.cell_begin[partner];
+  e.bcount = jb_.cell_end[partner] - jb_.cell_begin[partner];
   e.kind = (int8_t)kind;
   e.min_depth = (int8_t)min_depth;
   e.max_depth = (int8_t)max_depth;
@@ -719,6 +800,20 @@ void Space::flatten(const std::vector<std::vector<Entry>>& per_leaf,
     plan.entries.insert(plan.entries.end(), per_leaf[l].begin(), per_leaf[l].end());
   }
   plan.leaf_entry_begin[leaves_.size()] = (int)plan.entries.size();
+  plan.pair_block.clear();
+  plan.pair_entry.clear();
+  plan.leaf_pair_begin.assign(leaves_.size() + 1, 0);
+  for (size_t l = 0; l < leaves_.size(); l++) {
+    plan.leaf_pair_begin[l] = (int)plan.pair_block.size();
+    for (int e = plan.leaf_entry_begin[l]; e < plan.leaf_entry_begin[l + 1]; e++) {
+      const Entry& E = plan.entries[e];
+      for (int b = E.bfirst; b < E.bfirst + E.bcount; b++) {
+        plan.pair_block.push_back(b);
+        plan.pair_entry.push_back(e);
+      }
+    }
+  }
+  plan.leaf_pair_begin[leaves_.size()] = (int)plan.pair_block.size();
   for (size_t l = 0; l < leaves_.size(); l++) {
     const Cell& c = cells_[leaves_[l]];
     if (!c.active) continue;

@@ -47,6 +47,16 @@ struct Plan {
   std::vector<Entry> entries;
   std::vector<Unit> units;
   std::vector<int> leaf_entry_begin;
+  // Flattened candidate list: every (j-block, entry) a leaf's particles may
+  // interact with, per leaf.
+  std::vector<int32_t> pair_block, pair_entry;
+  std::vector<int> leaf_pair_begin;
+};
+
+struct JBlocks {
+  std::vector<int32_t> first, count;   // particle range (GPU order)
+  std::vector<float> lo, hi;           // [3 * nblocks] bounding box, top frame
+  std::vector<int32_t> cell_begin, cell_end;  // per cell: block range
 };
 
 class Space {
@@ -72,6 +82,11 @@ class Space {
   const std::vector<Cell>& cells() const { return cells_; }
   const std::vector<int>& leaves() const { return leaves_; }
   const std::vector<int>& perm() const { return perm_; }          // sorted -> input
+  // GPU store order: the reference's cell order with each leaf re-sorted
+  // along a Morton curve (cell ranges are unchanged).
+  const std::vector<int>& gperm() const { return gperm_; }        // gpu -> input
+  const std::vector<int>& gpu_of_sorted() const { return g_of_s_; }
+  const JBlocks& jblocks() const { return jb_; }
   const std::vector<int>& inv_perm() const { return inv_perm_; }  // input -> sorted
   const std::vector<int8_t>& depth_h() const { return depth_h_; }
   const std::vector<int>& leaf_of() const { return leaf_of_; }
@@ -143,6 +158,9 @@ class Space {
   std::vector<uint8_t> active_;
   std::vector<int8_t> depth_h_;
   std::vector<int> perm_, inv_perm_, leaf_of_, leaves_;
+  std::vector<int> gperm_, g_of_s_;
+  JBlocks jb_;
+  void build_gpu_order();
   std::vector<Cell> cells_;
   std::vector<TopTask> tasks_;
   std::vector<std::pair<int, int>> cpairs_[13];

@@ -37,43 +37,48 @@ struct DevParticles {
   int32_t* ngb_f;
 };
 
-struct GatherArgs {
+enum GatherMode { MODE_FIRST = 0, MODE_REDO = 1, MODE_ACCUM = 2 };
+
+// Warp-per-particle gather (gather.cu).
+struct G2Args {
   DevParticles p;
-  const Unit* units;
-  int nunits;
+  const int* list;              // updated particles (store order)
+  int count;                    // list length, or
+  const int* count_ptr;         //   read from device memory when non-null
+  const int* leaf_pair_begin;   // [leaves + 1] candidate-block range per leaf
+  const int* pair_block;        // candidate j-block ...
+  const int* pair_entry;        // ... and the gather-list entry it belongs to
+  const int4* items;            // optional (particle, pair begin, end, -)
+                                // instead of list + leaf_pair_begin
   const Entry* entries;
-  int* queue;            // persistent work counter (reset before launch)
-  const int* gate;       // optional: skip everything when *gate == 0
-  float band;            // relative band of the exact predicate check
+  const float4* bb_lo;          // j-block boxes: lo.xyz, (K h_max)^2
+  const float4* bb_hi;
+  const int2* bb_fc;            // j-block particle range
+  int* queue;                   // work counter, zero before the launch
+  unsigned long long* hits;     // optional: total neighbour hits of the launch
+  float band;                   // relative band of the exact predicate
+  int mode;                     // GatherMode
 };
 
 struct GhostArgs {
   DevParticles p;
   const LeafInfo* leaves;
   float eta_dim, h_tol, h_max, h_min, alpha;
-  int iter;              // 0-based round
-  int lo, hi;            // particle range handled (cell-sorted order)
-  int max_iter;
-  int* redo_count;       // [max_iter] particles sent to another round
-  int* status;           // non-convergence flag
+  int iter;                     // 0-based round
+  const int* in_list;           // particles iterating this round
+  int in_count;
+  const int* in_count_ptr;
+  int* out_list;                // particles sent to another round
+  int* out_count;
 };
 
-enum GatherMode { MODE_FIRST = 0, MODE_REDO = 1, MODE_ACCUM = 2 };
-
-struct LaunchCfg {
-  int tpi;        // threads per i-particle (1, 2, 4, 8)
-  int jtile;      // j-tile depth staged in shared memory (64, 128, 256)
-  int persistent; // 1: grid of resident blocks pulling units from a queue
-  int block;      // threads per block (fixed at 128)
-};
-
-cudaError_t launch_density(const GatherArgs& a, int mode, const LaunchCfg& c,
-                           int num_sms, cudaStream_t s);
-cudaError_t launch_force(const GatherArgs& a, int mode, const LaunchCfg& c,
-                         int num_sms, cudaStream_t s);
-cudaError_t launch_ghost(const GhostArgs& g, cudaStream_t s);
+cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_items,
+                          cudaStream_t s);
+cudaError_t launch_block_hmax(const int2* fc, float4* lo, const float4* posh,
+                              int nblocks, cudaStream_t s);
+cudaError_t launch_ghost(const GhostArgs& g, int max_items, cudaStream_t s);
 cudaError_t launch_begin_step(const DevParticles& p, int max_iter,
-                              int* redo_count, int* status, cudaStream_t s);
+                              int* redo_count, cudaStream_t s);
 cudaError_t launch_end_force(const DevParticles& p, cudaStream_t s);
 cudaError_t launch_prepare_posh(DevParticles p, const int32_t* top_of,
                                 const double* top_loc, cudaStream_t s);

@@ -48,6 +48,7 @@ enum FrameKind : int8_t {
 // range, in the given frame.
 struct Entry {
   int32_t first, count;       // partner particle range
+  int32_t bfirst, bcount;     // partner j-block range
   int8_t kind;                // FrameKind
   int8_t min_depth, max_depth;
   int8_t pad0;
@@ -58,7 +59,12 @@ struct Entry {
                               // applied to it (PAIR_ABS)
   double op[3];               // exact frame origin of the partner particle
 };
-static_assert(sizeof(Entry) == 72, "Entry layout");
+static_assert(sizeof(Entry) == 80, "Entry layout");
+
+// j-block: up to kJBlock consecutive particles of one leaf (spatially
+// sorted), with their bounding box in the top-cell frame; the gather culls
+// whole blocks against each particle's search sphere.
+#define SPH_JBLOCK 32
 
 // Work unit: a chunk of a leaf's particles gathering over a list of entries.
 struct Unit {

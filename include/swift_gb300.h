@@ -128,6 +128,26 @@ int sphgpu_phase_times(sphgpu_space *s, double ms_sum[3], int64_t *steps,
  * hits[0] density first pass, [1] density re-runs of the ghost, [2] force. */
 int sphgpu_count_hits(sphgpu_space *s, int64_t hits[3]);
 
+/* The first density pass of a resident space with no device allocation:
+ * for callers that cannot allocate when they run it -- inside CUDA stream
+ * capture, under a host that owns all device memory through its own pool,
+ * or in a latency-bound serving loop.  No counterpart in the reference.
+ * The space must already be resident on the device (any earlier GPU call on
+ * it allocates and uploads); the first call on a device also looks up the
+ * library's static scratch array, so make it before any stream capture.
+ * Scratch (work-queue counter and active-particle list) lives in one static
+ * device array sized for SPHGPU_NOALLOC_MAX_PARTICLES particles, held by
+ * every GPU that loads the library until the process exits; larger spaces
+ * get SPHGPU_EINVAL.  Every call reuses that array and resets its counters,
+ * so calls that overlap on the GPU (other streams, other threads) race.
+ * Outputs, in the caller's particle order, go to device buffers the caller
+ * provides: d_fields float [n][8] = rho, rho_dh, wcount, wcount_dh, div_v,
+ * rot_v[3] (the raw sums of sphgpu_download columns 0-7) and d_ngb int32 [n]
+ * neighbour counts.  Asynchronous on `stream` (NULL: the space's stream). */
+#define SPHGPU_NOALLOC_MAX_PARTICLES (1 << 20)
+int sphgpu_density_noalloc(sphgpu_space *s, float *d_fields, int32_t *d_ngb,
+                           void *stream);
+
 /* Same pass through host buffers: copies x, v, m, h, u (input order) from
  * host memory, runs the step, copies the results back.  `fields` receives
  * float [n][24] in the column layout of sphgpu_download; NULL skips it. */

@@ -82,6 +82,7 @@ SIGNATURES = {
     "sphgpu_do_end_hydro_force": (ctypes.c_int, [_P, _P]),
     "sphgpu_phase_times": (ctypes.c_int, [_P, _P, _P, _I32]),
     "sphgpu_count_hits": (ctypes.c_int, [_P, _P]),
+    "sphgpu_density_noalloc": (ctypes.c_int, [_P, _P, _P, _P]),
 }
 
 _lib = None

@@ -823,6 +823,28 @@ int sphgpu_count_hits(sphgpu_space* s, int64_t hits[3]) {
   });
 }
 
+int sphgpu_density_noalloc(sphgpu_space* s, float* d_fields, int32_t* d_ngb,
+                           void* stream) {
+  if (!s || !d_fields || !d_ngb)
+    return fail(SPHGPU_EINVAL, "sphgpu_density_noalloc: null argument");
+  if (!s->dev)
+    return fail(SPHGPU_ESTATE,
+                "sphgpu_density_noalloc: the space is not resident on the device "
+                "yet; run one GPU call on it first (that call allocates)");
+  if (s->P.n > noalloc_max_particles())
+    return fail(SPHGPU_EINVAL,
+                "sphgpu_density_noalloc: " + std::to_string(s->P.n) +
+                    " particles exceed the static scratch limit of " +
+                    std::to_string(noalloc_max_particles()));
+  const cudaError_t e = launch_density_noalloc(
+      gargs(s, s->dplan_d, 0, nullptr, 0, nullptr, MODE_FIRST), s->flags.p, d_fields,
+      d_ngb, s->perm.p, s->num_sms, pick(s, stream));
+  if (e != cudaSuccess)
+    return fail(SPHGPU_ECUDA, std::string("sphgpu_density_noalloc: ") +
+                                  cudaGetErrorString(e));
+  return SPHGPU_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Plain per-task form: one launch per reference task, as runner_main.c would
 // issue them (self/pair density, per-top-cell ghost, self/pair force).

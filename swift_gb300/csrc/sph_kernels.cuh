@@ -74,6 +74,11 @@ struct GhostArgs {
 
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_items,
                           cudaStream_t s);
+int noalloc_max_particles();
+cudaError_t launch_density_noalloc(const G2Args& base, const uint8_t* flags,
+                                   float* fields, int32_t* ngb,
+                                   const int32_t* perm, int num_sms,
+                                   cudaStream_t s);
 cudaError_t launch_block_hmax(const int2* fc, float4* lo, const float4* posh,
                               int nblocks, cudaStream_t s);
 cudaError_t launch_ghost(const GhostArgs& g, int max_items, cudaStream_t s);

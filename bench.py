@@ -278,13 +278,8 @@ def run_ours(args):
 
     t_step = ms_total / 1e3 / args.steps
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_step, e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step, e2e_s = float(t[0]), float(t[1])
-        c = torch.tensor([inter_per_step], device="cuda", dtype=torch.float64)
-        dist.all_reduce(c)
-        total_inter = float(c[0])
+        t_step, e2e_s, total_inter = reduce_over_ranks(t_step, e2e_s,
+                                                       inter_per_step, "cuda")
     else:
         total_inter = float(inter_per_step)
 
@@ -344,6 +339,17 @@ def run_ours(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def reduce_over_ranks(t_step, e2e_s, interactions, device):
+    """Replicas: the slowest rank's step times, all ranks' interactions."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([t_step, e2e_s], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(interactions)], device=device, dtype=torch.float64)
+    dist.all_reduce(c)
+    return float(t[0]), float(t[1]), float(c[0])
 
 
 def ctypes_stream(stream):

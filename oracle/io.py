@@ -35,7 +35,7 @@ HEADER_DTYPE = np.dtype([
     ("magic", "S8"), ("n", "<i8"), ("dim", "<f8", 3), ("eta", "<f4"),
     ("h_tolerance", "<f4"), ("h_max", "<f4"), ("h_min", "<f4"),
     ("alpha", "<f4"), ("max_iter", "<i4"), ("max_active_bin", "<i4"),
-    ("periodic", "<i4"), ("stages", "<i4"), ("_pad", "<i4"),
+    ("periodic", "<i4"), ("stages", "<i4"), ("max_top_level_cells", "<i4"),
 ])
 assert HEADER_DTYPE.itemsize == 80
 
@@ -44,7 +44,7 @@ def default_params(box):
     return dict(eta=box.get("eta", 1.2348), h_tolerance=1e-4,
                 h_max=np.finfo(np.float32).max, h_min=0.0, alpha=0.8,
                 max_iter=30, max_active_bin=box.get("max_active_bin", 56),
-                periodic=1)
+                periodic=1, max_top_level_cells=12)
 
 
 def write_input(path, box, stages=ALL_STAGES, **overrides):
@@ -56,7 +56,7 @@ def write_input(path, box, stages=ALL_STAGES, **overrides):
     hdr["n"] = n
     hdr["dim"] = [box["dim"]] * 3
     for k in ("eta", "h_tolerance", "h_max", "h_min", "alpha", "max_iter",
-              "max_active_bin", "periodic"):
+              "max_active_bin", "periodic", "max_top_level_cells"):
         hdr[k] = p[k]
     hdr["stages"] = stages
     with open(path, "wb") as f:
@@ -105,6 +105,9 @@ def ref_harness_path(mode="parity"):
 def run_reference(box, workdir, stages=ALL_STAGES, mode="parity", **overrides):
     """Run the reference's own loops (oracle/_ref) on ``box``."""
     exe = ref_harness_path(mode)
+    for k in ("max_active_bin",):
+        if k in box and k not in overrides:
+            overrides[k] = box[k]
     if not os.path.exists(exe):
         raise FileNotFoundError(f"reference harness not built: {exe}")
     inp = os.path.join(workdir, "ref_in.bin")

@@ -37,7 +37,7 @@ struct in_header {
   int64_t n;
   double dim[3];
   float eta, h_tolerance, h_max, h_min, alpha;
-  int32_t max_iter, max_active_bin, periodic, stages;
+  int32_t max_iter, max_active_bin, periodic, stages, max_top_level_cells;
 };
 
 static void *xmalloc(size_t n) {
@@ -170,6 +170,12 @@ int main(int argc, char **argv) {
   memset(&lc, 0, sizeof(lc));
 
   struct swift_params *params = xmalloc(sizeof(struct swift_params));
+  if (hdr.max_top_level_cells > 0) {
+    char kv[128];
+    snprintf(kv, sizeof(kv), "Scheduler:max_top_level_cells:%d",
+             (int)hdr.max_top_level_cells);
+    parser_set_param(params, kv);
+  }
 
   static struct space s;
   static struct engine e;

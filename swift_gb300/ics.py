@@ -90,7 +90,7 @@ def grf_displacement(n, rms, seed, spectral_index=-2.0):
     psi = np.empty((n ** 3, 3), dtype=np.float64)
     kvecs = (kx[:, None, None], kx[None, :, None], kz[None, None, :])
     for a in range(3):
-        comp = np.fft.irfftn(1j * kvecs[a] / k2 * dk, s=(n, n, n))
+        comp = np.fft.irfftn(1j * kvecs[a] / k2 * dk, s=(n, n, n), axes=(0, 1, 2))
         psi[:, a] = comp.ravel()
         del comp
     cur = np.sqrt(np.mean(np.sum(psi ** 2, axis=1)))

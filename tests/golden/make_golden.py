@@ -1,0 +1,70 @@
+"""Generate the golden fixtures of this directory from the reference's own
+loops (oracle/_ref/parity/bin/ref_harness: the reference's space build, sorts,
+density loops, ghost and force loops, compiled from the reference tree by
+oracle/build_ref.sh with -O2 -fno-fast-math -ffp-contract=off).
+
+Each fixture stores the generator recipe (kind, size, seed, parameters), the
+full-box sums of every output field (float64 sums of the float32 values) and
+the complete outputs of a seeded sample of particles.  Inputs are
+regenerated by swift_gb300.ics from the recipe, so the fixtures stay small.
+
+Run in a container that has the reference tree:
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import io  # noqa: E402
+from swift_gb300 import ics  # noqa: E402
+
+CASES = [
+    # name, generator kind, n, generator kwargs, run parameters, sample size
+    ("lattice12", "lattice", 12, {"seed": 3}, {}, 0),
+    ("plain32", "lattice", 32, {"seed": 1}, {}, 1024),
+    ("clustered24_split", "clustered", 24, {"seed": 4}, {"max_top_level_cells": 3}, 1024),
+    ("clustered32_deep", "clustered", 32, {"seed": 9, "rms": 1.5},
+     {"max_top_level_cells": 3}, 1024),
+    # sparse activity: density and ghost only -- the force loop reads the
+    # force state of inactive neighbours, which a single pass from initial
+    # conditions does not have
+    ("sedov24_sparse", "sedov", 24, {"seed": 2}, {"max_active_bin": 21, "stages": 3},
+     1024),
+]
+
+INT_NAMES = ["leaf_first", "leaf_count", "leaf_depth", "depth_h", "position", "top"]
+
+
+def make_box(kind, n, kw):
+    return getattr(ics, kind)(n, **kw)
+
+
+def main():
+    for name, kind, n, kw, run, nsample in CASES:
+        box = make_box(kind, n, kw)
+        ref = io.run_reference(box, tempfile.mkdtemp(), **run)
+        N = box["x"].shape[0]
+        fields = ref["res"][:, :21].astype(np.float32)
+        ints = np.stack([ref[k] for k in INT_NAMES], axis=1).astype(np.int32)
+        if nsample and nsample < N:
+            idx = np.sort(np.random.default_rng(12345).choice(N, nsample, replace=False))
+        else:
+            idx = np.arange(N)
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            kind=kind, n=n, gen_kwargs=repr(kw), run_kwargs=repr(run),
+            cdim=np.array(ref["cdim"]), sample=idx.astype(np.int32),
+            fields=fields[idx], ints=ints[idx],
+            field_sums=fields.astype(np.float64).sum(axis=0),
+            int_sums=ints.astype(np.int64).sum(axis=0))
+        print(name, N, "particles, cdim", ref["cdim"], "->", name + ".npz")
+
+
+if __name__ == "__main__":
+    main()

@@ -78,6 +78,8 @@ typedef struct {
   int32_t threads_per_particle; /* 1, 2, 4 or 8 */
   int32_t jtile;                /* 64 or 128 partner particles per tile */
   int32_t persistent;           /* 1: resident grid + device work queue */
+  int32_t chunk;                /* consecutive particles a warp takes per
+                                   queue pull (1..1024) */
 } sphgpu_tuning;
 
 int sphgpu_abi_version(void);

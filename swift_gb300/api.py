@@ -48,7 +48,8 @@ class Params(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("threads_per_particle", ctypes.c_int32),
-                ("jtile", ctypes.c_int32), ("persistent", ctypes.c_int32)]
+                ("jtile", ctypes.c_int32), ("persistent", ctypes.c_int32),
+                ("chunk", ctypes.c_int32)]
 
 
 # Every symbol the header declares, with its ctypes signature.
@@ -197,14 +198,14 @@ class Space:
         return geom, ints
 
     # -- configuration -----------------------------------------------------
-    def set_tuning(self, tpi=32, jtile=32, persistent=1):
-        t = Tuning(tpi, jtile, persistent)
+    def set_tuning(self, tpi=32, jtile=32, persistent=1, chunk=16):
+        t = Tuning(tpi, jtile, persistent, chunk)
         _check(lib().sphgpu_set_tuning(self._h, ctypes.byref(t)))
 
     def tuning(self):
         t = Tuning()
         _check(lib().sphgpu_get_tuning(self._h, ctypes.byref(t)))
-        return (t.threads_per_particle, t.jtile, t.persistent)
+        return (t.threads_per_particle, t.jtile, t.persistent, t.chunk)
 
     def set_active(self, max_active_bin):
         _check(lib().sphgpu_set_active(self._h, int(max_active_bin)))

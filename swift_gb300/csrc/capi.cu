@@ -78,7 +78,7 @@ struct sphgpu_space {
   std::vector<double> x_in;
   std::vector<float> v_in, m_in, h_in, u_in;
   std::vector<int8_t> tb_in;
-  sphgpu_tuning tune{32, 32, 1};
+  sphgpu_tuning tune{32, 32, 1, 16};
 
   // host plans
   Plan plan_d, plan_s, plan_f;
@@ -105,12 +105,13 @@ struct sphgpu_space {
   DBuf<int> queue, redo;
   DBuf<float4> bb_lo, bb_hi;
   DBuf<int2> bb_fc;
-  DBuf<int32_t> active_list, redo_list;
-  DBuf<int4> task_items_d, task_items_f;
+  DBuf<int4> units;              // gather work groups (device-built)
+  int max_units = 0;             // 32-particle windows of all leaves
+  std::vector<int> top_leaf;     // per top cell: first leaf (+1 sentinel)
+  DBuf<int4> task_units_d, task_units_f;
   DBuf<Entry> task_entries_d, task_entries_f;
   DBuf<int> task_pb_d, task_pe_d, task_pb_f, task_pe_f;
-  std::vector<int> task_items_begin_d, task_items_begin_f;
-  std::vector<int> active_top_begin;   // per top cell: slice of the active list
+  std::vector<int> task_units_begin_d, task_units_begin_f;
   int n_active = 0;
   std::vector<int> s_of_g;             // store index -> reference sorted index
   // host staging for step_host
@@ -169,10 +170,7 @@ void ensure_device(sphgpu_space* s) {
   const auto& cells = sp.cells();
   const auto& leaf_of = sp.leaf_of();
   const auto& lvs = sp.leaves();
-  std::vector<int32_t> alist;
-  alist.reserve(n);
   const int ntop = sp.cdim()[0] * sp.cdim()[1] * sp.cdim()[2];
-  s->active_top_begin.assign(ntop + 1, 0);
   for (int g = 0; g < n; g++) {
     const int k = gperm[g];
     const int srt = s->s_of_g[g];
@@ -186,15 +184,15 @@ void ensure_device(sphgpu_space* s) {
     lf[g] = leaf_of[srt];
     top[g] = cells[lvs[leaf_of[srt]]].top;
   }
-  // active list, grouped by top cell (store order is top-cell major)
-  for (int t = 0; t < ntop; t++) {
-    s->active_top_begin[t] = (int)alist.size();
-    const Cell& c = cells[t];
-    for (int g = c.first; g < c.first + c.count; g++)
-      if (fl[g]) alist.push_back(g);
-  }
-  s->active_top_begin[ntop] = (int)alist.size();
-  s->n_active = (int)alist.size();
+  s->n_active = 0;
+  for (int g = 0; g < n; g++) s->n_active += fl[g];
+  // one work group per 32-particle window of every leaf at most
+  s->max_units = 0;
+  for (size_t l = 0; l < lvs.size(); l++) s->max_units += (cells[lvs[l]].count + 31) / 32;
+  s->top_leaf.assign(ntop + 1, (int)lvs.size());
+  for (int l = (int)lvs.size() - 1; l >= 0; l--) s->top_leaf[cells[lvs[l]].top] = l;
+  for (int t = ntop - 1; t >= 0; t--)
+    if (s->top_leaf[t] > s->top_leaf[t + 1]) s->top_leaf[t] = s->top_leaf[t + 1];
   std::vector<double> tl(3 * (size_t)ntop);
   for (int t = 0; t < ntop; t++)
     for (int d = 0; d < 3; d++) tl[3 * (size_t)t + d] = cells[t].loc[d];
@@ -224,8 +222,7 @@ void ensure_device(sphgpu_space* s) {
   s->bb_lo.upload(blo.data(), nb, st);
   s->bb_hi.upload(bhi.data(), nb, st);
   s->bb_fc.upload(bfc.data(), nb, st);
-  s->active_list.upload(alist.data(), alist.size(), st);
-  s->redo_list.alloc(2 * (size_t)n);
+  s->units.alloc(std::max(1, s->max_units));
   s->posh.alloc(n);
   s->dens0.alloc(n);
   s->dens1.alloc(n);
@@ -239,7 +236,7 @@ void ensure_device(sphgpu_space* s) {
   s->ngb_d.alloc(n);
   s->ngb_d_first.alloc(n);
   s->ngb_f.alloc(n);
-  s->queue.alloc(8);
+  s->queue.alloc(16);  // [0..7] work counters, [8..15] unit counts
   s->redo.alloc(std::max(1, s->prm.max_iter));
   s->hit_ctr.alloc(4);
   for (auto& e : s->ev) CK(cudaEventCreate(&e));
@@ -282,21 +279,22 @@ void ensure_device(sphgpu_space* s) {
 // (~0.005 box units) that is < 1e-5 relative on r^2, far inside this band.
 constexpr float kBand = 2.44140625e-4f;  // 2^-12
 
-G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, const int* list, int count,
-             const int* count_ptr, int mode) {
+// qslot selects the work counter (queue[qslot]) and the unit count
+// (queue[8 + qslot]) of a launch.
+G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   G2Args a;
   a.p = s->P;
-  a.list = list;
-  a.count = count;
-  a.count_ptr = count_ptr;
-  a.leaf_pair_begin = dp.lpb.p;
+  a.units = s->units.p;
+  a.count = 0;
+  a.count_ptr = s->queue.p + 8 + qslot;
   a.pair_block = dp.pb.p;
   a.pair_entry = dp.pe.p;
   a.entries = dp.entries.p;
-  a.items = nullptr;
   a.bb_lo = s->bb_lo.p;
   a.bb_hi = s->bb_hi.p;
   a.bb_fc = s->bb_fc.p;
+  const double* w = s->space->width();
+  a.top_width = make_float3((float)w[0], (float)w[1], (float)w[2]);
   a.queue = s->queue.p + qslot;
   a.hits = nullptr;
   if (s->count_hits) a.hits = s->hit_ctr.p + (qslot == 0 ? 0 : (qslot == 2 ? 2 : 1));
@@ -305,8 +303,22 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, const int* list, int count
   return a;
 }
 
-GhostArgs ghargs(sphgpu_space* s, int iter, const int* in_list, int in_count,
-                 const int* in_count_ptr, int* out_list, int* out_count) {
+// Build the work groups of a loop (windows whose particles carry `need`
+// in their flags) and run the gather over them.
+void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
+                    int mode, bool force, int need, const int* gate,
+                    int leaf_begin = 0, int leaf_end = -1) {
+  const int nl = (int)s->space->leaves().size();
+  if (leaf_end < 0) leaf_end = nl;
+  CK(cudaMemsetAsync(s->queue.p + qslot, 0, sizeof(int), st));
+  CK(cudaMemsetAsync(s->queue.p + 8 + qslot, 0, sizeof(int), st));
+  CK(launch_build_units(s->leaves.p + leaf_begin, leaf_end - leaf_begin, s->flags.p,
+                        need, dp.lpb.p + leaf_begin, s->units.p,
+                        s->queue.p + 8 + qslot, gate, st));
+  CK(launch_gather(gargs(s, dp, qslot, mode), force, s->num_sms, s->max_units, st));
+}
+
+GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
   GhostArgs g;
   g.p = s->P;
   g.leaves = s->leaves.p;
@@ -316,53 +328,36 @@ GhostArgs ghargs(sphgpu_space* s, int iter, const int* in_list, int in_count,
   g.h_min = s->prm.h_min;
   g.alpha = s->prm.alpha;
   g.iter = iter;
-  g.in_list = in_list;
-  g.in_count = in_count;
-  g.in_count_ptr = in_count_ptr;
-  g.out_list = out_list;
-  g.out_count = out_count;
+  g.lo = lo;
+  g.hi = hi;
+  g.redo_count = s->redo.p;
   return g;
 }
 
-// Ghost rounds over a list of particles (the whole active list, or the
-// active particles of one top cell): round k iterates the particles sent on
-// by round k-1 and re-runs their density (subset gather lists) when any
-// were sent to another round.
-void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st, const int* list0,
-                          int count0) {
-  const int n = s->P.n;
+// Ghost rounds over all particles: round k iterates the particles still
+// flagged, and re-runs the density of those it sends to another round
+// (subset gather lists); both kernels return at once when the previous
+// round sent none (gates on the redo counts).
+void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st) {
   for (int k = 0; k < s->prm.max_iter; k++) {
-    const int* in = k == 0 ? list0 : s->redo_list.p + (size_t)((k - 1) & 1) * n;
-    const int* inc = k == 0 ? nullptr : s->redo.p + (k - 1);
-    int* out = s->redo_list.p + (size_t)(k & 1) * n;
-    CK(launch_ghost(ghargs(s, k, in, count0, inc, out, s->redo.p + k), count0, st));
-    CK(cudaMemsetAsync(s->queue.p + 1, 0, sizeof(int), st));
-    CK(launch_gather(gargs(s, s->dplan_s, 1, out, 0, s->redo.p + k, MODE_REDO),
-                     false, s->num_sms, count0, st));
+    CK(launch_ghost(ghargs(s, k, 0, s->P.n), st));
+    enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k);
   }
 }
 
 void enqueue_density(sphgpu_space* s, cudaStream_t st, bool density) {
   CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, st));
-  CK(cudaMemsetAsync(s->queue.p, 0, 8 * sizeof(int), st));
-  if (density)
-    CK(launch_gather(gargs(s, s->dplan_d, 0, s->active_list.p, s->n_active,
-                           nullptr, MODE_FIRST),
-                     false, s->num_sms, s->n_active, st));
+  if (density) enqueue_gather(s, st, s->dplan_d, 0, MODE_FIRST, false, 1, nullptr);
 }
 
 void enqueue_density_ghost(sphgpu_space* s, cudaStream_t st, int stages) {
   enqueue_density(s, st, (stages & SPHGPU_STAGE_DENSITY) != 0);
-  if (stages & SPHGPU_STAGE_GHOST)
-    enqueue_ghost_rounds(s, st, s->active_list.p, s->n_active);
+  if (stages & SPHGPU_STAGE_GHOST) enqueue_ghost_rounds(s, st);
 }
 
 void enqueue_force(sphgpu_space* s, cudaStream_t st) {
   CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
-  CK(cudaMemsetAsync(s->queue.p + 2, 0, sizeof(int), st));
-  CK(launch_gather(gargs(s, s->dplan_f, 2, s->active_list.p, s->n_active,
-                         nullptr, MODE_FIRST),
-                   true, s->num_sms, s->n_active, st));
+  enqueue_gather(s, st, s->dplan_f, 2, MODE_FIRST, true, 1, nullptr);
 }
 
 int check_conv(sphgpu_space* s, cudaStream_t st) {
@@ -563,8 +558,10 @@ int sphgpu_space_leaves(const sphgpu_space* s, double* geom, int32_t* ints) {
 
 int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
   if (!s || !t) return fail(SPHGPU_EINVAL, "null argument");
-  if (t->threads_per_particle != 32 || t->jtile != SPH_JBLOCK)
-    return fail(SPHGPU_EINVAL, "tuning: threads_per_particle 32, jtile 32 supported");
+  if (t->threads_per_particle != 32 || t->jtile != SPH_JBLOCK || t->chunk < 1 ||
+      t->chunk > 1024)
+    return fail(SPHGPU_EINVAL,
+                "tuning: threads_per_particle 32, jtile 32, chunk in [1, 1024]");
   s->tune = *t;
   drop_graph(s);
   return SPHGPU_OK;
@@ -591,18 +588,9 @@ int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
       const int n = s->P.n;
       std::vector<uint8_t> fl(n);
       for (int g = 0; g < n; g++) fl[g] = s->space->active()[s->s_of_g[g]] ? 1 : 0;
-      std::vector<int32_t> alist;
-      const auto& cells = s->space->cells();
-      const int ntop = s->space->cdim()[0] * s->space->cdim()[1] * s->space->cdim()[2];
-      for (int t = 0; t < ntop; t++) {
-        s->active_top_begin[t] = (int)alist.size();
-        for (int g = cells[t].first; g < cells[t].first + cells[t].count; g++)
-          if (fl[g]) alist.push_back(g);
-      }
-      s->active_top_begin[ntop] = (int)alist.size();
-      s->n_active = (int)alist.size();
+      s->n_active = 0;
+      for (int g = 0; g < n; g++) s->n_active += fl[g];
       s->flags.upload(fl.data(), n, s->stream);
-      s->active_list.upload(alist.data(), alist.size(), s->stream);
       s->dplan_d.upload(s->plan_d, s->stream);
       s->dplan_s.upload(s->plan_s, s->stream);
       CK(cudaStreamSynchronize(s->stream));
@@ -634,9 +622,7 @@ int sphgpu_step(sphgpu_space* s, int32_t stages, void* stream) {
     }
     if (!s->graph[0]) {
       s->graph[0] = capture(st, [&]() { enqueue_density(s, st, true); });
-      s->graph[1] = capture(st, [&]() {
-        enqueue_ghost_rounds(s, st, s->active_list.p, s->n_active);
-      });
+      s->graph[1] = capture(st, [&]() { enqueue_ghost_rounds(s, st); });
       s->graph[2] = capture(st, [&]() { enqueue_force(s, st); });
     }
     CK(cudaEventRecord(s->ev[0], st));
@@ -772,9 +758,7 @@ int sphgpu_force_from_state(sphgpu_space* s, const float* h, const float* rho,
     DevPlan dp;
     dp.upload(pf, st);
     CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
-    CK(cudaMemsetAsync(s->queue.p + 3, 0, sizeof(int), st));
-    CK(launch_gather(gargs(s, dp, 3, s->active_list.p, s->n_active, nullptr, MODE_FIRST),
-                     true, s->num_sms, s->n_active, st));
+    enqueue_gather(s, st, dp, 3, MODE_FIRST, true, 1, nullptr);
     CK(cudaStreamSynchronize(st));
     // the step's plans assume its own ghost: re-plan on the next step
     s->force_planned = false;
@@ -836,9 +820,15 @@ int sphgpu_density_noalloc(sphgpu_space* s, float* d_fields, int32_t* d_ngb,
                 "sphgpu_density_noalloc: " + std::to_string(s->P.n) +
                     " particles exceed the static scratch limit of " +
                     std::to_string(noalloc_max_particles()));
+  if (s->max_units > noalloc_max_units())
+    return fail(SPHGPU_EINVAL,
+                "sphgpu_density_noalloc: " + std::to_string(s->max_units) +
+                    " particle windows exceed the static scratch limit of " +
+                    std::to_string(noalloc_max_units()));
   const cudaError_t e = launch_density_noalloc(
-      gargs(s, s->dplan_d, 0, nullptr, 0, nullptr, MODE_FIRST), s->flags.p, d_fields,
-      d_ngb, s->perm.p, s->num_sms, pick(s, stream));
+      gargs(s, s->dplan_d, 0, MODE_FIRST), s->leaves.p,
+      (int)s->space->leaves().size(), s->dplan_d.lpb.p, d_fields, d_ngb, s->perm.p,
+      s->num_sms, pick(s, stream));
   if (e != cudaSuccess)
     return fail(SPHGPU_ECUDA, std::string("sphgpu_density_noalloc: ") +
                                   cudaGetErrorString(e));
@@ -859,7 +849,7 @@ static void ensure_task_plans(sphgpu_space* s, bool force) {
   plans.resize(tasks.size());
   std::vector<Item> items;
   std::vector<Entry> all_entries;
-  std::vector<int4> all_items;
+  std::vector<int4> all_units;
   std::vector<int> all_pb, all_pe;
   std::vector<int> ib(tasks.size() + 1, 0);
   const auto& cells = sp.cells();
@@ -880,7 +870,7 @@ static void ensure_task_plans(sphgpu_space* s, bool force) {
     else
       sp.dosub_pair(items, tasks[t].ci, tasks[t].cj, 0, force);
     sp.items_to_entries(items, per_leaf);
-    ib[t] = (int)all_items.size();
+    ib[t] = (int)all_units.size();
     touched.clear();
     // leaves touched by this task: those of its cells whose list is non-empty
     const int ci = tasks[t].ci, cj = tasks[t].cj;
@@ -902,18 +892,22 @@ static void ensure_task_plans(sphgpu_space* s, bool force) {
       const int pb1 = (int)all_pb.size();
       per_leaf[l].clear();
       const Cell& c = cells[lvs[l]];
-      for (int g = c.first; g < c.first + c.count; g++)
-        if (active[s->s_of_g[g]]) all_items.push_back(make_int4(g, pb0, pb1, 0));
+      for (int w0 = c.first; w0 < c.first + c.count; w0 += 32) {
+        unsigned m = 0;
+        for (int q = 0; q < 32 && w0 + q < c.first + c.count; q++)
+          if (active[s->s_of_g[w0 + q]]) m |= 1u << q;
+        if (m) all_units.push_back(make_int4(w0, (int)m, pb0, pb1));
+      }
     }
   }
-  ib[tasks.size()] = (int)all_items.size();
-  auto& di = force ? s->task_items_f : s->task_items_d;
+  ib[tasks.size()] = (int)all_units.size();
+  auto& di = force ? s->task_units_f : s->task_units_d;
   auto& de = force ? s->task_entries_f : s->task_entries_d;
-  di.upload(all_items.data(), all_items.size(), s->stream);
+  di.upload(all_units.data(), all_units.size(), s->stream);
   de.upload(all_entries.data(), all_entries.size(), s->stream);
   (force ? s->task_pb_f : s->task_pb_d).upload(all_pb.data(), all_pb.size(), s->stream);
   (force ? s->task_pe_f : s->task_pe_d).upload(all_pe.data(), all_pe.size(), s->stream);
-  (force ? s->task_items_begin_f : s->task_items_begin_d) = ib;
+  (force ? s->task_units_begin_f : s->task_units_begin_d) = ib;
   CK(cudaStreamSynchronize(s->stream));
 }
 
@@ -926,15 +920,16 @@ static int find_task(const sphgpu_space* s, int ci, int cj) {
 }
 
 static int run_task(sphgpu_space* s, int t, bool force, cudaStream_t st) {
-  const auto& ib = force ? s->task_items_begin_f : s->task_items_begin_d;
+  const auto& ib = force ? s->task_units_begin_f : s->task_units_begin_d;
   const int b = ib[t], e = ib[t + 1];
   if (e == b) return SPHGPU_OK;
-  G2Args a = gargs(s, s->dplan_d, 4, nullptr, e - b, nullptr, MODE_ACCUM);
-  a.items = (force ? s->task_items_f.p : s->task_items_d.p) + b;
+  G2Args a = gargs(s, s->dplan_d, 4, MODE_ACCUM);
+  a.units = (force ? s->task_units_f.p : s->task_units_d.p) + b;
+  a.count = e - b;
+  a.count_ptr = nullptr;
   a.entries = force ? s->task_entries_f.p : s->task_entries_d.p;
   a.pair_block = force ? s->task_pb_f.p : s->task_pb_d.p;
   a.pair_entry = force ? s->task_pe_f.p : s->task_pe_d.p;
-  a.leaf_pair_begin = nullptr;
   CK(cudaMemsetAsync(s->queue.p + 4, 0, sizeof(int), st));
   CK(launch_gather(a, force, s->num_sms, e - b, st));
   return SPHGPU_OK;
@@ -979,22 +974,17 @@ int sphgpu_do_ghost(sphgpu_space* s, int32_t cell, void* stream) {
   return guard([&]() {
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
-    const int b = s->active_top_begin[cell], e = s->active_top_begin[cell + 1];
-    if (e == b) return SPHGPU_OK;
-    const int n = s->P.n;
+    const Cell& c = s->space->cells()[cell];
+    if (c.count == 0 || !c.active) return SPHGPU_OK;
     CK(cudaMemsetAsync(s->redo.p, 0, sizeof(int) * s->prm.max_iter, st));
     for (int k = 0; k < s->prm.max_iter; k++) {
-      const int* in = k == 0 ? s->active_list.p + b : s->redo_list.p + (size_t)((k - 1) & 1) * n;
-      const int* inc = k == 0 ? nullptr : s->redo.p + (k - 1);
-      int* out = s->redo_list.p + (size_t)(k & 1) * n;
-      CK(launch_ghost(ghargs(s, k, in, e - b, inc, out, s->redo.p + k), e - b, st));
+      CK(launch_ghost(ghargs(s, k, c.first, c.first + c.count), st));
       int cnt = 0;
       CK(cudaMemcpyAsync(&cnt, s->redo.p + k, sizeof(int), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
       if (cnt == 0) return SPHGPU_OK;
-      CK(cudaMemsetAsync(s->queue.p + 5, 0, sizeof(int), st));
-      CK(launch_gather(gargs(s, s->dplan_s, 5, out, cnt, nullptr, MODE_REDO), false,
-                       s->num_sms, cnt, st));
+      enqueue_gather(s, st, s->dplan_s, 5, MODE_REDO, false, 3, nullptr,
+                     s->top_leaf[cell], s->top_leaf[cell + 1]);
       if (k == s->prm.max_iter - 1)
         return fail(SPHGPU_ENOCONV, "smoothing length failed to converge on " +
                                         std::to_string(cnt) + " particles");

@@ -1,21 +1,17 @@
-// gather.cu -- warp-per-particle neighbour gathers for the density and force
-// loops (sm_103a).
+// gather.cu -- launchers of the neighbour gathers (kernels in
+// gather_impl.cuh) for the density and force loops (sm_103a).
 //
-// One warp owns one updated particle i at a time (particles are pulled from
-// a device work queue: the active list, or the ghost's re-run list).  For
-// each partner cell of i's leaf the warp
-//   1. tests 32 candidate j-blocks at once (one per lane; the leaf's
-//      candidate list flattens all its partner cells) against i's search
-//      sphere (bounding box of <= 32 spatially sorted particles; FP32,
-//      conservative), compacting the survivors into shared memory;
-//   2. for each surviving block, evaluates the neighbour predicate with one
-//      partner particle per lane: FP32 r^2 from top-cell-relative offsets,
-//      and -- only inside a 2^-12 relative band around H^2 -- the exact FP64
-//      evaluation in the reference's frame for that cell pair;
-//   3. appends hits to a per-warp buffer in shared memory (ballot + popc);
-//      whenever 32 hits are buffered, every lane computes one interaction.
-// Partial sums are reduced over the warp with shuffles at the end.  There
-// are no atomics on particle data and no block-wide barriers.
+// One warp owns a group of up to 32 particles of one leaf, one per lane
+// (groups come from a device-built list of 32-particle windows with a lane
+// mask: all active particles, or those the ghost sends to another round).
+// The group's box culls the leaf's candidate j-blocks; each surviving block
+// is staged in shared memory (frame offset applied) and every lane tests its
+// own particle against it with broadcast reads -- FP32 r^2 from
+// top-cell-relative offsets and, only inside a 2^-12 relative band around
+// H^2, the exact FP64 evaluation in the reference's frame for that cell
+// pair.  Hits queue per lane in shared memory and are computed in batches;
+// every lane keeps its own particle's sums in registers.  No atomics on
+// particle data, no block-wide barriers.
 //
 // Physics per hit: runner_iact_nonsym_density (hydro/Minimal/hydro_iact.h:
 // 137-189) and runner_iact_nonsym_force (:378-490), Wendland C2 kernel
@@ -42,22 +38,33 @@ __global__ void block_hmax(const int2* __restrict__ fc, float4* __restrict__ lo,
   }
 }
 
-cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_items,
+cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
                           cudaStream_t s) {
   int per_sm = 0;
   if (force)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_warp<true>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_lanes<true>,
                                                   WARPS_PER_BLOCK * 32, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_warp<false>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_lanes<false>,
                                                   WARPS_PER_BLOCK * 32, 0);
   int grid = std::max(1, per_sm) * num_sms;
-  const int need = (max_items + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
+  const int need = (max_units + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
   grid = std::max(1, std::min(grid, need));
   if (force)
-    gather_warp<true><<<grid, WARPS_PER_BLOCK * 32, 0, s>>>(a);
+    gather_lanes<true><<<grid, WARPS_PER_BLOCK * 32, 0, s>>>(a);
   else
-    gather_warp<false><<<grid, WARPS_PER_BLOCK * 32, 0, s>>>(a);
+    gather_lanes<false><<<grid, WARPS_PER_BLOCK * 32, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
+                               const uint8_t* flags, int need,
+                               const int* leaf_pair_begin, int4* units,
+                               int* nunits, const int* gate, cudaStream_t s) {
+  int g = (nleaves * 32 + 255) / 256;
+  g = std::max(1, std::min(g, 152 * 16));
+  build_units<<<g, 256, 0, s>>>(leaves, nleaves, flags, need, leaf_pair_begin,
+                                units, nunits, gate);
   return cudaGetLastError();
 }
 

@@ -74,75 +74,115 @@ static __device__ __forceinline__ float h2_exact(float h) {
   return __fmul_rn(__fmul_rn(h, h), SPH_KG2);
 }
 
-struct WarpSmem {
-  int j[64];
-  float4 d[64];   // dx, dy, dz (i - j, in i's frame), r2
-  int sb[32];     // surviving candidate blocks of the current chunk
-  int se[32];     // their gather-list entries
-  float4 sf[32];  // their frame offsets
+// Per-warp shared memory: the staged partner block and each lane's queue
+// of pending hits (partner index and frame-offset index packed in 32 bits).
+#define QCAP 24
+struct LaneSmem {
+  float4 jpos[32];     // staged block: offset xyz in the group's frame, (K h)^2
+  int sfirst[32];      // surviving candidate blocks of the current chunk
+  int scount[32];
+  int se[32];
+  float4 sf[32];       // their frame offsets (w: frame-offset index)
+  float4 slo[32];      // their boxes
+  float4 shi[32];
+  int q[QCAP][32];     // per-lane hit queue
 };
 
+// Frame offset of a partner top cell from its index in the 3x3x3
+// neighbourhood of the group's top cell (ix + 3 iy + 9 iz, each in 0..2).
+__device__ __forceinline__ float3 offset_of(int idx, float3 tw) {
+  return make_float3((float)(idx % 3 - 1) * tw.x, (float)((idx / 3) % 3 - 1) * tw.y,
+                     (float)(idx / 9 - 1) * tw.z);
+}
+
+// One warp = one group of <= 32 particles of a leaf (one lane each).
+//   1. the group's box, grown by the largest search radius, culls the
+//      leaf's candidate blocks 32 at a time (one per lane), survivors are
+//      compacted into shared memory;
+//   2. each survivor is tested against every lane's own search sphere
+//      (skipped when no lane reaches it), then staged in shared memory with
+//      the frame offset applied;
+//   3. every lane tests its own particle against each staged partner
+//      (broadcast reads): FP32 r^2, and inside a 2^-12 band around H^2 the
+//      exact FP64 predicate in the reference frame; hits go to the lane's
+//      queue;
+//   4. when a queue is nearly full all lanes flush: each computes the
+//      interactions of its own queue.  Sums stay in the lane's registers.
 template <bool FORCE, int OUT = OUT_STORE>
 __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32, 3)
-gather_warp(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
-  __shared__ WarpSmem smem[WARPS_PER_BLOCK];
+gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
+  __shared__ LaneSmem smem[WARPS_PER_BLOCK];
   const int lane = threadIdx.x & 31;
-  WarpSmem& ws = smem[threadIdx.x >> 5];
+  LaneSmem& ws = smem[threadIdx.x >> 5];
   const DevParticles& P = a.p;
-  const int count = a.count_ptr ? *a.count_ptr : a.count;
+  const int nunits = a.count_ptr ? *a.count_ptr : a.count;
   const unsigned lt_mask = (1u << lane) - 1u;
   const float band = a.band;
-  int base = 0, left = 0;
+  const float3 tw = a.top_width;
   for (;;) {
-    if (left == 0) {
-      int w = 0;
-      if (lane == 0) w = atomicAdd(a.queue, 4);
-      base = __shfl_sync(FULL, w, 0);
-      left = 4;
+    int u = 0;
+    if (lane == 0) u = atomicAdd(a.queue, 1);
+    u = __shfl_sync(FULL, u, 0);
+    if (u >= nunits) break;
+    const int4 U = a.units[u];  // base, mask, pair begin, pair end
+    const bool valid = (U.y >> lane) & 1;
+    const int i = U.x + lane;
+    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), vi = make_float4(0.f, 0.f, 0.f, 1.f);
+    float4 fi = make_float4(1.f, 0.f, 0.f, 0.f);
+    float bi = 0.f;
+    int dh = 0;
+    if (valid) {
+      pi = P.posh[i];
+      vi = P.velm[i];
+      dh = P.depth_h[i];
+      if (FORCE) {
+        fi = P.fin0[i];
+        bi = P.fin1[i].x;
+      }
     }
-    const int w = base++;
-    left--;
-    if (w >= count) break;
-    int i, p0, p1;
-    if (a.items) {
-      const int4 it = a.items[w];
-      i = it.x;
-      p0 = it.y;
-      p1 = it.z;
-    } else {
-      i = a.list[w];
-      const int leaf = P.leaf_of[i];
-      p0 = a.leaf_pair_begin[leaf];
-      p1 = a.leaf_pair_begin[leaf + 1];
-    }
-    const float4 pi = P.posh[i];
-    const float4 vi = P.velm[i];
-    const int dh = P.depth_h[i];
-    const float hi = pi.w;
-    const float hig2 = h2_exact(hi);
+    const float hi = valid ? pi.w : 1.f;
+    const float hig2 = valid ? h2_exact(hi) : 0.f;
     const float hi_inv = 1.f / hi;
-    float4 fi = make_float4(0.f, 0.f, 0.f, 0.f);
-    float bi = 0.f, hid_inv = 0.f;
-    if (FORCE) {
-      fi = P.fin0[i];
-      bi = P.fin1[i].x;
-      const float t = hi_inv * hi_inv;
-      hid_inv = t * t;
+    const float hid_inv = (hi_inv * hi_inv) * (hi_inv * hi_inv);
+    const float mi_inv = 1.f / vi.w;
+    const float lo2 = hig2 * (1.f - band), hi2 = hig2 * (1.f + band);
+    // group box grown by the group's largest radius
+    float gx0 = valid ? pi.x : 3.4e38f, gy0 = valid ? pi.y : 3.4e38f,
+          gz0 = valid ? pi.z : 3.4e38f;
+    float gx1 = valid ? pi.x : -3.4e38f, gy1 = valid ? pi.y : -3.4e38f,
+          gz1 = valid ? pi.z : -3.4e38f;
+    float gh2 = hig2;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      gx0 = fminf(gx0, __shfl_xor_sync(FULL, gx0, off));
+      gy0 = fminf(gy0, __shfl_xor_sync(FULL, gy0, off));
+      gz0 = fminf(gz0, __shfl_xor_sync(FULL, gz0, off));
+      gx1 = fmaxf(gx1, __shfl_xor_sync(FULL, gx1, off));
+      gy1 = fmaxf(gy1, __shfl_xor_sync(FULL, gy1, off));
+      gz1 = fmaxf(gz1, __shfl_xor_sync(FULL, gz1, off));
+      gh2 = fmaxf(gh2, __shfl_xor_sync(FULL, gh2, off));
     }
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f, s5 = 0.f, s6 = 0.f,
           s7 = 0.f;
     if (FORCE) s5 = 2.f * fi.w;
     int ngb = 0;
-    int nbuf = 0;
+    int qn = 0;
 
-    auto interact = [&](int j, float4 d) {
-      const float r2 = d.w;
+    auto interact = [&](int packed) {
+      const int j = packed & 0x07ffffff;
+      const float3 fd = offset_of((int)((unsigned)packed >> 27), tw);
+      const float4 q = P.posh[j];
+      const float dx = pi.x - (q.x + fd.x), dy = pi.y - (q.y + fd.y),
+                  dz = pi.z - (q.z + fd.z);
+      const float r2 = dx * dx + dy * dy + dz * dz;
       const float4 vm = P.velm[j];
       const float mj = vm.w;
-      const float r = sqrtf(r2);
-      const float r_inv = r > 0.f ? 1.f / r : 0.f;
+      // hardware reciprocal square root (MUFU.RSQ, ~2 ulp): the sums are
+      // held to 1e-4 relative, and the neighbour decision was made exactly
+      const float r_inv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+      const float r = r2 * r_inv;
       const float dvx = vi.x - vm.x, dvy = vi.y - vm.y, dvz = vi.z - vm.z;
-      const float dvdr = dvx * d.x + dvy * d.y + dvz * d.z;
+      const float dvdr = dvx * dx + dvy * dy + dvz * dz;
       if (!FORCE) {
         const float ui = r * hi_inv;
         float W, dW;
@@ -154,172 +194,206 @@ gather_warp(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         s3 -= t3;
         const float fac = mj * dW * r_inv;
         s4 -= fac * dvdr;
-        s5 += fac * (dvy * d.z - dvz * d.y);
-        s6 += fac * (dvz * d.x - dvx * d.z);
-        s7 += fac * (dvx * d.y - dvy * d.x);
+        s5 += fac * (dvy * dz - dvz * dy);
+        s6 += fac * (dvz * dx - dvx * dz);
+        s7 += fac * (dvx * dy - dvy * dx);
       } else {
-        const float hj = P.posh[j].w;
+        const float hj = q.w;
         const float4 fj = P.fin0[j];
         const float bj = P.fin1[j].x;
         float Wi, dWi, Wj, dWj;
         wendland(r * hi_inv, Wi, dWi);
         const float wi_dr = hid_inv * dWi;
-        const float hj_inv = 1.f / hj;
+        const float hj_inv = __fdividef(1.f, hj);
         const float hj2 = hj_inv * hj_inv;
         wendland(r * hj_inv, Wj, dWj);
         const float wj_dr = hj2 * hj2 * dWj;
-        const float f_ij = 1.f - fi.y / mj;
-        const float f_ji = 1.f - fj.y / vi.w;
+        const float f_ij = 1.f - __fdividef(fi.y, mj);
+        const float f_ji = 1.f - fj.y * mi_inv;
         const float Pi = fi.z * f_ij;
         const float Pj = fj.z * f_ji;
         const float mu = r_inv * fminf(dvdr, 0.f);
         const float vs = fi.w + fj.w - SPH_VISC_BETA * mu;
-        const float visc = -0.25f * vs * (bi + bj) * mu / (0.5f * (fi.x + fj.x));
+        const float visc =
+            __fdividef(-0.25f * vs * (bi + bj) * mu, 0.5f * (fi.x + fj.x));
         const float visc_acc = 0.5f * visc * (wi_dr * f_ij + wj_dr * f_ji) * r_inv;
         const float acc = (Pi * wi_dr + Pj * wj_dr) * r_inv + visc_acc;
-        s0 -= mj * acc * d.x;
-        s1 -= mj * acc * d.y;
-        s2 -= mj * acc * d.z;
+        s0 -= mj * acc * dx;
+        s1 -= mj * acc * dy;
+        s2 -= mj * acc * dz;
         s3 += (Pi * dvdr * r_inv * wi_dr + 0.5f * visc_acc * dvdr) * mj;
-        s4 -= mj * dvdr * r_inv / fj.x * wi_dr * f_ij;
+        s4 -= __fdividef(mj * dvdr * r_inv, fj.x) * wi_dr * f_ij;
         s5 = fmaxf(s5, vs);
       }
       ngb++;
     };
 
-    // Test one surviving block: one partner particle per lane.
-    auto test_block = [&](int k) {
-      const int b = ws.sb[k];
-      const int2 fc = a.bb_fc[b];
-      const float4 fd = ws.sf[k];
-      bool hit = false;
-      float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
-      int j = -1;
-      if (lane < fc.y) {
-        j = fc.x + lane;
-        const float4 q = P.posh[j];
-        d.x = pi.x - (q.x + fd.x);
-        d.y = pi.y - (q.y + fd.y);
-        d.z = pi.z - (q.z + fd.z);
-        d.w = d.x * d.x + d.y * d.y + d.z * d.z;
-        const float H2 = FORCE ? fmaxf(hig2, h2_exact(q.w)) : hig2;
-        if (d.w < H2 * (1.f + band) && j != i)
-          hit = (d.w < H2 * (1.f - band)) ||
-                (exact_r2_2(P.xd, i, j, &a.entries[ws.se[k]]) < H2);
-      }
-      const unsigned hm = __ballot_sync(FULL, hit);
-      if (hit) {
-        const int slot = nbuf + __popc(hm & lt_mask);
-        ws.j[slot] = j;
-        ws.d[slot] = d;
-      }
-      nbuf += __popc(hm);
-      if (nbuf >= 32) {
-        __syncwarp();
-        interact(ws.j[lane], ws.d[lane]);
-        __syncwarp();
-        if (lane + 32 < nbuf) {
-          ws.j[lane] = ws.j[lane + 32];
-          ws.d[lane] = ws.d[lane + 32];
-        }
-        nbuf -= 32;
-        __syncwarp();
-      }
+    auto flush = [&]() {
+      const int m = (int)__reduce_max_sync(FULL, (unsigned)qn);
+      __syncwarp();
+      for (int k = 0; k < m; k++)
+        if (k < qn) interact(ws.q[k][lane]);
+      qn = 0;
+      __syncwarp();
     };
 
-    for (int c0 = p0; c0 < p1; c0 += 32) {
+    for (int c0 = U.z; c0 < U.w; c0 += 32) {
       const int p = c0 + lane;
       bool ov = false;
-      int b = 0, e = 0;
-      float4 fd = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (p < p1) {
-        b = a.pair_block[p];
+      int e = 0;
+      float4 fd = make_float4(0.f, 0.f, 0.f, 0.f), lo = fd, hb = fd;
+      int2 fc = make_int2(0, 0);
+      if (p < U.w) {
+        const int b = a.pair_block[p];
         e = a.pair_entry[p];
         const Entry* E = &a.entries[e];
-        const int mind = E->min_depth, maxd = E->max_depth;
         fd = make_float4(E->fdx, E->fdy, E->fdz, 0.f);
-        if (dh >= mind && dh <= maxd) {
-          const float4 lo = a.bb_lo[b];
-          const float4 hb = a.bb_hi[b];
-          const float px = pi.x - fd.x, py = pi.y - fd.y, pz = pi.z - fd.z;
-          const float dx = fmaxf(fmaxf(lo.x - px, px - hb.x), 0.f);
-          const float dy = fmaxf(fmaxf(lo.y - py, py - hb.y), 0.f);
-          const float dz = fmaxf(fmaxf(lo.z - pz, pz - hb.z), 0.f);
-          const float R2 = FORCE ? fmaxf(hig2, lo.w) : hig2;
-          ov = dx * dx + dy * dy + dz * dz < R2 * (1.f + 4.f * band) + 1e-30f;
+        lo = a.bb_lo[b];
+        hb = a.bb_hi[b];
+        const float dx = fmaxf(fmaxf(lo.x + fd.x - gx1, gx0 - hb.x - fd.x), 0.f);
+        const float dy = fmaxf(fmaxf(lo.y + fd.y - gy1, gy0 - hb.y - fd.y), 0.f);
+        const float dz = fmaxf(fmaxf(lo.z + fd.z - gz1, gz0 - hb.z - fd.z), 0.f);
+        const float R2 = FORCE ? fmaxf(gh2, lo.w) : gh2;
+        ov = dx * dx + dy * dy + dz * dz < R2 * (1.f + 4.f * band) + 1e-30f;
+        if (ov) {
+          fc = a.bb_fc[b];
+          // frame-offset index of the partner top cell (for the queues)
+          const int ix = (int)rintf(fd.x / tw.x) + 1, iy = (int)rintf(fd.y / tw.y) + 1,
+                    iz = (int)rintf(fd.z / tw.z) + 1;
+          fd.w = __int_as_float(ix + 3 * iy + 9 * iz);
         }
       }
       const unsigned mask = __ballot_sync(FULL, ov);
       if (ov) {
         const int slot = __popc(mask & lt_mask);
-        ws.sb[slot] = b;
+        ws.sfirst[slot] = fc.x;
+        ws.scount[slot] = fc.y;
         ws.se[slot] = e;
         ws.sf[slot] = fd;
+        ws.slo[slot] = lo;
+        ws.shi[slot] = hb;
       }
       __syncwarp();
       const int nsurv = __popc(mask);
-      for (int k = 0; k < nsurv; k++) test_block(k);
+      for (int k = 0; k < nsurv; k++) {
+        const float4 sfd = ws.sf[k];
+        const float4 slo = ws.slo[k], shi = ws.shi[k];
+        const int eidx = ws.se[k];
+        const Entry* E = &a.entries[eidx];
+        // does this lane's own sphere reach the block, and may it use the
+        // entry (depth filter)?
+        bool mine = false;
+        if (valid && dh >= E->min_depth && dh <= E->max_depth) {
+          const float px = pi.x - sfd.x, py = pi.y - sfd.y, pz = pi.z - sfd.z;
+          const float dx = fmaxf(fmaxf(slo.x - px, px - shi.x), 0.f);
+          const float dy = fmaxf(fmaxf(slo.y - py, py - shi.y), 0.f);
+          const float dz = fmaxf(fmaxf(slo.z - pz, pz - shi.z), 0.f);
+          const float R2 = FORCE ? fmaxf(hig2, slo.w) : hig2;
+          mine = dx * dx + dy * dy + dz * dz < R2 * (1.f + 4.f * band) + 1e-30f;
+        }
+        if (!__any_sync(FULL, mine)) continue;
+        const int bfirst = ws.sfirst[k], bcount = ws.scount[k];
+        const int fidx = __float_as_int(sfd.w);
+        __syncwarp();
+        if (lane < bcount) {
+          float4 q = P.posh[bfirst + lane];
+          q.x += sfd.x;
+          q.y += sfd.y;
+          q.z += sfd.z;
+          q.w = FORCE ? h2_exact(q.w) : 0.f;
+          ws.jpos[lane] = q;
+        }
+        __syncwarp();
+        for (int t = 0; t < bcount; t++) {
+          const float4 q = ws.jpos[t];
+          const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          float L2 = lo2, U2 = hi2, H2 = hig2;
+          if (FORCE) {
+            H2 = fmaxf(hig2, q.w);
+            L2 = H2 * (1.f - band);
+            U2 = H2 * (1.f + band);
+          }
+          const int j = bfirst + t;
+          if (mine && r2 < U2 && j != i &&
+              (r2 < L2 || exact_r2_2(P.xd, i, j, E) < H2)) {
+            ws.q[qn][lane] = j | (fidx << 27);
+            qn++;
+          }
+          if ((t & 7) == 7 && __any_sync(FULL, qn > QCAP - 8)) flush();
+        }
+        if (__any_sync(FULL, qn > QCAP - 8)) flush();
+      }
       __syncwarp();
     }
-    __syncwarp();
-    if (lane < nbuf) interact(ws.j[lane], ws.d[lane]);
-    __syncwarp();
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      s0 += __shfl_xor_sync(FULL, s0, off);
-      s1 += __shfl_xor_sync(FULL, s1, off);
-      s2 += __shfl_xor_sync(FULL, s2, off);
-      s3 += __shfl_xor_sync(FULL, s3, off);
-      s4 += __shfl_xor_sync(FULL, s4, off);
-      if (!FORCE) {
-        s5 += __shfl_xor_sync(FULL, s5, off);
-        s6 += __shfl_xor_sync(FULL, s6, off);
-        s7 += __shfl_xor_sync(FULL, s7, off);
-      } else {
-        s5 = fmaxf(s5, __shfl_xor_sync(FULL, s5, off));
-      }
-      ngb += __shfl_xor_sync(FULL, ngb, off);
-    }
-    if (OUT == OUT_CALLER && lane == 0) {
+    flush();
+    if (!valid) continue;
+    if (OUT == OUT_CALLER) {
       const size_t k = (size_t)co.perm[i];
       float* o = co.fields + 8 * k;
       o[0] = s0; o[1] = s1; o[2] = s2; o[3] = s3;
       o[4] = s4; o[5] = s5; o[6] = s6; o[7] = s7;
       co.ngb[k] = ngb;
+      continue;
     }
-    if (OUT == OUT_STORE && lane == 0) {
-      if (a.hits) atomicAdd(a.hits, (unsigned long long)ngb);
-      if (!FORCE) {
-        if (a.mode == MODE_ACCUM) {
-          float4 d0 = P.dens0[i], d1 = P.dens1[i];
-          d0.x += s0; d0.y += s1; d0.z += s2; d0.w += s3;
-          d1.x += s4; d1.y += s5; d1.z += s6; d1.w += s7;
-          P.dens0[i] = d0;
-          P.dens1[i] = d1;
-          P.ngb_d[i] += ngb;
-          P.ngb_d_first[i] += ngb;
-        } else {
-          P.dens0[i] = make_float4(s0, s1, s2, s3);
-          P.dens1[i] = make_float4(s4, s5, s6, s7);
-          P.ngb_d[i] = ngb;
-          if (a.mode == MODE_FIRST) P.ngb_d_first[i] = ngb;
-        }
+    if (a.hits) atomicAdd(a.hits, (unsigned long long)ngb);
+    if (!FORCE) {
+      if (a.mode == MODE_ACCUM) {
+        float4 d0 = P.dens0[i], d1 = P.dens1[i];
+        d0.x += s0; d0.y += s1; d0.z += s2; d0.w += s3;
+        d1.x += s4; d1.y += s5; d1.z += s6; d1.w += s7;
+        P.dens0[i] = d0;
+        P.dens1[i] = d1;
+        P.ngb_d[i] += ngb;
+        P.ngb_d_first[i] += ngb;
       } else {
-        if (a.mode == MODE_ACCUM) {
-          float4 ac = P.acc[i];
-          float2 hv = P.hdt_vsig[i];
-          ac.x += s0; ac.y += s1; ac.z += s2; ac.w += s3;
-          hv.x += s4;
-          hv.y = fmaxf(hv.y, s5);
-          P.acc[i] = ac;
-          P.hdt_vsig[i] = hv;
-          P.ngb_f[i] += ngb;
-        } else {
-          // hydro_end_force (hydro.h:878) folded in
-          P.acc[i] = make_float4(s0, s1, s2, s3);
-          P.hdt_vsig[i] = make_float2(s4 * (hi * SPH_HDIM_INV), s5);
-          P.ngb_f[i] = ngb;
-        }
+        P.dens0[i] = make_float4(s0, s1, s2, s3);
+        P.dens1[i] = make_float4(s4, s5, s6, s7);
+        P.ngb_d[i] = ngb;
+        if (a.mode == MODE_FIRST) P.ngb_d_first[i] = ngb;
+      }
+    } else {
+      if (a.mode == MODE_ACCUM) {
+        float4 ac = P.acc[i];
+        float2 hv = P.hdt_vsig[i];
+        ac.x += s0; ac.y += s1; ac.z += s2; ac.w += s3;
+        hv.x += s4;
+        hv.y = fmaxf(hv.y, s5);
+        P.acc[i] = ac;
+        P.hdt_vsig[i] = hv;
+        P.ngb_f[i] += ngb;
+      } else {
+        // hydro_end_force (hydro.h:878) folded in
+        P.acc[i] = make_float4(s0, s1, s2, s3);
+        P.hdt_vsig[i] = make_float2(s4 * (hi * SPH_HDIM_INV), s5);
+        P.ngb_f[i] = ngb;
+      }
+    }
+  }
+}
+
+// Work groups for the gathers: every 32-particle window of every leaf with
+// at least one particle whose flags contain `need`, as
+// (window base, lane mask, candidate-list begin, end).
+static __global__ void build_units(const LeafInfo* __restrict__ leaves, int nleaves,
+                            const uint8_t* __restrict__ flags, int need,
+                            const int* __restrict__ leaf_pair_begin,
+                            int4* __restrict__ units, int* __restrict__ nunits,
+                            const int* gate) {
+  if (gate && *gate == 0) return;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int l = warp; l < nleaves; l += nwarps) {
+    const int first = leaves[l].first, count = leaves[l].count;
+    const int p0 = leaf_pair_begin[l], p1 = leaf_pair_begin[l + 1];
+    if (p0 == p1) continue;
+    for (int w0 = 0; w0 < count; w0 += 32) {
+      const bool ok = w0 + lane < count && (flags[first + w0 + lane] & need) == need;
+      const unsigned m = __ballot_sync(FULL, ok);
+      if (m && lane == 0) {
+        const int slot = atomicAdd(nunits, 1);
+        units[slot] = make_int4(first + w0, (int)m, p0, p1);
       }
     }
   }

@@ -40,12 +40,12 @@ __device__ void prepare_force(const DevParticles& P, int i, float h, float rho,
 }
 
 __global__ void ghost_round(GhostArgs g) {
-  const int count = g.in_count_ptr ? *g.in_count_ptr : g.in_count;
+  if (g.iter > 0 && g.redo_count[g.iter - 1] == 0) return;
   const DevParticles& P = g.p;
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < count;
-       idx += gridDim.x * blockDim.x) {
-    const int i = g.in_list[idx];
+  for (int i = g.lo + blockIdx.x * blockDim.x + threadIdx.x; i < g.hi;
+       i += gridDim.x * blockDim.x) {
     const uint8_t fl = P.flags[i];
+    if ((fl & 3) != 3) continue;  // active and still iterating
     P.ghost_iters[i] = g.iter + 1;
     float4 ph = P.posh[i];
     const float h_old = ph.w;
@@ -90,6 +90,7 @@ __global__ void ghost_round(GhostArgs g) {
       if ((h_old >= g.h_max && f < 0.f) || (h_old <= g.h_min && f > 0.f)) {
         prepare_force(P, i, h_old, rho, wc, wc_dh, rho_dh, divv, rx, ry, rz,
                       P.u[i], g.alpha, g.h_max);
+        P.flags[i] = fl & ~2;
         P.left[i] = left;
         P.right[i] = right;
         continue;
@@ -112,8 +113,8 @@ __global__ void ghost_round(GhostArgs g) {
         P.posh[i] = ph;
         P.left[i] = left;
         P.right[i] = right;
-        g.out_list[atomicAdd(g.out_count, 1)] = i;
-        continue;  // another round
+        atomicAdd(&g.redo_count[g.iter], 1);
+        continue;  // flags keep bit 1: another round
       } else if (h <= g.h_min) {
         h = g.h_min;
       } else {
@@ -147,8 +148,8 @@ __global__ void ghost_round(GhostArgs g) {
     P.right[i] = right;
     prepare_force(P, i, h, rho, wc, wc_dh, rho_dh, divv, rx, ry, rz, P.u[i],
                   g.alpha, g.h_max);
+    P.flags[i] = fl & ~2;
     (void)done;
-    (void)fl;
   }
 }
 
@@ -159,6 +160,7 @@ __global__ void begin_step(DevParticles P, int max_iter, int* redo_count) {
     float4 ph = P.posh[i];
     ph.w = P.h0[i];
     P.posh[i] = ph;
+    P.flags[i] = (P.flags[i] & 1) ? 3 : 0;
     P.left[i] = 0.f;
     P.right[i] = 3.40282347e+38f;
     P.ghost_iters[i] = 0;
@@ -250,8 +252,8 @@ static int grid_for(int n) {
   return g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g);
 }
 
-cudaError_t launch_ghost(const GhostArgs& g, int max_items, cudaStream_t s) {
-  ghost_round<<<grid_for(max_items), 256, 0, s>>>(g);
+cudaError_t launch_ghost(const GhostArgs& g, cudaStream_t s) {
+  ghost_round<<<grid_for(g.hi - g.lo), 256, 0, s>>>(g);
   return cudaGetLastError();
 }
 

@@ -39,21 +39,19 @@ struct DevParticles {
 
 enum GatherMode { MODE_FIRST = 0, MODE_REDO = 1, MODE_ACCUM = 2 };
 
-// Warp-per-particle gather (gather.cu).
+// Lane-per-particle gather (gather_impl.cuh).
 struct G2Args {
   DevParticles p;
-  const int* list;              // updated particles (store order)
-  int count;                    // list length, or
+  const int4* units;            // (window base, lane mask, pair begin, end)
+  int count;                    // number of units, or
   const int* count_ptr;         //   read from device memory when non-null
-  const int* leaf_pair_begin;   // [leaves + 1] candidate-block range per leaf
   const int* pair_block;        // candidate j-block ...
   const int* pair_entry;        // ... and the gather-list entry it belongs to
-  const int4* items;            // optional (particle, pair begin, end, -)
-                                // instead of list + leaf_pair_begin
   const Entry* entries;
   const float4* bb_lo;          // j-block boxes: lo.xyz, (K h_max)^2
   const float4* bb_hi;
   const int2* bb_fc;            // j-block particle range
+  float3 top_width;             // top-level cell width (frame offsets)
   int* queue;                   // work counter, zero before the launch
   unsigned long long* hits;     // optional: total neighbour hits of the launch
   float band;                   // relative band of the exact predicate
@@ -65,23 +63,26 @@ struct GhostArgs {
   const LeafInfo* leaves;
   float eta_dim, h_tol, h_max, h_min, alpha;
   int iter;                     // 0-based round
-  const int* in_list;           // particles iterating this round
-  int in_count;
-  const int* in_count_ptr;
-  int* out_list;                // particles sent to another round
-  int* out_count;
+  int lo, hi;                   // particle range handled (store order)
+  int* redo_count;              // [max_iter] particles sent to another round
 };
 
-cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_items,
+cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
                           cudaStream_t s);
+cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
+                               const uint8_t* flags, int need,
+                               const int* leaf_pair_begin, int4* units,
+                               int* nunits, const int* gate, cudaStream_t s);
 int noalloc_max_particles();
-cudaError_t launch_density_noalloc(const G2Args& base, const uint8_t* flags,
+int noalloc_max_units();
+cudaError_t launch_density_noalloc(const G2Args& base, const LeafInfo* leaves,
+                                   int nleaves, const int* leaf_pair_begin,
                                    float* fields, int32_t* ngb,
                                    const int32_t* perm, int num_sms,
                                    cudaStream_t s);
 cudaError_t launch_block_hmax(const int2* fc, float4* lo, const float4* posh,
                               int nblocks, cudaStream_t s);
-cudaError_t launch_ghost(const GhostArgs& g, int max_items, cudaStream_t s);
+cudaError_t launch_ghost(const GhostArgs& g, cudaStream_t s);
 cudaError_t launch_begin_step(const DevParticles& p, int max_iter,
                               int* redo_count, cudaStream_t s);
 cudaError_t launch_end_force(const DevParticles& p, cudaStream_t s);

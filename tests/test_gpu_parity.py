@@ -99,3 +99,39 @@ def test_plain_equals_batched(case):
         assert rel_err(b[k], a[k]).max() < 3e-4, (name, k)
     for k in ("ax", "ay", "az", "u_dt", "h_dt"):
         assert scaled_err(b[k], a[k]).max() < 1e-3, (name, k)
+
+
+# --- directly against the reference's own outputs (golden fixtures) ---------
+
+import ast  # noqa: E402
+import glob  # noqa: E402
+import os  # noqa: E402
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))),
+                         ids=lambda p: os.path.basename(p)[:-4])
+def test_gpu_against_reference_golden(path):
+    g = np.load(path)
+    box = getattr(ics, str(g["kind"]))(int(g["n"]), **ast.literal_eval(str(g["gen_kwargs"])))
+    run = ast.literal_eval(str(g["run_kwargs"]))
+    stages = run.pop("stages", api.STAGE_ALL)
+    with api.Space(box, **run) as sp:
+        sp.step(stages)
+        out = sp.download()
+    idx = g["sample"]
+    ref = g["fields"]
+    active = box["time_bin"][idx] <= run.get("max_active_bin", 56)
+    assert active.sum() > 0
+    col = api.FIELD_COLS
+    h = out["fields"][idx][active]
+    r = ref[active]
+    assert np.max(np.abs(h[:, col["h"]] - r[:, 8]) / r[:, 8]) < 2e-4
+    for name, c in (("rho", 9), ("pressure", 11), ("soundspeed", 12)):
+        assert np.max(np.abs(h[:, col[name]] - r[:, c]) / np.abs(r[:, c])) < 3e-4, name
+    if stages & api.STAGE_FORCE:
+        for name, c in (("ax", 15), ("ay", 16), ("az", 17), ("u_dt", 18), ("h_dt", 19)):
+            scale = np.max(np.abs(ref[:, c])) + 1e-30
+            assert np.max(np.abs(h[:, col[name]] - r[:, c])) / scale < 1e-3, name
+        assert np.max(np.abs(h[:, col["v_sig"]] - r[:, 20]) / r[:, 20]) < 3e-4

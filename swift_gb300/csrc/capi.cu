@@ -107,6 +107,8 @@ struct sphgpu_space {
   DBuf<int2> bb_fc;
   DBuf<int4> units;              // gather work groups (device-built)
   int max_units = 0;             // 32-particle windows of all leaves
+  DBuf<int> leaf_window_begin;   // per leaf: its first window
+  std::vector<int> lwb_host;
   std::vector<int> top_leaf;     // per top cell: first leaf (+1 sentinel)
   DBuf<int4> task_units_d, task_units_f;
   DBuf<Entry> task_entries_d, task_entries_f;
@@ -188,7 +190,13 @@ void ensure_device(sphgpu_space* s) {
   for (int g = 0; g < n; g++) s->n_active += fl[g];
   // one work group per 32-particle window of every leaf at most
   s->max_units = 0;
-  for (size_t l = 0; l < lvs.size(); l++) s->max_units += (cells[lvs[l]].count + 31) / 32;
+  std::vector<int> lwb(lvs.size() + 1, 0);
+  for (size_t l = 0; l < lvs.size(); l++) {
+    lwb[l] = s->max_units;
+    s->max_units += (cells[lvs[l]].count + 31) / 32;
+  }
+  lwb[lvs.size()] = s->max_units;
+  s->lwb_host = lwb;
   s->top_leaf.assign(ntop + 1, (int)lvs.size());
   for (int l = (int)lvs.size() - 1; l >= 0; l--) s->top_leaf[cells[lvs[l]].top] = l;
   for (int t = ntop - 1; t >= 0; t--)
@@ -223,6 +231,7 @@ void ensure_device(sphgpu_space* s) {
   s->bb_hi.upload(bhi.data(), nb, st);
   s->bb_fc.upload(bfc.data(), nb, st);
   s->units.alloc(std::max(1, s->max_units));
+  s->leaf_window_begin.upload(lwb.data(), lwb.size(), st);
   s->posh.alloc(n);
   s->dens0.alloc(n);
   s->dens1.alloc(n);
@@ -297,6 +306,7 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   a.top_width = make_float3((float)w[0], (float)w[1], (float)w[2]);
   a.queue = s->queue.p + qslot;
   a.hits = nullptr;
+  a.gate = nullptr;
   if (s->count_hits) a.hits = s->hit_ctr.p + (qslot == 0 ? 0 : (qslot == 2 ? 2 : 1));
   a.band = kBand;
   a.mode = mode;
@@ -311,11 +321,17 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
   const int nl = (int)s->space->leaves().size();
   if (leaf_end < 0) leaf_end = nl;
   CK(cudaMemsetAsync(s->queue.p + qslot, 0, sizeof(int), st));
-  CK(cudaMemsetAsync(s->queue.p + 8 + qslot, 0, sizeof(int), st));
-  CK(launch_build_units(s->leaves.p + leaf_begin, leaf_end - leaf_begin, s->flags.p,
-                        need, dp.lpb.p + leaf_begin, s->units.p,
-                        s->queue.p + 8 + qslot, gate, st));
-  CK(launch_gather(gargs(s, dp, qslot, mode), force, s->num_sms, s->max_units, st));
+  CK(launch_build_units(s->leaves.p + leaf_begin, leaf_end - leaf_begin,
+                        s->leaf_window_begin.p + leaf_begin, s->flags.p, need,
+                        dp.lpb.p + leaf_begin, s->units.p, gate, st));
+  // the groups of this leaf range occupy [w0, w1) of the window slots
+  G2Args a = gargs(s, dp, qslot, mode);
+  const int w0 = s->lwb_host[leaf_begin], w1 = s->lwb_host[leaf_end];
+  a.units = s->units.p + w0;
+  a.count = w1 - w0;
+  a.count_ptr = nullptr;
+  a.gate = gate;  // gated loops (ghost re-runs) do nothing when it reads 0
+  CK(launch_gather(a, force, s->num_sms, w1 - w0, st));
 }
 
 GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
@@ -827,8 +843,8 @@ int sphgpu_density_noalloc(sphgpu_space* s, float* d_fields, int32_t* d_ngb,
                     std::to_string(noalloc_max_units()));
   const cudaError_t e = launch_density_noalloc(
       gargs(s, s->dplan_d, 0, MODE_FIRST), s->leaves.p,
-      (int)s->space->leaves().size(), s->dplan_d.lpb.p, d_fields, d_ngb, s->perm.p,
-      s->num_sms, pick(s, stream));
+      (int)s->space->leaves().size(), s->leaf_window_begin.p, s->max_units,
+      s->dplan_d.lpb.p, d_fields, d_ngb, s->perm.p, s->num_sms, pick(s, stream));
   if (e != cudaSuccess)
     return fail(SPHGPU_ECUDA, std::string("sphgpu_density_noalloc: ") +
                                   cudaGetErrorString(e));

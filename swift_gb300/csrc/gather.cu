@@ -58,13 +58,13 @@ cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_unit
 }
 
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
-                               const uint8_t* flags, int need,
-                               const int* leaf_pair_begin, int4* units,
-                               int* nunits, const int* gate, cudaStream_t s) {
+                               const int* leaf_window_begin, const uint8_t* flags,
+                               int need, const int* leaf_pair_begin, int4* units,
+                               const int* gate, cudaStream_t s) {
   int g = (nleaves * 32 + 255) / 256;
   g = std::max(1, std::min(g, 152 * 16));
-  build_units<<<g, 256, 0, s>>>(leaves, nleaves, flags, need, leaf_pair_begin,
-                                units, nunits, gate);
+  build_units<<<g, 256, 0, s>>>(leaves, nleaves, leaf_window_begin, flags, need,
+                                leaf_pair_begin, units, gate);
   return cudaGetLastError();
 }
 

@@ -115,6 +115,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
   const int lane = threadIdx.x & 31;
   LaneSmem& ws = smem[threadIdx.x >> 5];
   const DevParticles& P = a.p;
+  if (a.gate && *a.gate == 0) return;
   const int nunits = a.count_ptr ? *a.count_ptr : a.count;
   const unsigned lt_mask = (1u << lane) - 1u;
   const float band = a.band;
@@ -125,6 +126,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     u = __shfl_sync(FULL, u, 0);
     if (u >= nunits) break;
     const int4 U = a.units[u];  // base, mask, pair begin, pair end
+    if (U.y == 0) continue;     // no particle of this window takes part
     const bool valid = (U.y >> lane) & 1;
     const int i = U.x + lane;
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), vi = make_float4(0.f, 0.f, 0.f, 1.f);
@@ -372,14 +374,16 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
   }
 }
 
-// Work groups for the gathers: every 32-particle window of every leaf with
-// at least one particle whose flags contain `need`, as
-// (window base, lane mask, candidate-list begin, end).
+// Work groups for the gathers: one slot per 32-particle window of every
+// leaf, in leaf order (so consecutive groups are spatial neighbours and
+// share cache lines), holding (window base, mask of the particles whose
+// flags contain `need`, candidate-list begin, end).  Windows with an empty
+// mask are skipped by the gathers.
 static __global__ void build_units(const LeafInfo* __restrict__ leaves, int nleaves,
-                            const uint8_t* __restrict__ flags, int need,
-                            const int* __restrict__ leaf_pair_begin,
-                            int4* __restrict__ units, int* __restrict__ nunits,
-                            const int* gate) {
+                                   const int* __restrict__ leaf_window_begin,
+                                   const uint8_t* __restrict__ flags, int need,
+                                   const int* __restrict__ leaf_pair_begin,
+                                   int4* __restrict__ units, const int* gate) {
   if (gate && *gate == 0) return;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -387,14 +391,11 @@ static __global__ void build_units(const LeafInfo* __restrict__ leaves, int nlea
   for (int l = warp; l < nleaves; l += nwarps) {
     const int first = leaves[l].first, count = leaves[l].count;
     const int p0 = leaf_pair_begin[l], p1 = leaf_pair_begin[l + 1];
-    if (p0 == p1) continue;
-    for (int w0 = 0; w0 < count; w0 += 32) {
+    int slot = leaf_window_begin[l];
+    for (int w0 = 0; w0 < count; w0 += 32, slot++) {
       const bool ok = w0 + lane < count && (flags[first + w0 + lane] & need) == need;
       const unsigned m = __ballot_sync(FULL, ok);
-      if (m && lane == 0) {
-        const int slot = atomicAdd(nunits, 1);
-        units[slot] = make_int4(first + w0, (int)m, p0, p1);
-      }
+      if (lane == 0) units[slot] = make_int4(first + w0, p0 == p1 ? 0 : (int)m, p0, p1);
     }
   }
 }

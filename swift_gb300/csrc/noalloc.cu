@@ -25,8 +25,8 @@ namespace sphgpu {
 // the scratch below can serve.
 #define NOALLOC_MAX_PARTICLES (1 << 20)
 #define NOALLOC_MAX_UNITS (1 << 16)
-// ints [0] number of work groups, [1] work-queue counter, [2..63] unused;
-// then the work groups (int4 each).
+// ints [0] unused, [1] work-queue counter, [2..63] unused; then the work
+// groups (int4 each, one per 32-particle leaf window).
 #define NOALLOC_UNITS_OFFSET 64
 
 static __device__ __align__(256) int g_noalloc_scratch[NOALLOC_UNITS_OFFSET +
@@ -56,12 +56,14 @@ int noalloc_max_particles() { return NOALLOC_MAX_PARTICLES; }
 int noalloc_max_units() { return NOALLOC_MAX_UNITS; }
 
 cudaError_t launch_density_noalloc(const G2Args& base, const LeafInfo* leaves,
-                                   int nleaves, const int* leaf_pair_begin,
+                                   int nleaves, const int* leaf_window_begin,
+                                   int nwindows, const int* leaf_pair_begin,
                                    float* fields, int32_t* ngb,
                                    const int32_t* perm, int num_sms,
                                    cudaStream_t s) {
   const int n = base.p.n;
-  if (n > NOALLOC_MAX_PARTICLES) return cudaErrorInvalidValue;
+  if (n > NOALLOC_MAX_PARTICLES || nwindows > NOALLOC_MAX_UNITS)
+    return cudaErrorInvalidValue;
   int* scratch = nullptr;
   cudaError_t e = scratch_for_current_device(&scratch);
   if (e != cudaSuccess) return e;
@@ -70,22 +72,23 @@ cudaError_t launch_density_noalloc(const G2Args& base, const LeafInfo* leaves,
   if (e != cudaSuccess) return e;
   int4* units = reinterpret_cast<int4*>(scratch + NOALLOC_UNITS_OFFSET);
   const int g = std::max(1, std::min((nleaves * 32 + 255) / 256, num_sms * 16));
-  build_units<<<g, 256, 0, s>>>(leaves, nleaves, base.p.flags, 1, leaf_pair_begin,
-                                units, scratch, nullptr);
+  build_units<<<g, 256, 0, s>>>(leaves, nleaves, leaf_window_begin, base.p.flags,
+                                1, leaf_pair_begin, units, nullptr);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   G2Args a = base;
   a.units = units;
-  a.count = 0;
-  a.count_ptr = scratch;
+  a.count = nwindows;
+  a.count_ptr = nullptr;
   a.queue = scratch + 1;
   a.hits = nullptr;
+  a.gate = nullptr;
   a.mode = MODE_FIRST;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(
       &per_sm, gather_lanes<false, OUT_CALLER>, WARPS_PER_BLOCK * 32, 0);
   int grid = std::max(1, per_sm) * num_sms;
-  grid = std::max(1, std::min(grid, (n / 32 + nleaves + WARPS_PER_BLOCK - 1) /
+  grid = std::max(1, std::min(grid, (nwindows + WARPS_PER_BLOCK - 1) /
                                         WARPS_PER_BLOCK));
   gather_lanes<false, OUT_CALLER><<<grid, WARPS_PER_BLOCK * 32, 0, s>>>(
       a, CallerOut{fields, ngb, perm});

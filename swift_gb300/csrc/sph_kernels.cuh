@@ -54,6 +54,7 @@ struct G2Args {
   float3 top_width;             // top-level cell width (frame offsets)
   int* queue;                   // work counter, zero before the launch
   unsigned long long* hits;     // optional: total neighbour hits of the launch
+  const int* gate;              // optional: do nothing when *gate == 0
   float band;                   // relative band of the exact predicate
   int mode;                     // GatherMode
 };
@@ -70,13 +71,14 @@ struct GhostArgs {
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
                           cudaStream_t s);
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
-                               const uint8_t* flags, int need,
-                               const int* leaf_pair_begin, int4* units,
-                               int* nunits, const int* gate, cudaStream_t s);
+                               const int* leaf_window_begin, const uint8_t* flags,
+                               int need, const int* leaf_pair_begin, int4* units,
+                               const int* gate, cudaStream_t s);
 int noalloc_max_particles();
 int noalloc_max_units();
 cudaError_t launch_density_noalloc(const G2Args& base, const LeafInfo* leaves,
-                                   int nleaves, const int* leaf_pair_begin,
+                                   int nleaves, const int* leaf_window_begin,
+                                   int nwindows, const int* leaf_pair_begin,
                                    float* fields, int32_t* ngb,
                                    const int32_t* perm, int num_sms,
                                    cudaStream_t s);

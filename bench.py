@@ -234,8 +234,11 @@ def run_ours(args):
     sp = api.Space(box)
     stream = torch.cuda.Stream()
     sh = ctypes_stream(stream)
-    # plan (first step) + warm-up
+    # plan (first step), autotune (tile shape x j-block depth), warm-up
     sp.step(stream=sh)
+    tuning, tune_ms = (sp.autotune(reps=2) if not args.no_tune else
+                       (dict(zip(("threads_per_particle", "jtile", "persistent",
+                                  "block_warps"), sp.tuning())), {}))
     for _ in range(args.warmup):
         sp.step(stream=sh)
     hits = sp.count_hits()
@@ -310,6 +313,7 @@ def run_ours(args):
                 "l2": "inputs larger than L2 (particle state ~150 B/particle)",
                 "parallelism": "replicas" if world > 1 else "single",
                 "interactions_per_step": inter_per_step,
+                "tuning": tuning, "autotune_ms_per_step": tune_ms,
             },
             "phases_ms": {"density": dens_ms, "ghost_rounds": ghost_ms,
                           "force": force_ms},
@@ -318,7 +322,7 @@ def run_ours(args):
                               "force": int(hits[2])},
             "step_tflops": step_flops / t_step / 1e12,
             "roofline": {
-                "bound": "fp32", "kernel": "gather_warp<force>",
+                "bound": "fp32", "kernel": "gather_lanes<force>",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak,
                 "peak_note": f"derived: 152 SMs x 128 FP32 lanes x 2 x {mhz:.0f} MHz "
@@ -368,6 +372,8 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-sample", default="clustered:48")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the default gather configuration")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

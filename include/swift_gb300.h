@@ -75,11 +75,13 @@ typedef struct {
 
 /* Launch configuration of the gather kernels (what the autotuner picks). */
 typedef struct {
-  int32_t threads_per_particle; /* 1, 2, 4 or 8 */
-  int32_t jtile;                /* 64 or 128 partner particles per tile */
+  int32_t threads_per_particle; /* lanes per updated particle: 1 (one warp
+                                   serves a group of up to 32 particles) */
+  int32_t jtile;                /* partner particles per culled j-block:
+                                   16 or 32 */
   int32_t persistent;           /* 1: resident grid + device work queue */
-  int32_t chunk;                /* consecutive particles a warp takes per
-                                   queue pull (1..1024) */
+  int32_t block_warps;          /* tile shape: 8 warps x 3 blocks per SM,
+                                   or 4 warps x 6 blocks per SM */
 } sphgpu_tuning;
 
 int sphgpu_abi_version(void);
@@ -112,6 +114,14 @@ int sphgpu_set_active(sphgpu_space *s, int32_t max_active_bin);
 
 int sphgpu_set_tuning(sphgpu_space *s, const sphgpu_tuning *t);
 int sphgpu_get_tuning(const sphgpu_space *s, sphgpu_tuning *t);
+
+/* Autotuner: times the batched step of this space (CUDA events, `reps`
+ * steps per candidate after one warm-up) for every candidate configuration
+ * (j-block depth x tile shape), keeps the fastest and returns it in *best;
+ * ms[k] receives the mean step time of candidate k (up to 8 candidates,
+ * order: jtile 32/16 x block_warps 8/4), *ncand their number. */
+int sphgpu_autotune(sphgpu_space *s, int32_t reps, sphgpu_tuning *best,
+                    float ms[8], int32_t *ncand);
 
 /* Batched form: density -> ghost -> force over the whole box, one
  * persistent launch per loop, captured as one CUDA graph on the first call

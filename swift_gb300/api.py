@@ -49,7 +49,7 @@ class Params(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("threads_per_particle", ctypes.c_int32),
                 ("jtile", ctypes.c_int32), ("persistent", ctypes.c_int32),
-                ("chunk", ctypes.c_int32)]
+                ("block_warps", ctypes.c_int32)]
 
 
 # Every symbol the header declares, with its ctypes signature.
@@ -84,6 +84,7 @@ SIGNATURES = {
     "sphgpu_phase_times": (ctypes.c_int, [_P, _P, _P, _I32]),
     "sphgpu_count_hits": (ctypes.c_int, [_P, _P]),
     "sphgpu_density_noalloc": (ctypes.c_int, [_P, _P, _P, _P]),
+    "sphgpu_autotune": (ctypes.c_int, [_P, _I32, _P, _P, _P]),
 }
 
 _lib = None
@@ -198,14 +199,28 @@ class Space:
         return geom, ints
 
     # -- configuration -----------------------------------------------------
-    def set_tuning(self, tpi=32, jtile=32, persistent=1, chunk=16):
-        t = Tuning(tpi, jtile, persistent, chunk)
+    def set_tuning(self, tpi=1, jtile=32, persistent=1, block_warps=8):
+        t = Tuning(tpi, jtile, persistent, block_warps)
         _check(lib().sphgpu_set_tuning(self._h, ctypes.byref(t)))
 
     def tuning(self):
         t = Tuning()
         _check(lib().sphgpu_get_tuning(self._h, ctypes.byref(t)))
-        return (t.threads_per_particle, t.jtile, t.persistent, t.chunk)
+        return (t.threads_per_particle, t.jtile, t.persistent, t.block_warps)
+
+    def autotune(self, reps=3):
+        """Pick the fastest gather configuration for this box (native
+        autotuner); returns ({jtile, block_warps, ...}, {config: ms})."""
+        best = Tuning()
+        ms = np.zeros(8, np.float32)
+        n = ctypes.c_int32()
+        _check(lib().sphgpu_autotune(self._h, int(reps), ctypes.byref(best),
+                                     _ptr(ms), ctypes.byref(n)))
+        cands = [(jt, bw) for jt in (32, 16) for bw in (8, 4)]
+        table = {f"jtile={jt},block_warps={bw}": float(ms[k])
+                 for k, (jt, bw) in enumerate(cands[:n.value])}
+        return ({"threads_per_particle": best.threads_per_particle,
+                 "jtile": best.jtile, "block_warps": best.block_warps}, table)
 
     def set_active(self, max_active_bin):
         _check(lib().sphgpu_set_active(self._h, int(max_active_bin)))

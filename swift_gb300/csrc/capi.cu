@@ -78,7 +78,7 @@ struct sphgpu_space {
   std::vector<double> x_in;
   std::vector<float> v_in, m_in, h_in, u_in;
   std::vector<int8_t> tb_in;
-  sphgpu_tuning tune{32, 32, 1, 16};
+  sphgpu_tuning tune{1, 32, 1, 8};
 
   // host plans
   Plan plan_d, plan_s, plan_f;
@@ -105,6 +105,7 @@ struct sphgpu_space {
   DBuf<int> queue, redo;
   DBuf<float4> bb_lo, bb_hi;
   DBuf<int2> bb_fc;
+  int bb_n = 0;
   DBuf<int4> units;              // gather work groups (device-built)
   int max_units = 0;             // 32-particle windows of all leaves
   DBuf<int> leaf_window_begin;   // per leaf: its first window
@@ -142,6 +143,23 @@ namespace {
 void build_plans(sphgpu_space* s) {
   s->space->plan_density(s->plan_d, false);
   s->space->plan_subset(s->plan_s);
+}
+
+// j-block boxes and particle ranges of the current j-block depth.
+void upload_blocks(sphgpu_space* s, cudaStream_t st) {
+  const JBlocks& jb = s->space->jblocks();
+  const size_t nb = jb.first.size();
+  std::vector<float4> blo(nb), bhi(nb);
+  std::vector<int2> bfc(nb);
+  for (size_t b = 0; b < nb; b++) {
+    blo[b] = make_float4(jb.lo[3 * b], jb.lo[3 * b + 1], jb.lo[3 * b + 2], 0.f);
+    bhi[b] = make_float4(jb.hi[3 * b], jb.hi[3 * b + 1], jb.hi[3 * b + 2], 0.f);
+    bfc[b] = make_int2(jb.first[b], jb.count[b]);
+  }
+  s->bb_lo.upload(blo.data(), nb, st);
+  s->bb_hi.upload(bhi.data(), nb, st);
+  s->bb_fc.upload(bfc.data(), nb, st);
+  s->bb_n = (int)nb;
 }
 
 void ensure_device(sphgpu_space* s) {
@@ -206,15 +224,6 @@ void ensure_device(sphgpu_space* s) {
     for (int d = 0; d < 3; d++) tl[3 * (size_t)t + d] = cells[t].loc[d];
   std::vector<LeafInfo> li;
   sp.leaf_infos(li);
-  const JBlocks& jb = sp.jblocks();
-  const size_t nb = jb.first.size();
-  std::vector<float4> blo(nb), bhi(nb);
-  std::vector<int2> bfc(nb);
-  for (size_t b = 0; b < nb; b++) {
-    blo[b] = make_float4(jb.lo[3 * b], jb.lo[3 * b + 1], jb.lo[3 * b + 2], 0.f);
-    bhi[b] = make_float4(jb.hi[3 * b], jb.hi[3 * b + 1], jb.hi[3 * b + 2], 0.f);
-    bfc[b] = make_int2(jb.first[b], jb.count[b]);
-  }
 
   s->xd.upload(xs.data(), xs.size(), st);
   s->velm.upload(vm.data(), n, st);
@@ -227,9 +236,7 @@ void ensure_device(sphgpu_space* s) {
   s->perm.upload(gperm.data(), n, st);
   s->top_loc.upload(tl.data(), tl.size(), st);
   s->leaves.upload(li.data(), li.size(), st);
-  s->bb_lo.upload(blo.data(), nb, st);
-  s->bb_hi.upload(bhi.data(), nb, st);
-  s->bb_fc.upload(bfc.data(), nb, st);
+  upload_blocks(s, st);
   s->units.alloc(std::max(1, s->max_units));
   s->leaf_window_begin.upload(lwb.data(), lwb.size(), st);
   s->posh.alloc(n);
@@ -331,7 +338,7 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
   a.count = w1 - w0;
   a.count_ptr = nullptr;
   a.gate = gate;  // gated loops (ghost re-runs) do nothing when it reads 0
-  CK(launch_gather(a, force, s->num_sms, w1 - w0, st));
+  CK(launch_gather(a, force, s->num_sms, w1 - w0, st, s->tune.block_warps));
 }
 
 GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
@@ -372,7 +379,7 @@ void enqueue_density_ghost(sphgpu_space* s, cudaStream_t st, int stages) {
 }
 
 void enqueue_force(sphgpu_space* s, cudaStream_t st) {
-  CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
+  CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, s->bb_n, st));
   enqueue_gather(s, st, s->dplan_f, 2, MODE_FIRST, true, 1, nullptr);
 }
 
@@ -574,13 +581,32 @@ int sphgpu_space_leaves(const sphgpu_space* s, double* geom, int32_t* ints) {
 
 int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
   if (!s || !t) return fail(SPHGPU_EINVAL, "null argument");
-  if (t->threads_per_particle != 32 || t->jtile != SPH_JBLOCK || t->chunk < 1 ||
-      t->chunk > 1024)
+  if (t->threads_per_particle != 1 || !(t->jtile == 16 || t->jtile == 32) ||
+      !(t->block_warps == 4 || t->block_warps == 8))
     return fail(SPHGPU_EINVAL,
-                "tuning: threads_per_particle 32, jtile 32, chunk in [1, 1024]");
-  s->tune = *t;
-  drop_graph(s);
-  return SPHGPU_OK;
+                "tuning: threads_per_particle 1, jtile 16 or 32, block_warps 4 or 8");
+  return guard([&]() {
+    if (s->dev) CK(cudaStreamSynchronize(s->stream));
+    const bool reblock = t->jtile != s->tune.jtile;
+    s->tune = *t;
+    s->tune.persistent = 1;
+    drop_graph(s);
+    if (reblock) {
+      // blocks, candidate lists and every plan referring to them change
+      s->space->set_jblock(t->jtile);
+      build_plans(s);
+      s->force_planned = false;
+      s->task_d.clear();
+      s->task_f.clear();
+      if (s->dev) {
+        upload_blocks(s, s->stream);
+        s->dplan_d.upload(s->plan_d, s->stream);
+        s->dplan_s.upload(s->plan_s, s->stream);
+        CK(cudaStreamSynchronize(s->stream));
+      }
+    }
+    return SPHGPU_OK;
+  });
 }
 
 int sphgpu_get_tuning(const sphgpu_space* s, sphgpu_tuning* t) {
@@ -773,7 +799,7 @@ int sphgpu_force_from_state(sphgpu_space* s, const float* h, const float* rho,
     s->space->plan_density(pf, true);
     DevPlan dp;
     dp.upload(pf, st);
-    CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
+    CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, s->bb_n, st));
     enqueue_gather(s, st, dp, 3, MODE_FIRST, true, 1, nullptr);
     CK(cudaStreamSynchronize(st));
     // the step's plans assume its own ghost: re-plan on the next step
@@ -781,6 +807,42 @@ int sphgpu_force_from_state(sphgpu_space* s, const float* h, const float* rho,
     drop_graph(s);
     return SPHGPU_OK;
   });
+}
+
+int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms[8],
+                    int32_t* ncand) {
+  if (!s || !best || !ms || !ncand || reps < 1)
+    return fail(SPHGPU_EINVAL, "sphgpu_autotune: null argument or reps < 1");
+  const int jt[2] = {32, 16}, bw[2] = {8, 4};
+  float best_ms = 3.4e38f;
+  sphgpu_tuning bt = s->tune;
+  int k = 0;
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++, k++) {
+      sphgpu_tuning t{1, jt[a], 1, bw[b]};
+      int rc = sphgpu_set_tuning(s, &t);
+      if (rc) return rc;
+      rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);  // plan + capture + warm
+      if (rc) return rc;
+      double sum[3];
+      int64_t n = 0;
+      sphgpu_phase_times(s, sum, &n, 1);
+      for (int r = 0; r < reps; r++) {
+        rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);
+        if (rc) return rc;
+      }
+      sphgpu_phase_times(s, sum, &n, 1);
+      ms[k] = (float)((sum[0] + sum[1] + sum[2]) / std::max<int64_t>(1, n));
+      if (ms[k] < best_ms) {
+        best_ms = ms[k];
+        bt = t;
+      }
+    }
+  *ncand = k;
+  const int rc = sphgpu_set_tuning(s, &bt);
+  if (rc) return rc;
+  *best = bt;
+  return SPHGPU_OK;
 }
 
 int sphgpu_phase_times(sphgpu_space* s, double ms_sum[3], int64_t* steps,
@@ -947,7 +1009,7 @@ static int run_task(sphgpu_space* s, int t, bool force, cudaStream_t st) {
   a.pair_block = force ? s->task_pb_f.p : s->task_pb_d.p;
   a.pair_entry = force ? s->task_pe_f.p : s->task_pe_d.p;
   CK(cudaMemsetAsync(s->queue.p + 4, 0, sizeof(int), st));
-  CK(launch_gather(a, force, s->num_sms, e - b, st));
+  CK(launch_gather(a, force, s->num_sms, e - b, st, s->tune.block_warps));
   return SPHGPU_OK;
 }
 
@@ -1014,7 +1076,7 @@ static void ensure_force_plans(sphgpu_space* s, cudaStream_t st) {
   // the force recursion needs the post-ghost h_max of every cell
   plan_force(s, st);
   ensure_task_plans(s, true);
-  CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
+  CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, s->bb_n, st));
 }
 
 int sphgpu_dosub_self2_force(sphgpu_space* s, int32_t cell, void* stream) {
@@ -1066,7 +1128,7 @@ int sphgpu_step_plain(sphgpu_space* s, void* stream) {
       if (rc) return rc;
     }
     ensure_force_plans(s, st);
-    CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, (int)s->bb_fc.n, st));
+    CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, s->bb_n, st));
     for (size_t t = 0; t < ntasks; t++) {
       rc = run_task(s, (int)t, true, st);
       if (rc) return rc;

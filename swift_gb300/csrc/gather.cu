@@ -38,23 +38,28 @@ __global__ void block_hmax(const int2* __restrict__ fc, float4* __restrict__ lo,
   }
 }
 
-cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
-                          cudaStream_t s) {
+template <bool FORCE, int WPB, int MINB>
+static cudaError_t launch_variant(const G2Args& a, int num_sms, int max_units,
+                                  cudaStream_t s) {
   int per_sm = 0;
-  if (force)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_lanes<true>,
-                                                  WARPS_PER_BLOCK * 32, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_lanes<false>,
-                                                  WARPS_PER_BLOCK * 32, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, gather_lanes<FORCE, OUT_STORE, WPB, MINB>, WPB * 32, 0);
   int grid = std::max(1, per_sm) * num_sms;
-  const int need = (max_units + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
-  grid = std::max(1, std::min(grid, need));
-  if (force)
-    gather_lanes<true><<<grid, WARPS_PER_BLOCK * 32, 0, s>>>(a);
-  else
-    gather_lanes<false><<<grid, WARPS_PER_BLOCK * 32, 0, s>>>(a);
+  grid = std::max(1, std::min(grid, (max_units + WPB - 1) / WPB));
+  gather_lanes<FORCE, OUT_STORE, WPB, MINB><<<grid, WPB * 32, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+// Tile shapes the autotuner chooses from: 8 warps x 3 blocks per SM (up to
+// 85 registers) or 4 warps x 6 blocks per SM (up to 85 registers, finer
+// blocks for the tail of the work queue).
+cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
+                          cudaStream_t s, int block_warps) {
+  if (block_warps == 4)
+    return force ? launch_variant<true, 4, 6>(a, num_sms, max_units, s)
+                 : launch_variant<false, 4, 6>(a, num_sms, max_units, s);
+  return force ? launch_variant<true, 8, 3>(a, num_sms, max_units, s)
+               : launch_variant<false, 8, 3>(a, num_sms, max_units, s);
 }
 
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,

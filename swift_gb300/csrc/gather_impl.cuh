@@ -108,10 +108,10 @@ __device__ __forceinline__ float3 offset_of(int idx, float3 tw) {
 //      queue;
 //   4. when a queue is nearly full all lanes flush: each computes the
 //      interactions of its own queue.  Sums stay in the lane's registers.
-template <bool FORCE, int OUT = OUT_STORE>
-__global__ void __launch_bounds__(WARPS_PER_BLOCK * 32, 3)
+template <bool FORCE, int OUT = OUT_STORE, int WPB = WARPS_PER_BLOCK, int MINB = 3>
+__global__ void __launch_bounds__(WPB * 32, MINB)
 gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
-  __shared__ LaneSmem smem[WARPS_PER_BLOCK];
+  __shared__ LaneSmem smem[WPB];
   const int lane = threadIdx.x & 31;
   LaneSmem& ws = smem[threadIdx.x >> 5];
   const DevParticles& P = a.p;

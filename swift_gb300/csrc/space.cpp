@@ -305,8 +305,8 @@ void Space::build_gpu_order() {
     }
     leaf_block_begin[l] = (int)jb_.first.size();
     const Cell& top = cells_[c.top];
-    for (int b0 = c.first; b0 < c.first + c.count; b0 += SPH_JBLOCK) {
-      const int bc = std::min(SPH_JBLOCK, c.first + c.count - b0);
+    for (int b0 = c.first; b0 < c.first + c.count; b0 += jblock_) {
+      const int bc = std::min(jblock_, c.first + c.count - b0);
       float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
       for (int k = b0; k < b0 + bc; k++) {
         const double* x = &x_[3 * (size_t)gperm_[k]];

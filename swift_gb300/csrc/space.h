@@ -68,6 +68,12 @@ class Space {
   void build(int64_t n, const double* x, const float* h, const int8_t* time_bin);
   void set_activity(int max_active_bin);
   void set_unit_chunk(int c) { unit_chunk_ = c; }
+  // j-block depth (partner particles per culled block, <= 32)
+  void set_jblock(int jb) {
+    jblock_ = jb;
+    build_gpu_order();
+  }
+  int jblock() const { return jblock_; }
 
   // Gather lists: first density pass (second=false) or force pass
   // (second=true, call update_h_after_ghost first); ghost re-runs.
@@ -152,6 +158,7 @@ class Space {
   int cdim_[3] = {0, 0, 0};
   double width_[3] = {0, 0, 0};
   int unit_chunk_ = 128;
+  int jblock_ = SPH_JBLOCK;
   std::vector<double> x_;
   std::vector<float> h_in_, h_;
   std::vector<int8_t> tb_in_;

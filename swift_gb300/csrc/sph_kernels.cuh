@@ -69,7 +69,7 @@ struct GhostArgs {
 };
 
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
-                          cudaStream_t s);
+                          cudaStream_t s, int block_warps = 8);
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                const int* leaf_window_begin, const uint8_t* flags,
                                int need, const int* leaf_pair_begin, int4* units,

@@ -101,6 +101,39 @@ def test_plain_equals_batched(case):
         assert scaled_err(b[k], a[k]).max() < 1e-3, (name, k)
 
 
+@pytest.mark.parametrize("jtile,block_warps", [(32, 4), (16, 8), (16, 4)])
+def test_every_tuning_keeps_parity(case, jtile, block_warps):
+    """Each configuration the autotuner may pick holds the exact-count bar."""
+    name, box, ref = case
+    with api.Space(box) as sp:
+        sp.set_tuning(jtile=jtile, block_warps=block_warps)
+        assert sp.tuning()[1:] == (jtile, 1, block_warps)
+        sp.step(api.STAGE_DENSITY)
+        first = sp.download()
+        sp.step(api.STAGE_ALL)
+        sp.force_from_state(ref["h"], ref["rho"], ref["f"], ref["pressure"],
+                            ref["soundspeed"], ref["balsara"])
+        out = sp.download()
+    assert np.array_equal(first["ngb_first"], ref["ngb_first"]), name
+    assert rel_err(first["d_rho"], ref["d_rho"]).max() < REL, name
+    assert np.array_equal(out["ngb_force"], ref["ngb_force"]), name
+    for k in ("ax", "ay", "az", "u_dt", "h_dt"):
+        assert scaled_err(out[k], ref[k]).max() < REL, (name, k)
+
+
+def test_autotune_picks_a_candidate():
+    box = ics.make("clustered:24", seed=2)
+    with api.Space(box) as sp:
+        sp.step()
+        best, table = sp.autotune(reps=1)
+        assert len(table) == 4 and all(v > 0 for v in table.values())
+        key = f"jtile={best['jtile']},block_warps={best['block_warps']}"
+        assert table[key] == min(table.values())
+        assert sp.tuning()[1] == best["jtile"]
+        sp.step()
+        assert np.all(np.isfinite(sp.download()["ax"]))
+
+
 # --- directly against the reference's own outputs (golden fixtures) ---------
 
 import ast  # noqa: E402

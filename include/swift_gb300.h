@@ -137,8 +137,10 @@ int sphgpu_phase_times(sphgpu_space *s, double ms_sum[3], int64_t *steps,
                        int32_t reset);
 
 /* One instrumented (uncaptured) step that counts neighbour interactions:
- * hits[0] density first pass, [1] density re-runs of the ghost, [2] force. */
-int sphgpu_count_hits(sphgpu_space *s, int64_t hits[3]);
+ * hits[0] density first pass, [1] density re-runs of the ghost, [2] force,
+ * [3] density neighbours at the converged h (the last pass of every active
+ * particle). */
+int sphgpu_count_hits(sphgpu_space *s, int64_t hits[4]);
 
 /* The first density pass of a resident space with no device allocation:
  * for callers that cannot allocate when they run it -- inside CUDA stream

@@ -31,6 +31,9 @@
 #define STAGE_DENSITY 1
 #define STAGE_GHOST 2
 #define STAGE_FORCE 4
+/* Run one full step with every particle active first, then the requested
+ * stages at max_active_bin on the state it leaves (see redrift below). */
+#define STAGE_PRIME 8
 
 struct in_header {
   char magic[8];
@@ -100,6 +103,38 @@ static void collect(const struct cell *c, const struct part *base, int parent,
     for (int k = 0; k < c->hydro.count; k++)
       leaf_of[c->hydro.parts[k].id] = me;
   }
+}
+
+/* State change between the priming step and the measured step, as the
+ * reference's drift does it with a zero drift (cell_drift.c:330-371): active
+ * particles restart from the caller's predicted h (h_in, already inside
+ * [h_min, h_max]), every particle takes the depth_h of its h
+ * (cell_set_part_h_depth, cell.h:1787), every cell its h_max / h_max_active
+ * from its particles, and the unskip sets h_max_old = h_max
+ * (cell_unskip.c:875-880).  Inactive particles keep everything. */
+static void redrift(struct cell *c, const struct engine *e, const float *h_in) {
+  float h_max = 0.f, h_max_active = 0.f;
+  if (c->split) {
+    for (int k = 0; k < 8; k++) {
+      struct cell *cp = c->progeny[k];
+      if (cp == NULL) continue;
+      redrift(cp, e, h_in);
+      h_max = max(h_max, cp->hydro.h_max);
+      h_max_active = max(h_max_active, cp->hydro.h_max_active);
+    }
+  } else {
+    for (int k = 0; k < c->hydro.count; k++) {
+      struct part *p = &c->hydro.parts[k];
+      if (part_is_active(p, e)) p->h = h_in[p->id];
+      cell_set_part_h_depth(p, c);
+      h_max = max(h_max, p->h);
+      if (part_is_active(p, e)) h_max_active = max(h_max_active, p->h);
+    }
+  }
+  c->hydro.h_max = h_max;
+  c->hydro.h_max_active = h_max_active;
+  c->hydro.h_max_old = h_max;
+  c->hydro.dx_max_part_old = 0.f;
 }
 
 int main(int argc, char **argv) {
@@ -188,7 +223,9 @@ int main(int argc, char **argv) {
   e.lightcone_array_properties = &lc;
   e.policy = engine_policy_hydro;
   e.ti_current = 0;
-  e.max_active_bin = (timebin_t)hdr.max_active_bin;
+  /* the tree's h_max_active is built for the first step that runs */
+  e.max_active_bin =
+      (hdr.stages & STAGE_PRIME) ? 127 : (timebin_t)hdr.max_active_bin;
   e.nodeID = 0;
   e.nr_nodes = 1;
   e.nr_threads = 1;
@@ -283,60 +320,75 @@ int main(int argc, char **argv) {
 #define NI 6
   int32_t *ipart = xmalloc(n * NI * sizeof(int32_t));
 
-  if (hdr.stages & STAGE_DENSITY) {
-    for (size_t k = 0; k < s.nr_parts; k++) hydro_init_part(&P[k], &s.hs);
-    for (int t = 0; t < ntasks; t++) {
-      if (tasks[t].type == task_type_self)
-        runner_dosub_self1_density(&r, tasks[t].ci, 0, 0);
-      else
-        runner_dosub_pair1_density(&r, tasks[t].ci, tasks[t].cj, 0, 0);
+  const int prime = (hdr.stages & STAGE_PRIME) != 0;
+  for (int pass = prime ? 0 : 1; pass <= 1; pass++) {
+    int stages = hdr.stages & (STAGE_DENSITY | STAGE_GHOST | STAGE_FORCE);
+    if (pass == 0) {
+      stages = STAGE_DENSITY | STAGE_GHOST | STAGE_FORCE;
+      e.max_active_bin = 127; /* every particle active */
+    } else {
+      e.max_active_bin = (timebin_t)hdr.max_active_bin;
+      if (prime)
+        for (int c = 0; c < ncells; c++)
+          if (s.cells_top[c].hydro.count > 0) redrift(&s.cells_top[c], &e, h);
     }
-    for (size_t k = 0; k < s.nr_parts; k++) {
-      const struct part *p = &P[k];
-      float *o = &res[nf * (size_t)p->id];
-      o[0] = p->rho;
-      o[1] = p->density.rho_dh;
-      o[2] = p->density.wcount;
-      o[3] = p->density.wcount_dh;
-      o[4] = p->density.div_v;
-      o[5] = p->density.rot_v[0];
-      o[6] = p->density.rot_v[1];
-      o[7] = p->density.rot_v[2];
+    if (stages & STAGE_DENSITY) {
+      for (size_t k = 0; k < s.nr_parts; k++)
+        if (pass == 0 || !prime || part_is_active(&P[k], &e))
+          hydro_init_part(&P[k], &s.hs);
+      for (int t = 0; t < ntasks; t++) {
+        if (tasks[t].type == task_type_self)
+          runner_dosub_self1_density(&r, tasks[t].ci, 0, 0);
+        else
+          runner_dosub_pair1_density(&r, tasks[t].ci, tasks[t].cj, 0, 0);
+      }
+      for (size_t k = 0; k < s.nr_parts; k++) {
+        const struct part *p = &P[k];
+        float *o = &res[nf * (size_t)p->id];
+        o[0] = p->rho;
+        o[1] = p->density.rho_dh;
+        o[2] = p->density.wcount;
+        o[3] = p->density.wcount_dh;
+        o[4] = p->density.div_v;
+        o[5] = p->density.rot_v[0];
+        o[6] = p->density.rot_v[1];
+        o[7] = p->density.rot_v[2];
+      }
     }
-  }
-  if (hdr.stages & STAGE_GHOST) {
-    for (int c = 0; c < ncells; c++)
-      runner_do_ghost(&r, &s.cells_top[c], 0, 1, 0);
-    for (size_t k = 0; k < s.nr_parts; k++) {
-      const struct part *p = &P[k];
-      float *o = &res[nf * (size_t)p->id];
-      o[8] = p->h;
-      o[9] = p->rho;
-      o[10] = p->force.f;
-      o[11] = p->force.pressure;
-      o[12] = p->force.soundspeed;
-      o[13] = p->force.balsara;
-      o[14] = p->force.v_sig;
+    if (stages & STAGE_GHOST) {
+      for (int c = 0; c < ncells; c++)
+        runner_do_ghost(&r, &s.cells_top[c], 0, 1, 0);
+      for (size_t k = 0; k < s.nr_parts; k++) {
+        const struct part *p = &P[k];
+        float *o = &res[nf * (size_t)p->id];
+        o[8] = p->h;
+        o[9] = p->rho;
+        o[10] = p->force.f;
+        o[11] = p->force.pressure;
+        o[12] = p->force.soundspeed;
+        o[13] = p->force.balsara;
+        o[14] = p->force.v_sig;
+      }
     }
-  }
-  if (hdr.stages & STAGE_FORCE) {
-    for (int t = 0; t < ntasks; t++) {
-      if (tasks[t].type == task_type_self)
-        runner_dosub_self2_force(&r, tasks[t].ci, 0, 0);
-      else
-        runner_dosub_pair2_force(&r, tasks[t].ci, tasks[t].cj, 0, 0);
-    }
-    for (int c = 0; c < ncells; c++)
-      runner_do_end_hydro_force(&r, &s.cells_top[c], 0);
-    for (size_t k = 0; k < s.nr_parts; k++) {
-      const struct part *p = &P[k];
-      float *o = &res[nf * (size_t)p->id];
-      o[15] = p->a_hydro[0];
-      o[16] = p->a_hydro[1];
-      o[17] = p->a_hydro[2];
-      o[18] = p->u_dt;
-      o[19] = p->force.h_dt;
-      o[20] = p->force.v_sig;
+    if (stages & STAGE_FORCE) {
+      for (int t = 0; t < ntasks; t++) {
+        if (tasks[t].type == task_type_self)
+          runner_dosub_self2_force(&r, tasks[t].ci, 0, 0);
+        else
+          runner_dosub_pair2_force(&r, tasks[t].ci, tasks[t].cj, 0, 0);
+      }
+      for (int c = 0; c < ncells; c++)
+        runner_do_end_hydro_force(&r, &s.cells_top[c], 0);
+      for (size_t k = 0; k < s.nr_parts; k++) {
+        const struct part *p = &P[k];
+        float *o = &res[nf * (size_t)p->id];
+        o[15] = p->a_hydro[0];
+        o[16] = p->a_hydro[1];
+        o[17] = p->a_hydro[2];
+        o[18] = p->u_dt;
+        o[19] = p->force.h_dt;
+        o[20] = p->force.v_sig;
+      }
     }
   }
 

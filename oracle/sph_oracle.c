@@ -1659,15 +1659,67 @@ static void free_space(ospace *s) {
   free(s->links);
 }
 
+/* The state change between the priming step and the measured step: the
+ * reference's drift with a zero drift (cell_drift.c:330-371).  Active
+ * particles restart from the caller's h, every particle takes the depth_h of
+ * its h (cell.h:1787), every cell its h_max / h_max_active from its
+ * particles, and h_max_old = h_max as the unskip sets it
+ * (cell_unskip.c:875-880).  Inactive particles keep their state. */
+static void redrift(const octx *e, ocell *c, const float *h_in) {
+  float h_max = 0.f, h_max_active = 0.f;
+  int any_active = 0;
+  if (c->split) {
+    for (int k = 0; k < 8; k++) {
+      ocell *p = c->progeny[k];
+      if (!p) continue;
+      redrift(e, p, h_in);
+      h_max = fmaxf_ref(h_max, p->h_max);
+      h_max_active = fmaxf_ref(h_max_active, p->h_max_active);
+      any_active |= p->active;
+    }
+  } else {
+    for (int k = 0; k < c->count; k++) {
+      opart *p = &c->parts[k];
+      if (part_active(e, p)) p->h = h_in[p->id];
+      set_h_depth(p, c);
+      h_max = fmaxf_ref(h_max, p->h);
+      if (part_active(e, p)) {
+        h_max_active = fmaxf_ref(h_max_active, p->h);
+        any_active = 1;
+      }
+    }
+  }
+  c->h_max = h_max;
+  c->h_max_active = h_max_active;
+  c->active = any_active;
+  c->h_max_old = h_max;
+}
+
 int sph_oracle_run(const oracle_params *prm, int n, const double *x,
                    const float *v, const float *m, const float *h,
-                   const float *u, const signed char *time_bin, int stages,
+                   const float *u, const signed char *time_bin, int stages_in,
                    oracle_result *res) {
   ospace s;
-  build_space(&s, prm, n, x, v, m, h, u, time_bin);
+  const int prime = (stages_in & ORACLE_STAGE_PRIME) != 0;
+  oracle_params prm0 = *prm;
+  prm0.max_active_bin = 127;
+  build_space(&s, prime ? &prm0 : prm, n, x, v, m, h, u, time_bin);
   const int ntop = s.cdim[0] * s.cdim[1] * s.cdim[2];
   int status = 0;
   for (int k = 0; k < n; k++) init_part(&s.parts[k]);
+  for (int pass = prime ? 0 : 1; pass <= 1; pass++) {
+  int stages = stages_in & (ORACLE_STAGE_DENSITY | ORACLE_STAGE_GHOST |
+                            ORACLE_STAGE_FORCE);
+  if (pass == 0) {
+    stages = ORACLE_STAGE_DENSITY | ORACLE_STAGE_GHOST | ORACLE_STAGE_FORCE;
+  } else if (prime) {
+    s.e.prm = prm;
+    s.e.max_active_bin = prm->max_active_bin;
+    for (int c = 0; c < ntop; c++)
+      if (s.top[c].count > 0) redrift(&s.e, &s.top[c], h);
+    for (int k = 0; k < n; k++)
+      if (part_active(&s.e, &s.parts[k])) init_part(&s.parts[k]);
+  }
   if (stages & ORACLE_STAGE_DENSITY) {
     for (int t = 0; t < s.ntasks; t++) {
       if (!s.tasks[t].is_pair)
@@ -1721,6 +1773,7 @@ int sph_oracle_run(const oracle_params *prm, int n, const double *x,
       o[19] = p->h_dt;
       o[20] = p->v_sig;
     }
+  }
   }
   /* Per-particle tree placement and counters. */
   for (int c = 0; c < s.pool.ncells; c++) {

@@ -7,6 +7,10 @@
 #define ORACLE_STAGE_DENSITY 1
 #define ORACLE_STAGE_GHOST 2
 #define ORACLE_STAGE_FORCE 4
+/* One full step with every particle active runs first; the requested stages
+ * then run at max_active_bin on the state it leaves: active particles
+ * restart from the input h, inactive ones keep their state. */
+#define ORACLE_STAGE_PRIME 8
 
 /* Per-particle float results, in input order (same columns as the
  * reference driver's output block): 0-7 first density pass (rho, rho_dh,

@@ -17,6 +17,8 @@ import numpy as np
 from . import build as _build
 
 STAGE_DENSITY, STAGE_GHOST, STAGE_FORCE, STAGE_ALL = 1, 2, 4, 7
+ALL_ACTIVE = 127  # max_active_bin that activates every time bin
+STAGE_PRIME = 8  # oracle/run flag: a full all-active step runs first
 OK, EINVAL, ECUDA, ENOMEM, ENOCONV, ESTATE, ENODEV = 0, -1, -2, -3, -4, -5, -6
 
 FIELD_COLS = {
@@ -232,6 +234,19 @@ class Space:
     def step_plain(self, stream=None):
         _check(lib().sphgpu_step_plain(self._h, stream))
 
+    def primed_step(self, max_active_bin, stages=STAGE_ALL, plain=False):
+        """Two steps: every particle active, then ``stages`` at
+        ``max_active_bin`` on the state the first leaves (active particles
+        restart from the input h; inactive ones keep h, density and force
+        state, which their active neighbours' loops read)."""
+        self.set_active(ALL_ACTIVE)
+        self.step()
+        self.set_active(max_active_bin)
+        if plain:
+            self.step_plain()
+        else:
+            self.step(stages)
+
     def step_host(self, box=None, fields=None, stream=None):
         b = self._keep if box is None else {
             "x": np.ascontiguousarray(box["x"], np.float64),
@@ -254,8 +269,8 @@ class Space:
 
     def count_hits(self):
         """Neighbour interactions of one pass: density first pass, ghost
-        re-runs, force."""
-        out = np.zeros(3, np.int64)
+        re-runs, force, density at the converged h."""
+        out = np.zeros(4, np.int64)
         _check(lib().sphgpu_count_hits(self._h, _ptr(out)))
         return out
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -83,6 +84,9 @@ struct sphgpu_space {
   // host plans
   Plan plan_d, plan_s, plan_f;
   bool force_planned = false;
+  // the planner's copy of h lags the device's (a ghost ran since it was
+  // last read back)
+  bool h_stale = false;
   // plain-form per-task plans
   std::vector<Plan> task_d, task_f;  // non-empty once the per-task lists exist
   std::vector<std::pair<int, int>> sub_units_of_top;  // subset units per top cell
@@ -97,12 +101,15 @@ struct sphgpu_space {
   DBuf<float2> fin1, hdt_vsig;
   DBuf<float> u, h0, left, right;
   DBuf<uint8_t> flags;
-  DBuf<int8_t> depth_h;
+  DBuf<int8_t> depth_h, depth_h0;
   DBuf<int32_t> leaf_of, ghost_iters, ngb_d, ngb_d_first, ngb_f, perm, top_of;
   DBuf<double> top_loc;
   DBuf<LeafInfo> leaves;
   DevPlan dplan_d, dplan_s, dplan_f;
   DBuf<int> queue, redo;
+  DBuf<int> act_g;     // store indices of the active particles (active_list order)
+  DBuf<float> act_h;   // their h, gathered for the planner
+  int n_act_dev = 0;
   DBuf<float4> bb_lo, bb_hi;
   DBuf<int2> bb_fc;
   int bb_n = 0;
@@ -123,7 +130,8 @@ struct sphgpu_space {
   // The batched step is three graphs (density first pass, ghost rounds,
   // force) so that CUDA events between them time each loop of every step.
   cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double plan_ms = 0;  // host planning inside steps (force re-plans)
   double phase_ms[3] = {0, 0, 0};
   long long phase_steps = 0;
   DBuf<unsigned long long> hit_ctr;
@@ -144,6 +152,8 @@ void build_plans(sphgpu_space* s) {
   s->space->plan_density(s->plan_d, false);
   s->space->plan_subset(s->plan_s);
 }
+
+void upload_activity(sphgpu_space* s, cudaStream_t st);
 
 // j-block boxes and particle ranges of the current j-block depth.
 void upload_blocks(sphgpu_space* s, cudaStream_t st) {
@@ -183,7 +193,7 @@ void ensure_device(sphgpu_space* s) {
   std::vector<float4> vm(n);
   std::vector<float> hs(n), us(n);
   std::vector<uint8_t> fl(n);
-  std::vector<int8_t> dh(n);
+  std::vector<int8_t> dh(n), dh0(n);
   std::vector<int32_t> top(n), lf(n);
   const auto& xw = sp.x();
   const auto& act = sp.active();
@@ -201,6 +211,7 @@ void ensure_device(sphgpu_space* s) {
     us[g] = s->u_in[k];
     fl[g] = act[srt] ? 1 : 0;
     dh[g] = sp.depth_h()[srt];
+    dh0[g] = sp.h_depth_of(s->h_in[k], lvs[leaf_of[srt]]);
     lf[g] = leaf_of[srt];
     top[g] = cells[lvs[leaf_of[srt]]].top;
   }
@@ -230,7 +241,10 @@ void ensure_device(sphgpu_space* s) {
   s->h0.upload(hs.data(), n, st);
   s->u.upload(us.data(), n, st);
   s->flags.upload(fl.data(), n, st);
+  s->n_act_dev = 0;
+  upload_activity(s, st);
   s->depth_h.upload(dh.data(), n, st);
+  s->depth_h0.upload(dh0.data(), n, st);
   s->leaf_of.upload(lf.data(), n, st);
   s->top_of.upload(top.data(), n, st);
   s->perm.upload(gperm.data(), n, st);
@@ -270,6 +284,7 @@ void ensure_device(sphgpu_space* s) {
   P.h0 = s->h0.p;
   P.flags = s->flags.p;
   P.depth_h = s->depth_h.p;
+  P.depth_h0 = s->depth_h0.p;
   P.leaf_of = s->leaf_of.p;
   P.dens0 = s->dens0.p;
   P.dens1 = s->dens1.p;
@@ -394,25 +409,43 @@ int check_conv(sphgpu_space* s, cudaStream_t st) {
   return SPHGPU_OK;
 }
 
-// Smoothing lengths in the reference's sorted order, from the store.
-std::vector<float> sorted_h(sphgpu_space* s, cudaStream_t st) {
-  const int n = s->P.n;
-  std::vector<float4> ph(n);
-  CK(cudaMemcpyAsync(ph.data(), s->posh.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
+// Activity of the store: clears the flags of the previously active
+// particles, sets those of the current active list.
+void upload_activity(sphgpu_space* s, cudaStream_t st) {
+  const auto& al = s->space->active_list();
+  const auto& gos = s->space->gpu_of_sorted();
+  std::vector<int> g(al.size());
+  for (size_t a = 0; a < al.size(); a++) g[a] = gos[al[a]];
+  CK(launch_set_flags(s->flags.p, s->act_g.p, s->n_act_dev, 0, st));
+  s->act_g.upload(g.data(), g.size(), st);
+  s->n_act_dev = (int)g.size();
+  s->n_active = s->n_act_dev;
+  CK(launch_set_flags(s->flags.p, s->act_g.p, s->n_act_dev, 1, st));
+}
+
+// Bring the planner's h up to date: only the active particles' h changes
+// on the device between two activations, so only theirs is read back.
+void fetch_active_h(sphgpu_space* s, cudaStream_t st) {
+  const int m = s->n_act_dev;
+  std::vector<float> h(m);
+  if (m) {
+    if (s->act_h.n < (size_t)m) s->act_h.alloc(m);
+    CK(launch_gather_h(s->posh.p, s->act_g.p, m, s->act_h.p, st));
+    CK(cudaMemcpyAsync(h.data(), s->act_h.p, sizeof(float) * m, cudaMemcpyDeviceToHost, st));
+  }
   CK(cudaStreamSynchronize(st));
-  std::vector<float> h(n);
-  for (int g = 0; g < n; g++) h[s->s_of_g[g]] = ph[g].w;
-  return h;
+  s->space->update_h_active(h.data());
+  s->h_stale = false;
 }
 
 // The force loop's recursion depends on the post-ghost h_max of every cell
 // (cell.h:966-1010 use hydro.h_max); plan it once the ghost has run.
 void plan_force(sphgpu_space* s, cudaStream_t st) {
-  const std::vector<float> h = sorted_h(s, st);
-  s->space->update_h_after_ghost(h.data());
+  fetch_active_h(s, st);
   s->space->plan_density(s->plan_f, true);
   s->dplan_f.upload(s->plan_f, st);
   s->force_planned = true;
+  s->h_stale = false;
 }
 
 cudaStream_t pick(sphgpu_space* s, void* stream) {
@@ -619,6 +652,7 @@ int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     if (s->dev) CK(cudaStreamSynchronize(s->stream));
+    if (s->dev && s->h_stale) fetch_active_h(s, s->stream);
     s->prm.max_active_bin = max_active_bin;
     s->space->set_activity(max_active_bin);
     build_plans(s);
@@ -627,12 +661,7 @@ int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
     s->task_f.clear();
     drop_graph(s);
     if (s->dev) {
-      const int n = s->P.n;
-      std::vector<uint8_t> fl(n);
-      for (int g = 0; g < n; g++) fl[g] = s->space->active()[s->s_of_g[g]] ? 1 : 0;
-      s->n_active = 0;
-      for (int g = 0; g < n; g++) s->n_active += fl[g];
-      s->flags.upload(fl.data(), n, s->stream);
+      upload_activity(s, s->stream);
       s->dplan_d.upload(s->plan_d, s->stream);
       s->dplan_s.upload(s->plan_s, s->stream);
       CK(cudaStreamSynchronize(s->stream));
@@ -651,17 +680,41 @@ int sphgpu_step(sphgpu_space* s, int32_t stages, void* stream) {
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
     if (stages != SPHGPU_STAGE_ALL) {
+      if (stages & SPHGPU_STAGE_GHOST) s->h_stale = true;
       enqueue_density_ghost(s, st, stages);
       if (stages & SPHGPU_STAGE_GHOST) return check_conv(s, st);
       CK(cudaStreamSynchronize(st));
       return SPHGPU_OK;
     }
     if (!s->force_planned) {
-      enqueue_density_ghost(s, st, SPHGPU_STAGE_DENSITY | SPHGPU_STAGE_GHOST);
-      const int rc = check_conv(s, st);
+      // First step on these plans: the force recursion needs the post-ghost
+      // h_max, so density and ghost run, the force loop is planned on the
+      // host, then runs; the graphs are captured at the next step.
+      s->h_stale = true;
+      CK(cudaEventRecord(s->ev[0], st));
+      enqueue_density(s, st, true);
+      CK(cudaEventRecord(s->ev[1], st));
+      enqueue_ghost_rounds(s, st);
+      CK(cudaEventRecord(s->ev[2], st));
+      int rc = check_conv(s, st);
       if (rc != SPHGPU_OK) return rc;
+      const auto t0 = std::chrono::steady_clock::now();
       plan_force(s, st);
+      s->plan_ms += std::chrono::duration<double, std::milli>(
+                        std::chrono::steady_clock::now() - t0).count();
+      CK(cudaEventRecord(s->ev[4], st));
+      enqueue_force(s, st);
+      CK(cudaEventRecord(s->ev[5], st));
+      CK(cudaStreamSynchronize(st));
+      float ms[3] = {0.f, 0.f, 0.f};
+      CK(cudaEventElapsedTime(&ms[0], s->ev[0], s->ev[1]));
+      CK(cudaEventElapsedTime(&ms[1], s->ev[1], s->ev[2]));
+      CK(cudaEventElapsedTime(&ms[2], s->ev[4], s->ev[5]));
+      for (int k = 0; k < 3; k++) s->phase_ms[k] += ms[k];
+      s->phase_steps++;
+      return SPHGPU_OK;
     }
+    s->h_stale = true;
     if (!s->graph[0]) {
       s->graph[0] = capture(st, [&]() { enqueue_density(s, st, true); });
       s->graph[1] = capture(st, [&]() { enqueue_ghost_rounds(s, st); });
@@ -857,7 +910,7 @@ int sphgpu_phase_times(sphgpu_space* s, double ms_sum[3], int64_t* steps,
   return SPHGPU_OK;
 }
 
-int sphgpu_count_hits(sphgpu_space* s, int64_t hits[3]) {
+int sphgpu_count_hits(sphgpu_space* s, int64_t hits[4]) {
   if (!s || !hits) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
@@ -875,12 +928,11 @@ int sphgpu_count_hits(sphgpu_space* s, int64_t hits[3]) {
       throw;
     }
     s->count_hits = false;
+    CK(launch_sum_active_ngb(s->P, s->hit_ctr.p + 3, st));
     rc = check_conv(s, st);
     unsigned long long h[4];
     CK(cudaMemcpy(h, s->hit_ctr.p, sizeof(h), cudaMemcpyDeviceToHost));
-    hits[0] = (int64_t)h[0];
-    hits[1] = (int64_t)h[1];
-    hits[2] = (int64_t)h[2];
+    for (int k = 0; k < 4; k++) hits[k] = (int64_t)h[k];
     return rc;
   });
 }
@@ -1054,6 +1106,7 @@ int sphgpu_do_ghost(sphgpu_space* s, int32_t cell, void* stream) {
     cudaStream_t st = pick(s, stream);
     const Cell& c = s->space->cells()[cell];
     if (c.count == 0 || !c.active) return SPHGPU_OK;
+    s->h_stale = true;
     CK(cudaMemsetAsync(s->redo.p, 0, sizeof(int) * s->prm.max_iter, st));
     for (int k = 0; k < s->prm.max_iter; k++) {
       CK(launch_ghost(ghargs(s, k, c.first, c.first + c.count), st));

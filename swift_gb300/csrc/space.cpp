@@ -19,7 +19,11 @@
 #include "space.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <exception>
+#include <mutex>
+#include <thread>
 #include <cstring>
 #include <stdexcept>
 
@@ -150,6 +154,17 @@ void Space::octant_permute(int first, int n, const double pivot[3],
   for (int b = 0; b < 8; b++) counts[b] = bcount[b];
 }
 
+int8_t Space::h_depth_of(float h, int leaf) const {
+  int c = leaf;
+  if (h < cells_[c].h_min_allowed) return (int8_t)cells_[c].depth;
+  while (c >= 0) {
+    if (h >= cells_[c].h_min_allowed && h < cells_[c].h_max_allowed)
+      return (int8_t)cells_[c].depth;
+    c = cells_[c].parent;
+  }
+  return 0;  // above the top cell: the reference leaves depth_h unchanged
+}
+
 void Space::set_h_depth(int sorted_idx, int leaf) {
   const float h = h_[sorted_idx];
   int c = leaf;
@@ -266,6 +281,13 @@ void Space::build(int64_t n, const double* x, const float* h,
   for (int k = 0; k < n_; k++) inv_perm_[perm_[k]] = k;
   build_top_pairs();
   build_gpu_order();
+  bin_members_.assign(256, {});
+  active_list_.clear();
+  for (int k = 0; k < n_; k++) {
+    bin_members_[tb_in_[perm_[k]] + 128].push_back(k);
+    if (active_[k]) active_list_.push_back(k);
+  }
+  cell_mark_.assign(cells_.size(), 0);
 }
 
 static inline uint32_t spread10(uint32_t v) {
@@ -466,36 +488,137 @@ void Space::build_top_pairs() {
               tasks_.push_back({cid, cjd});
             }
       }
+  top_links_.assign((size_t)cdim[0] * cdim[1] * cdim[2], {});
+  for (int t = 0; t < (int)tasks_.size(); t++) {
+    top_links_[tasks_[t].ci].push_back(t);
+    if (tasks_[t].cj >= 0) top_links_[tasks_[t].cj].push_back(t);
+  }
 }
 
+// Only particles whose h or activity can have changed since the last call
+// -- the previous step's active particles and this step's -- are visited;
+// their leaves are recomputed from their particles and every ancestor from
+// its progeny, which gives the same cells as recomputing the whole tree.
 void Space::set_activity(int max_active_bin) {
   prm_.max_active_bin = max_active_bin;
-  for (int k = 0; k < n_; k++) active_[k] = tb_in_[perm_[k]] <= max_active_bin;
-  for (int cid = 0; cid < cdim_[0] * cdim_[1] * cdim_[2]; cid++)
-    if (cells_[cid].count > 0) refresh_activity(cid);
+  std::vector<int> dirty;
+  auto mark_leaf = [&](int k) {
+    const int c = leaves_[leaf_of_[k]];
+    if (!cell_mark_[c]) {
+      cell_mark_[c] = 1;
+      dirty.push_back(c);
+    }
+  };
+  for (int k : active_list_) {
+    active_[k] = 0;
+    mark_leaf(k);
+  }
+  active_list_.clear();
+  for (int b = 0; b < 256; b++) {
+    if (b - 128 > max_active_bin) break;
+    for (int k : bin_members_[b]) {
+      active_[k] = 1;
+      h_[k] = h_in_[perm_[k]];
+      active_list_.push_back(k);
+      mark_leaf(k);
+    }
+  }
+  for (int c : dirty) redrift_leaf(c);
+  // ancestors, deepest first, each once
+  std::vector<std::vector<int>> by_depth;
+  std::vector<int> anc;
+  for (int c : dirty)
+    for (int p = cells_[c].parent; p >= 0 && !cell_mark_[p]; p = cells_[p].parent) {
+      cell_mark_[p] = 1;
+      const int d = cells_[p].depth;
+      if ((int)by_depth.size() <= d) by_depth.resize(d + 1);
+      by_depth[d].push_back(p);
+    }
+  for (int d = (int)by_depth.size() - 1; d >= 0; d--)
+    anc.insert(anc.end(), by_depth[d].begin(), by_depth[d].end());
+  for (int c : anc) {
+    float h_max = 0.f, h_max_active = 0.f;
+    int any = 0;
+    for (int k = 0; k < 8; k++) {
+      const int p = cells_[c].progeny[k];
+      if (p < 0) continue;
+      h_max = fmaxr(h_max, cells_[p].h_max);
+      h_max_active = fmaxr(h_max_active, cells_[p].h_max_active);
+      any |= cells_[p].active;
+    }
+    cells_[c].h_max = h_max;
+    cells_[c].h_max_active = h_max_active;
+    cells_[c].active = any;
+    cells_[c].h_max_old = h_max;
+  }
+  for (int c : dirty) cell_mark_[c] = 0;
+  for (int c : anc) cell_mark_[c] = 0;
 }
 
-void Space::refresh_activity(int c) {
+void Space::redrift_leaf(int c) {
+  float h_max = 0.f, h_max_active = 0.f;
+  int any = 0;
+  const Cell& cc = cells_[c];
+  for (int k = cc.first; k < cc.first + cc.count; k++) {
+    set_h_depth(k, c);
+    h_max = fmaxr(h_max, h_[k]);
+    if (active_[k]) {
+      h_max_active = fmaxr(h_max_active, h_[k]);
+      any = 1;
+    }
+  }
+  cells_[c].h_max = h_max;
+  cells_[c].h_max_active = h_max_active;
+  cells_[c].active = any;
+  cells_[c].h_max_old = h_max;
+}
+
+void Space::update_h_active(const float* h_active) {
+  // runner_ghost.c:1617-1632: a cell's h_max only grows (atomic max with the
+  // pre-ghost value); only the active particles' h changed.
+  for (size_t a = 0; a < active_list_.size(); a++) {
+    const int k = active_list_[a];
+    const float h = h_active[a];
+    h_[k] = h;
+    for (int c = leaves_[leaf_of_[k]]; c >= 0; c = cells_[c].parent) {
+      if (cells_[c].h_max >= h && cells_[c].h_max_active >= h) break;
+      cells_[c].h_max = fmaxr(cells_[c].h_max, h);
+      cells_[c].h_max_active = fmaxr(cells_[c].h_max_active, h);
+    }
+  }
+}
+
+void Space::assign_h(const float* h_sorted) {
+  for (int k = 0; k < n_; k++) h_[k] = h_sorted[k];
+}
+
+void Space::redrift(int c) {
   Cell& cc = cells_[c];
-  float h_max_active = 0.f;
+  float h_max = 0.f, h_max_active = 0.f;
   int any = 0;
   if (cc.split) {
     for (int k = 0; k < 8; k++) {
       const int p = cells_[c].progeny[k];
       if (p < 0) continue;
-      refresh_activity(p);
+      redrift(p);
+      h_max = fmaxr(h_max, cells_[p].h_max);
       h_max_active = fmaxr(h_max_active, cells_[p].h_max_active);
       any |= cells_[p].active;
     }
   } else {
-    for (int k = cc.first; k < cc.first + cc.count; k++)
+    for (int k = cc.first; k < cc.first + cc.count; k++) {
+      set_h_depth(k, c);
+      h_max = fmaxr(h_max, h_[k]);
       if (active_[k]) {
         h_max_active = fmaxr(h_max_active, h_[k]);
         any = 1;
       }
+    }
   }
+  cells_[c].h_max = h_max;
   cells_[c].h_max_active = h_max_active;
   cells_[c].active = any;
+  cells_[c].h_max_old = h_max;
 }
 
 // ---------------------------------------------------------------------------
@@ -716,120 +839,163 @@ void Space::leaves_under(int c, std::vector<int>& out) const {
 
 void Space::items_to_entries(const std::vector<Item>& items,
                              std::vector<std::vector<Entry>>& per_leaf) const {
+  std::vector<std::pair<int, Entry>> out;
+  items_to_entry_list(items, out);
+  for (auto& le : out) per_leaf[le.first].push_back(le.second);
+}
+
+// Entries of a list of items, as (leaf id, entry) in emission order; leaves
+// without an active particle get none (nothing of theirs is updated).
+void Space::items_to_entry_list(const std::vector<Item>& items,
+                                std::vector<std::pair<int, Entry>>& out) const {
   std::vector<int> lv;
   for (const Item& it : items) {
-    if (it.b < 0) {
+    const int side = it.b < 0 ? it.a : it.b;
+    lv.clear();
+    leaves_under(it.a, lv);
+    for (int L : lv)
+      if (cells_[L].active)
+        out.emplace_back(cells_[L].leaf, make_entry(L, side, it.kind, true, it.shift,
+                                                    side, it.min_depth, it.max_depth));
+    if (it.b >= 0 && it.kind == FRAME_PAIR_CELLREL) {
       lv.clear();
-      leaves_under(it.a, lv);
+      leaves_under(it.b, lv);
       for (int L : lv)
-        per_leaf[cells_[L].leaf].push_back(make_entry(
-            L, it.a, it.kind, true, it.shift, it.a, it.min_depth, it.max_depth));
-    } else {
-      lv.clear();
-      leaves_under(it.a, lv);
-      for (int L : lv)
-        per_leaf[cells_[L].leaf].push_back(make_entry(
-            L, it.b, it.kind, true, it.shift, it.b, it.min_depth, it.max_depth));
-      if (it.kind == FRAME_PAIR_CELLREL) {
-        lv.clear();
-        leaves_under(it.b, lv);
-        for (int L : lv)
-          per_leaf[cells_[L].leaf].push_back(make_entry(
-              L, it.a, it.kind, false, it.shift, it.b, it.min_depth, it.max_depth));
-      }
+        if (cells_[L].active)
+          out.emplace_back(cells_[L].leaf, make_entry(L, it.a, it.kind, false, it.shift,
+                                                      it.b, it.min_depth, it.max_depth));
     }
   }
 }
 
-void Space::plan_density(Plan& plan, bool second) const {
-  std::vector<std::vector<Entry>> per_leaf(leaves_.size());
-  std::vector<Item> items;
-  for (const auto& t : tasks_) {
-    items.clear();
-    if (t.cj < 0)
-      dosub_self(items, t.ci, 0, second);
-    else
-      dosub_pair(items, t.ci, t.cj, 0, second);
-    items_to_entries(items, per_leaf);
+// Planning runs on the host cores: work items are handed out in blocks by an
+// atomic counter; each block keeps its own output, merged in block order so
+// that the plan is the same for any number of threads.
+namespace {
+int planner_threads() {
+  const unsigned t = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(t, 16u));
+}
+
+template <class F>
+void parallel_blocks(int nblocks, F&& body) {
+  const int nt = std::min(planner_threads(), nblocks);
+  if (nt <= 1) {
+    for (int b = 0; b < nblocks; b++) body(b);
+    return;
   }
-  flatten(per_leaf, plan);
+  std::atomic<int> next{0};
+  std::exception_ptr err;
+  std::mutex mu;
+  auto run = [&]() {
+    try {
+      for (int b = next++; b < nblocks; b = next++) body(b);
+    } catch (...) {
+      std::lock_guard<std::mutex> lock(mu);
+      if (!err) err = std::current_exception();
+      next = nblocks;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; t++) pool.emplace_back(run);
+  run();
+  for (auto& th : pool) th.join();
+  if (err) std::rethrow_exception(err);
+}
+}  // namespace
+
+void Space::plan_density(Plan& plan, bool second) const {
+  constexpr int kBlock = 32;  // top-level tasks per work block
+  const int nt = (int)tasks_.size();
+  const int nb = (nt + kBlock - 1) / kBlock;
+  std::vector<std::vector<std::pair<int, Entry>>> outs(nb);
+  parallel_blocks(nb, [&](int blk) {
+    std::vector<Item> items;
+    for (int t = blk * kBlock; t < std::min(nt, (blk + 1) * kBlock); t++) {
+      const TopTask& tk = tasks_[t];
+      if (!cells_[tk.ci].active && (tk.cj < 0 || !cells_[tk.cj].active)) continue;
+      items.clear();
+      if (tk.cj < 0)
+        dosub_self(items, tk.ci, 0, second);
+      else
+        dosub_pair(items, tk.ci, tk.cj, 0, second);
+      items_to_entry_list(items, outs[blk]);
+    }
+  });
+  flatten(outs, plan);
 }
 
 void Space::plan_subset(Plan& plan) const {
   // The ghost re-runs density for the unconverged particles of one leaf
   // through the density tasks linked to the leaf's ancestors
   // (runner_ghost.c:1548-1579); here all tasks hang on top cells.
-  std::vector<std::vector<Entry>> per_leaf(leaves_.size());
-  std::vector<std::vector<int>> links(cells_.size());
-  for (int t = 0; t < (int)tasks_.size(); t++) {
-    links[tasks_[t].ci].push_back(t);
-    if (tasks_[t].cj >= 0) links[tasks_[t].cj].push_back(t);
-  }
-  std::vector<Item> items;
-  for (size_t l = 0; l < leaves_.size(); l++) {
-    const int L = leaves_[l];
-    if (!cells_[L].active) continue;
-    items.clear();
-    for (int finger = L; finger >= 0; finger = cells_[finger].parent) {
-      for (int ti : links[finger]) {
-        const TopTask& t = tasks_[ti];
-        if (t.cj < 0)
-          subset_self(items, finger, L);
-        else
-          subset_pair(items, finger, L, t.ci == finger ? t.cj : t.ci);
+  std::vector<int> act;
+  for (size_t l = 0; l < leaves_.size(); l++)
+    if (cells_[leaves_[l]].active) act.push_back((int)l);
+  constexpr int kBlock = 16;  // leaves per work block
+  const int na = (int)act.size();
+  const int nb = (na + kBlock - 1) / kBlock;
+  std::vector<std::vector<std::pair<int, Entry>>> outs(nb);
+  parallel_blocks(nb, [&](int blk) {
+    std::vector<Item> items;
+    for (int a = blk * kBlock; a < std::min(na, (blk + 1) * kBlock); a++) {
+      const int l = act[a];
+      const int L = leaves_[l];
+      items.clear();
+      for (int finger = L; finger >= 0; finger = cells_[finger].parent) {
+        if (cells_[finger].parent >= 0) continue;  // tasks hang on top cells
+        for (int ti : top_links_[finger]) {
+          const TopTask& t = tasks_[ti];
+          if (t.cj < 0)
+            subset_self(items, finger, L);
+          else
+            subset_pair(items, finger, L, t.ci == finger ? t.cj : t.ci);
+        }
+      }
+      for (const Item& it : items) {
+        // Subset items are always oriented with the leaf's side first.
+        const int side = it.kind == FRAME_SELF_CELLREL ? it.a : it.b;
+        outs[blk].emplace_back(l, make_entry(L, side, it.kind, true, it.shift, side, 0, 127));
       }
     }
-    for (const Item& it : items) {
-      // Subset items are always oriented with the leaf's side first.
-      if (it.kind == FRAME_SELF_CELLREL)
-        per_leaf[l].push_back(make_entry(L, it.a, it.kind, true, it.shift, it.a, 0, 127));
-      else
-        per_leaf[l].push_back(make_entry(L, it.b, it.kind, true, it.shift, it.b, 0, 127));
-    }
-  }
-  flatten(per_leaf, plan);
+  });
+  flatten(outs, plan);
 }
 
-void Space::flatten(const std::vector<std::vector<Entry>>& per_leaf,
+// Plan arrays from (leaf, entry) lists in emission order: entries grouped
+// by leaf (stable), then every leaf's (j-block, entry) candidate pairs.
+void Space::flatten(const std::vector<std::vector<std::pair<int, Entry>>>& outs,
                     Plan& plan) const {
-  plan.entries.clear();
-  plan.units.clear();
-  plan.leaf_entry_begin.assign(leaves_.size() + 1, 0);
-  for (size_t l = 0; l < leaves_.size(); l++) {
-    plan.leaf_entry_begin[l] = (int)plan.entries.size();
-    plan.entries.insert(plan.entries.end(), per_leaf[l].begin(), per_leaf[l].end());
+  const size_t nl = leaves_.size();
+  auto& leb = plan.leaf_entry_begin;
+  leb.assign(nl + 1, 0);
+  for (const auto& o : outs)
+    for (const auto& le : o) leb[le.first + 1]++;
+  for (size_t l = 0; l < nl; l++) leb[l + 1] += leb[l];
+  plan.entries.resize(leb[nl]);
+  std::vector<int> pos(leb.begin(), leb.end() - 1);
+  for (const auto& o : outs)
+    for (const auto& le : o) plan.entries[pos[le.first]++] = le.second;
+  auto& lpb = plan.leaf_pair_begin;
+  lpb.assign(nl + 1, 0);
+  for (size_t l = 0; l < nl; l++) {
+    int np = 0;
+    for (int e = leb[l]; e < leb[l + 1]; e++) np += plan.entries[e].bcount;
+    lpb[l + 1] = lpb[l] + np;
   }
-  plan.leaf_entry_begin[leaves_.size()] = (int)plan.entries.size();
-  plan.pair_block.clear();
-  plan.pair_entry.clear();
-  plan.leaf_pair_begin.assign(leaves_.size() + 1, 0);
-  for (size_t l = 0; l < leaves_.size(); l++) {
-    plan.leaf_pair_begin[l] = (int)plan.pair_block.size();
-    for (int e = plan.leaf_entry_begin[l]; e < plan.leaf_entry_begin[l + 1]; e++) {
+  plan.pair_block.resize(lpb[nl]);
+  plan.pair_entry.resize(lpb[nl]);
+  for (size_t l = 0; l < nl; l++) {
+    int w = lpb[l];
+    for (int e = leb[l]; e < leb[l + 1]; e++) {
       const Entry& E = plan.entries[e];
-      for (int b = E.bfirst; b < E.bfirst + E.bcount; b++) {
-        plan.pair_block.push_back(b);
-        plan.pair_entry.push_back(e);
+      for (int b = E.bfirst; b < E.bfirst + E.bcount; b++, w++) {
+        plan.pair_block[w] = b;
+        plan.pair_entry[w] = e;
       }
     }
   }
-  plan.leaf_pair_begin[leaves_.size()] = (int)plan.pair_block.size();
-  for (size_t l = 0; l < leaves_.size(); l++) {
-    const Cell& c = cells_[leaves_[l]];
-    if (!c.active) continue;
-    const int eb = plan.leaf_entry_begin[l], ee = plan.leaf_entry_begin[l + 1];
-    if (eb == ee) continue;
-    for (int i0 = c.first; i0 < c.first + c.count; i0 += unit_chunk_) {
-      Unit u;
-      u.i_first = i0;
-      u.i_count = std::min(unit_chunk_, c.first + c.count - i0);
-      u.e_begin = eb;
-      u.e_end = ee;
-      u.leaf = (int)l;
-      u.pad = 0;
-      plan.units.push_back(u);
-    }
-  }
+  plan.units.clear();
 }
 
 void Space::leaf_infos(std::vector<LeafInfo>& out) const {

@@ -66,7 +66,21 @@ class Space {
 
   explicit Space(const Params& prm);
   void build(int64_t n, const double* x, const float* h, const int8_t* time_bin);
+  // Start of a step at max_active_bin, with the reference's drift at zero
+  // displacement (cell_drift.c:330-371): active particles restart from the
+  // caller's h (the input h), every particle takes the depth_h of its h,
+  // every cell its h_max / h_max_active from its particles, h_max_old =
+  // h_max.  Inactive particles keep the h of their last step (assign_h).
   void set_activity(int max_active_bin);
+  // Current smoothing lengths of all particles (reference sorted order).
+  void assign_h(const float* h_sorted);
+  // New h of the active particles after a ghost (same order as
+  // active_list()); cells grow their h_max as runner_ghost.c:1617-1632 does.
+  void update_h_active(const float* h_active);
+  // Sorted indices of the active particles, grouped by time bin.
+  const std::vector<int>& active_list() const { return active_list_; }
+  // depth_h that cell_set_part_h_depth (cell.h:1787) gives h in this leaf.
+  int8_t h_depth_of(float h, int leaf_cell) const;
   void set_unit_chunk(int c) { unit_chunk_ = c; }
   // j-block depth (partner particles per culled block, <= 32)
   void set_jblock(int jb) {
@@ -106,7 +120,10 @@ class Space {
   void dosub_pair(std::vector<Item>& out, int ci, int cj, int below, bool second) const;
   void items_to_entries(const std::vector<Item>& items,
                         std::vector<std::vector<Entry>>& per_leaf) const;
-  void flatten(const std::vector<std::vector<Entry>>& per_leaf, Plan& plan) const;
+  void items_to_entry_list(const std::vector<Item>& items,
+                           std::vector<std::pair<int, Entry>>& out) const;
+  void flatten(const std::vector<std::vector<std::pair<int, Entry>>>& outs,
+               Plan& plan) const;
 
  private:
   int getsid_and_swap(int& ci, int& cj, double shift[3]) const;
@@ -118,7 +135,8 @@ class Space {
   void split_geometry(int c);
   void finalize_h(int c);
   void build_top_pairs();
-  void refresh_activity(int c);
+  void redrift(int c);
+  void redrift_leaf(int c);
   void refresh_hmax(int c);
   void emit_pair(std::vector<Item>& out, int ci, int cj, const double shift[3],
                  int lmin, int lmax) const;
@@ -163,6 +181,9 @@ class Space {
   std::vector<float> h_in_, h_;
   std::vector<int8_t> tb_in_;
   std::vector<uint8_t> active_;
+  std::vector<int> active_list_;
+  std::vector<std::vector<int>> bin_members_;  // sorted indices per bin + 128
+  std::vector<uint8_t> cell_mark_;
   std::vector<int8_t> depth_h_;
   std::vector<int> perm_, inv_perm_, leaf_of_, leaves_;
   std::vector<int> gperm_, g_of_s_;
@@ -170,6 +191,7 @@ class Space {
   void build_gpu_order();
   std::vector<Cell> cells_;
   std::vector<TopTask> tasks_;
+  std::vector<std::vector<int>> top_links_;  // per top cell: its tasks, in order
   std::vector<std::pair<int, int>> cpairs_[13];
 };
 

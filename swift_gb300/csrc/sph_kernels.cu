@@ -58,7 +58,6 @@ __global__ void ghost_round(GhostArgs g) {
     const float mass = P.velm[i].w;
     float h_new;
     bool no_ngb = false;
-    bool done = false;
     if ((double)wc < 1.e-5 * (double)SPH_KROOT) {
       no_ngb = true;
       h_new = 2.f * h_old;
@@ -130,7 +129,6 @@ __global__ void ghost_round(GhostArgs g) {
         }
       }
     }
-    done = true;
     // cell_set_part_h_depth (cell.h:1787) on the particle's leaf chain
     const LeafInfo* L = &g.leaves[P.leaf_of[i]];
     if (h < L->hmin[0]) {
@@ -149,18 +147,25 @@ __global__ void ghost_round(GhostArgs g) {
     prepare_force(P, i, h, rho, wc, wc_dh, rho_dh, divv, rx, ry, rz, P.u[i],
                   g.alpha, g.h_max);
     P.flags[i] = fl & ~2;
-    (void)done;
   }
 }
 
+// Start of a step: active particles restart from the input h with cleared
+// sums; inactive ones keep the state of their last step, which the loops of
+// their active neighbours read.
 __global__ void begin_step(DevParticles P, int max_iter, int* redo_count) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid < max_iter) redo_count[tid] = 0;
   for (int i = tid; i < P.n; i += gridDim.x * blockDim.x) {
+    if (!(P.flags[i] & 1)) {
+      P.flags[i] = 0;
+      continue;
+    }
     float4 ph = P.posh[i];
     ph.w = P.h0[i];
     P.posh[i] = ph;
-    P.flags[i] = (P.flags[i] & 1) ? 3 : 0;
+    P.flags[i] = 3;
+    P.depth_h[i] = P.depth_h0[i];
     P.left[i] = 0.f;
     P.right[i] = 3.40282347e+38f;
     P.ghost_iters[i] = 0;
@@ -170,6 +175,32 @@ __global__ void begin_step(DevParticles P, int max_iter, int* redo_count) {
     P.ngb_d_first[i] = 0;
     P.ngb_f[i] = 0;
   }
+}
+
+// Activity flags of a list of particles (bit 0 = active).
+__global__ void set_flags_k(uint8_t* flags, const int* __restrict__ idx, int n,
+                            uint8_t v) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += gridDim.x * blockDim.x)
+    flags[idx[k]] = v;
+}
+
+// Smoothing lengths of a list of particles.
+__global__ void gather_h_k(const float4* __restrict__ posh, const int* __restrict__ idx,
+                           int n, float* out) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += gridDim.x * blockDim.x)
+    out[k] = posh[idx[k]].w;
+}
+
+// Density neighbours at the converged h, summed over the active particles.
+__global__ void sum_active_ngb(DevParticles P, unsigned long long* out) {
+  unsigned long long acc = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n;
+       i += gridDim.x * blockDim.x)
+    if (P.flags[i] & 1) acc += (unsigned long long)P.ngb_d[i];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
 }
 
 __global__ void end_force_k(DevParticles P) {
@@ -260,6 +291,26 @@ cudaError_t launch_ghost(const GhostArgs& g, cudaStream_t s) {
 cudaError_t launch_begin_step(const DevParticles& p, int max_iter,
                               int* redo_count, cudaStream_t s) {
   begin_step<<<grid_for(std::max(p.n, max_iter)), 256, 0, s>>>(p, max_iter, redo_count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_flags(uint8_t* flags, const int* idx, int n, uint8_t v,
+                             cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  set_flags_k<<<grid_for(n), 256, 0, s>>>(flags, idx, n, v);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_h(const float4* posh, const int* idx, int n, float* out,
+                            cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  gather_h_k<<<grid_for(n), 256, 0, s>>>(posh, idx, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum_active_ngb(const DevParticles& p, unsigned long long* out,
+                                  cudaStream_t s) {
+  sum_active_ngb<<<grid_for(p.n), 256, 0, s>>>(p, out);
   return cudaGetLastError();
 }
 

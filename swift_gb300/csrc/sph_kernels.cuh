@@ -17,6 +17,7 @@ struct DevParticles {
   float* h0;            // [n] smoothing length at the start of the step
   uint8_t* flags;       // [n] bit0 active, bit1 needs another ghost round
   int8_t* depth_h;      // [n]
+  const int8_t* depth_h0;  // [n] depth_h of the input h (a step's start)
   int32_t* leaf_of;     // [n]
   // density sums: rho, rho_dh, wcount, wcount_dh | div_v, rot_v[3]
   float4* dens0;
@@ -87,6 +88,12 @@ cudaError_t launch_block_hmax(const int2* fc, float4* lo, const float4* posh,
 cudaError_t launch_ghost(const GhostArgs& g, cudaStream_t s);
 cudaError_t launch_begin_step(const DevParticles& p, int max_iter,
                               int* redo_count, cudaStream_t s);
+cudaError_t launch_set_flags(uint8_t* flags, const int* idx, int n, uint8_t v,
+                             cudaStream_t s);
+cudaError_t launch_gather_h(const float4* posh, const int* idx, int n, float* out,
+                            cudaStream_t s);
+cudaError_t launch_sum_active_ngb(const DevParticles& p, unsigned long long* out,
+                                  cudaStream_t s);
 cudaError_t launch_end_force(const DevParticles& p, cudaStream_t s);
 cudaError_t launch_prepare_posh(DevParticles p, const int32_t* top_of,
                                 const double* top_loc, cudaStream_t s);

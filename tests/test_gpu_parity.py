@@ -134,6 +134,60 @@ def test_autotune_picks_a_candidate():
         assert np.all(np.isfinite(sp.download()["ax"]))
 
 
+# --- sparse activity on carried state --------------------------------------
+
+@pytest.mark.parametrize("cfg,mab", [("sedov:24", 22), ("sedov:32", 21),
+                                     ("clustered:24", 21)])
+def test_primed_sparse_step(cfg, mab, oracle_lib):
+    """An all-active step, then a step at max_active_bin on the state it
+    leaves, against the oracle's same two steps; inactive particles keep
+    their state bit for bit on the GPU."""
+    box = ics.make(cfg, seed=6)
+    if cfg.startswith("clustered"):
+        box["time_bin"][:] = 20 + (np.arange(box["x"].shape[0]) * 7919) % 4
+    ref = oracle_lib.run(box, api.STAGE_PRIME | api.STAGE_ALL, max_active_bin=mab)
+    act = box["time_bin"] <= mab
+    assert 0 < act.sum() < act.size
+    with api.Space(box) as sp:
+        sp.set_active(api.ALL_ACTIVE)
+        sp.step()
+        first = sp.download()
+        sp.set_active(mab)
+        sp.step(api.STAGE_DENSITY)
+        dens = sp.download()
+        sp.step()
+        out = sp.download()
+    # first density pass of the active particles: counts exact
+    assert np.array_equal(dens["ngb_first"][act], ref["ngb_first"][act]), cfg
+    assert rel_err(dens["d_rho"][act], ref["d_rho"][act]).max() < REL
+    # inactive particles: untouched by the second step
+    for k in ("h", "rho", "f", "pressure", "soundspeed", "balsara", "ax", "ay",
+              "az", "u_dt", "h_dt", "v_sig"):
+        assert np.array_equal(out[k][~act], first[k][~act]), k
+    # every particle against the oracle's two steps
+    assert rel_err(out["h"], ref["h"]).max() < 2e-4, cfg
+    for k in ("rho", "pressure", "soundspeed", "v_sig"):
+        assert rel_err(out[k], ref[k]).max() < 3e-4, (cfg, k)
+    for k in ("ax", "ay", "az", "u_dt", "h_dt"):
+        assert scaled_err(out[k][act], ref[k][act]).max() < 1e-3, (cfg, k)
+    assert np.mean(out["ngb_final"][act] == ref["ngb_final"][act]) > 0.99
+
+
+def test_primed_sparse_plain_equals_batched():
+    box = ics.make("sedov:24", seed=8)
+    with api.Space(box) as sp:
+        sp.primed_step(22)
+        a = sp.download()
+    with api.Space(box) as sp:
+        sp.primed_step(22, plain=True)
+        b = sp.download()
+    act = box["time_bin"] <= 22
+    assert np.array_equal(a["ngb_first"][act], b["ngb_first"][act])
+    assert rel_err(b["h"], a["h"]).max() < 2e-4
+    for k in ("ax", "ay", "az", "u_dt"):
+        assert scaled_err(b[k][act], a[k][act]).max() < 1e-3, k
+
+
 # --- directly against the reference's own outputs (golden fixtures) ---------
 
 import ast  # noqa: E402
@@ -151,7 +205,10 @@ def test_gpu_against_reference_golden(path):
     run = ast.literal_eval(str(g["run_kwargs"]))
     stages = run.pop("stages", api.STAGE_ALL)
     with api.Space(box, **run) as sp:
-        sp.step(stages)
+        if stages & api.STAGE_PRIME:
+            sp.primed_step(run["max_active_bin"], stages & api.STAGE_ALL)
+        else:
+            sp.step(stages)
         out = sp.download()
     idx = g["sample"]
     ref = g["fields"]

@@ -203,6 +203,50 @@ int sphgpu_dosub_pair2_force(sphgpu_space *s, int32_t ci, int32_t cj,
                              void *stream);
 int sphgpu_do_end_hydro_force(sphgpu_space *s, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Serving: many independent boxes resident on the device, stepped together
+ * by the same persistent launches (continuous batching).  No counterpart in
+ * the reference, whose engine runs one simulation per process.
+ *
+ * sphgpu_server_create sizes one device arena for max_particles particles
+ * (0: a share of the free HBM) and starts planner_threads host workers
+ * (0: one per core, at most 16).  prm gives the physics (eta, tolerances,
+ * alpha, max_iter) every box shares.
+ * sphgpu_server_submit copies a box (its own dim / periodic /
+ * max_top_level_cells from *box, every particle active) and queues it for
+ * planning; it runs nsteps density -> ghost -> force steps once admitted.
+ * sphgpu_server_pump admits the planned boxes that fit (first come, first
+ * served; admission by free arena ranges), then advances every resident box
+ * by one step and retires the finished ones; when nothing is resident it
+ * first waits up to wait_s for a planner.  *resident: boxes on the device.
+ * sphgpu_server_poll lists finished request ids (each once);
+ * sphgpu_server_fetch copies one finished box out -- fields as
+ * sphgpu_download (24 per particle, input order), ints 4 per particle
+ * (density neighbours first / last pass, force neighbours, ghost
+ * iterations), times = submit, admission, completion (seconds, steady
+ * clock) -- and forgets it.
+ * stats: [0] resident boxes, [1] arena particles in use, [2] arena particle
+ * capacity, [3] boxes waiting or being planned, [4] pumps, [5] boxes
+ * retired, [6] arena bytes, [7] free HBM when the server started. */
+typedef struct sphgpu_server sphgpu_server;
+int sphgpu_server_create(const sphgpu_params *prm, int64_t max_particles,
+                         int32_t planner_threads, sphgpu_server **out);
+int sphgpu_server_destroy(sphgpu_server *s);
+int sphgpu_server_submit(sphgpu_server *s, int64_t id, const sphgpu_params *box,
+                         int64_t n, const double *x, const float *v,
+                         const float *m, const float *h, const float *u,
+                         int32_t nsteps);
+int sphgpu_server_pump(sphgpu_server *s, double wait_s, int32_t *resident);
+int sphgpu_server_poll(sphgpu_server *s, int64_t *ids, int32_t max_ids,
+                       int32_t *count);
+int sphgpu_server_fetch(sphgpu_server *s, int64_t id, float *fields,
+                        int32_t *ints, double times[3]);
+int sphgpu_server_stats(sphgpu_server *s, int64_t stats[8]);
+/* Where the pumps spent their time (seconds): [0] GPU (density, ghost
+ * rounds, force launches), [1] host planning of new boxes' force lists,
+ * [2] admissions (uploads), [3] retirements (read-back). */
+int sphgpu_server_times(sphgpu_server *s, double times[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,16 @@ SIGNATURES = {
     "sphgpu_count_hits": (ctypes.c_int, [_P, _P]),
     "sphgpu_density_noalloc": (ctypes.c_int, [_P, _P, _P, _P]),
     "sphgpu_autotune": (ctypes.c_int, [_P, _I32, _P, _P, _P]),
+    "sphgpu_server_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64, _I32,
+                                            ctypes.POINTER(_P)]),
+    "sphgpu_server_destroy": (ctypes.c_int, [_P]),
+    "sphgpu_server_submit": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(Params),
+                                            ctypes.c_int64, _P, _P, _P, _P, _P, _I32]),
+    "sphgpu_server_pump": (ctypes.c_int, [_P, ctypes.c_double, _P]),
+    "sphgpu_server_poll": (ctypes.c_int, [_P, _P, _I32, _P]),
+    "sphgpu_server_fetch": (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P]),
+    "sphgpu_server_stats": (ctypes.c_int, [_P, _P]),
+    "sphgpu_server_times": (ctypes.c_int, [_P, _P]),
 }
 
 _lib = None
@@ -312,3 +322,86 @@ class Space:
 
     def do_end_hydro_force(self):
         _check(lib().sphgpu_do_end_hydro_force(self._h, None))
+
+
+class Server:
+    """Continuous-batching serving loop: independent boxes resident in one
+    device arena, every resident box advanced one step per ``pump()`` by the
+    same persistent launches (include/swift_gb300.h, sphgpu_server_*)."""
+
+    def __init__(self, max_particles=0, planner_threads=0, **params):
+        L = lib()
+        self.params = make_params({"dim": 1.0}, **params)
+        h = ctypes.c_void_p()
+        _check(L.sphgpu_server_create(ctypes.byref(self.params), int(max_particles),
+                                      int(planner_threads), ctypes.byref(h)))
+        self._h = h
+        self._n = {}
+
+    def close(self):
+        if self._h:
+            lib().sphgpu_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, rid, box, nsteps=10, **params):
+        n = int(box["x"].shape[0])
+        bp = make_params(box, **params)
+        arrs = [np.ascontiguousarray(box["x"], np.float64),
+                np.ascontiguousarray(box["v"], np.float32),
+                np.ascontiguousarray(box["m"], np.float32),
+                np.ascontiguousarray(box["h"], np.float32),
+                np.ascontiguousarray(box["u"], np.float32)]
+        _check(lib().sphgpu_server_submit(self._h, int(rid), ctypes.byref(bp), n,
+                                          *[_ptr(a) for a in arrs], int(nsteps)))
+        self._n[int(rid)] = n
+
+    def pump(self, wait_s=0.0):
+        """Admit what fits, advance every resident box one step, retire the
+        finished ones; returns the number of resident boxes."""
+        r = ctypes.c_int32()
+        _check(lib().sphgpu_server_pump(self._h, float(wait_s), ctypes.byref(r)))
+        return r.value
+
+    def poll(self, max_ids=4096):
+        ids = np.zeros(max_ids, np.int64)
+        c = ctypes.c_int32()
+        _check(lib().sphgpu_server_poll(self._h, _ptr(ids), int(max_ids), ctypes.byref(c)))
+        return [int(i) for i in ids[:c.value]]
+
+    def fetch(self, rid):
+        n = self._n.pop(int(rid))
+        fields = np.zeros((n, 24), np.float32)
+        ints = np.zeros((n, 4), np.int32)
+        t = np.zeros(3, np.float64)
+        _check(lib().sphgpu_server_fetch(self._h, int(rid), _ptr(fields), _ptr(ints), _ptr(t)))
+        out = {"fields": fields, "ints": ints, "t_submit": t[0], "t_admit": t[1],
+               "t_done": t[2]}
+        for name, col in FIELD_COLS.items():
+            out[name] = fields[:, col]
+        for name, col in INT_COLS.items():
+            out[name] = ints[:, col]
+        return out
+
+    def stats(self):
+        st = np.zeros(8, np.int64)
+        _check(lib().sphgpu_server_stats(self._h, _ptr(st)))
+        keys = ("resident", "arena_particles_used", "arena_particles", "waiting",
+                "pumps", "retired", "arena_bytes", "free_hbm_at_start")
+        out = dict(zip(keys, (int(v) for v in st)))
+        t = np.zeros(4, np.float64)
+        _check(lib().sphgpu_server_times(self._h, _ptr(t)))
+        out.update(zip(("gpu_s", "force_plan_s", "admit_s", "retire_s"),
+                       (float(v) for v in t)))
+        return out

@@ -14,51 +14,15 @@
 
 #include "../../include/swift_gb300.h"
 #include "space.h"
+#include "capi_util.h"
 #include "sph_kernels.cuh"
 
 using namespace sphgpu;
+using namespace sphgpu::capi;
+
+thread_local std::string sphgpu::capi::g_err;
 
 namespace {
-
-thread_local std::string g_err;
-
-int fail(int code, const std::string& msg) {
-  g_err = msg;
-  return code;
-}
-
-struct CudaError : std::runtime_error {
-  explicit CudaError(const std::string& m) : std::runtime_error(m) {}
-};
-
-#define CK(call)                                                              \
-  do {                                                                        \
-    cudaError_t e_ = (call);                                                  \
-    if (e_ != cudaSuccess)                                                    \
-      throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));    \
-  } while (0)
-
-template <class T>
-struct DBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  void alloc(size_t count) {
-    release();
-    n = count;
-    if (count == 0) count = 1;
-    CK(cudaMalloc(&p, count * sizeof(T)));
-  }
-  void upload(const T* h, size_t count, cudaStream_t s) {
-    if (count > n) alloc(count);
-    if (count) CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  ~DBuf() { release(); }
-};
 
 struct DevPlan {
   DBuf<Entry> entries;
@@ -326,6 +290,7 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   a.bb_fc = s->bb_fc.p;
   const double* w = s->space->width();
   a.top_width = make_float3((float)w[0], (float)w[1], (float)w[2]);
+  a.leaf_tw = nullptr;
   a.queue = s->queue.p + qslot;
   a.hits = nullptr;
   a.gate = nullptr;
@@ -452,19 +417,6 @@ cudaStream_t pick(sphgpu_space* s, void* stream) {
   return stream ? (cudaStream_t)stream : s->stream;
 }
 
-int guard(const std::function<int()>& f) {
-  try {
-    return f();
-  } catch (const CudaError& e) {
-    return fail(SPHGPU_ECUDA, e.what());
-  } catch (const std::bad_alloc&) {
-    return fail(SPHGPU_ENOMEM, "host allocation failed");
-  } catch (const std::exception& e) {
-    const std::string m = e.what();
-    if (m.find("no CUDA device") != std::string::npos) return fail(SPHGPU_ENODEV, m);
-    return fail(SPHGPU_EINVAL, m);
-  }
-}
 
 void drop_graph(sphgpu_space* s) {
   for (auto& g : s->graph)

@@ -119,7 +119,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
   const int nunits = a.count_ptr ? *a.count_ptr : a.count;
   const unsigned lt_mask = (1u << lane) - 1u;
   const float band = a.band;
-  const float3 tw = a.top_width;
+  float3 tw = a.top_width;
   for (;;) {
     int u = 0;
     if (lane == 0) u = atomicAdd(a.queue, 1);
@@ -127,6 +127,10 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     if (u >= nunits) break;
     const int4 U = a.units[u];  // base, mask, pair begin, pair end
     if (U.y == 0) continue;     // no particle of this window takes part
+    if (a.leaf_tw) {
+      const float4 t = a.leaf_tw[P.leaf_of[U.x]];
+      tw = make_float3(t.x, t.y, t.z);
+    }
     const bool valid = (U.y >> lane) & 1;
     const int i = U.x + lane;
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), vi = make_float4(0.f, 0.f, 0.f, 1.f);

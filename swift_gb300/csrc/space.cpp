@@ -878,8 +878,8 @@ int planner_threads() {
 }
 
 template <class F>
-void parallel_blocks(int nblocks, F&& body) {
-  const int nt = std::min(planner_threads(), nblocks);
+void parallel_blocks(int nthreads, int nblocks, F&& body) {
+  const int nt = std::min(nthreads, nblocks);
   if (nt <= 1) {
     for (int b = 0; b < nblocks; b++) body(b);
     return;
@@ -904,12 +904,14 @@ void parallel_blocks(int nblocks, F&& body) {
 }
 }  // namespace
 
+int Space::threads() const { return threads_ > 0 ? threads_ : planner_threads(); }
+
 void Space::plan_density(Plan& plan, bool second) const {
   constexpr int kBlock = 32;  // top-level tasks per work block
   const int nt = (int)tasks_.size();
   const int nb = (nt + kBlock - 1) / kBlock;
   std::vector<std::vector<std::pair<int, Entry>>> outs(nb);
-  parallel_blocks(nb, [&](int blk) {
+  parallel_blocks(threads(), nb, [&](int blk) {
     std::vector<Item> items;
     for (int t = blk * kBlock; t < std::min(nt, (blk + 1) * kBlock); t++) {
       const TopTask& tk = tasks_[t];
@@ -936,7 +938,7 @@ void Space::plan_subset(Plan& plan) const {
   const int na = (int)act.size();
   const int nb = (na + kBlock - 1) / kBlock;
   std::vector<std::vector<std::pair<int, Entry>>> outs(nb);
-  parallel_blocks(nb, [&](int blk) {
+  parallel_blocks(threads(), nb, [&](int blk) {
     std::vector<Item> items;
     for (int a = blk * kBlock; a < std::min(na, (blk + 1) * kBlock); a++) {
       const int l = act[a];

@@ -88,6 +88,9 @@ class Space {
     build_gpu_order();
   }
   int jblock() const { return jblock_; }
+  // Host threads the planner uses (0: one per core, at most 16).
+  void set_threads(int t) { threads_ = t; }
+  int threads() const;
 
   // Gather lists: first density pass (second=false) or force pass
   // (second=true, call update_h_after_ghost first); ghost re-runs.
@@ -177,6 +180,7 @@ class Space {
   double width_[3] = {0, 0, 0};
   int unit_chunk_ = 128;
   int jblock_ = SPH_JBLOCK;
+  int threads_ = 0;
   std::vector<double> x_;
   std::vector<float> h_in_, h_;
   std::vector<int8_t> tb_in_;

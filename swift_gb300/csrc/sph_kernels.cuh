@@ -53,6 +53,7 @@ struct G2Args {
   const float4* bb_hi;
   const int2* bb_fc;            // j-block particle range
   float3 top_width;             // top-level cell width (frame offsets)
+  const float4* leaf_tw;        // or per leaf (boxes of different sizes)
   int* queue;                   // work counter, zero before the launch
   unsigned long long* hits;     // optional: total neighbour hits of the launch
   const int* gate;              // optional: do nothing when *gate == 0

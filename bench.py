@@ -45,6 +45,9 @@ WORKLOADS = {
     "clustered128": ("clustered", 128, 0.3,
                      "128^3=2,097,152 particles, lattice displaced by a P(k)~k^-2 "
                      "Gaussian random field (rms 0.3 spacing), periodic unit box"),
+    "large384": ("clustered", 384, 1.0,
+                 "384^3=56,623,104 particles, lattice displaced by a P(k)~k^-2 "
+                 "Gaussian random field (rms 1.0 spacing), periodic unit box"),
     "plain32": ("lattice", 32, None,
                 "32^3=32,768 particles, jittered lattice (+/-0.1 spacing), "
                 "Gaussian velocities sigma 0.05"),

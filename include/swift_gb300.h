@@ -78,7 +78,7 @@ typedef struct {
   int32_t threads_per_particle; /* lanes per updated particle: 1 (one warp
                                    serves a group of up to 32 particles) */
   int32_t jtile;                /* partner particles per culled j-block:
-                                   16 or 32 */
+                                   8, 16 or 32 */
   int32_t persistent;           /* 1: resident grid + device work queue */
   int32_t block_warps;          /* tile shape: 8 warps x 3 blocks per SM,
                                    or 4 warps x 6 blocks per SM */
@@ -119,7 +119,7 @@ int sphgpu_get_tuning(const sphgpu_space *s, sphgpu_tuning *t);
  * steps per candidate after one warm-up) for every candidate configuration
  * (j-block depth x tile shape), keeps the fastest and returns it in *best;
  * ms[k] receives the mean step time of candidate k (up to 8 candidates,
- * order: jtile 32/16 x block_warps 8/4), *ncand their number. */
+ * order: jtile 32/16/8 x block_warps 8/4), *ncand their number. */
 int sphgpu_autotune(sphgpu_space *s, int32_t reps, sphgpu_tuning *best,
                     float ms[8], int32_t *ncand);
 

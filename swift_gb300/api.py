@@ -228,7 +228,7 @@ class Space:
         n = ctypes.c_int32()
         _check(lib().sphgpu_autotune(self._h, int(reps), ctypes.byref(best),
                                      _ptr(ms), ctypes.byref(n)))
-        cands = [(jt, bw) for jt in (32, 16) for bw in (8, 4)]
+        cands = [(jt, bw) for jt in (32, 16, 8) for bw in (8, 4)]
         table = {f"jtile={jt},block_warps={bw}": float(ms[k])
                  for k, (jt, bw) in enumerate(cands[:n.value])}
         return ({"threads_per_particle": best.threads_per_particle,

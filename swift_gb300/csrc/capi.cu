@@ -566,10 +566,10 @@ int sphgpu_space_leaves(const sphgpu_space* s, double* geom, int32_t* ints) {
 
 int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
   if (!s || !t) return fail(SPHGPU_EINVAL, "null argument");
-  if (t->threads_per_particle != 1 || !(t->jtile == 16 || t->jtile == 32) ||
+  if (t->threads_per_particle != 1 || !(t->jtile == 8 || t->jtile == 16 || t->jtile == 32) ||
       !(t->block_warps == 4 || t->block_warps == 8))
     return fail(SPHGPU_EINVAL,
-                "tuning: threads_per_particle 1, jtile 16 or 32, block_warps 4 or 8");
+                "tuning: threads_per_particle 1, jtile 8, 16 or 32, block_warps 4 or 8");
   return guard([&]() {
     if (s->dev) CK(cudaStreamSynchronize(s->stream));
     const bool reblock = t->jtile != s->tune.jtile;
@@ -818,11 +818,11 @@ int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms
                     int32_t* ncand) {
   if (!s || !best || !ms || !ncand || reps < 1)
     return fail(SPHGPU_EINVAL, "sphgpu_autotune: null argument or reps < 1");
-  const int jt[2] = {32, 16}, bw[2] = {8, 4};
+  const int jt[3] = {32, 16, 8}, bw[2] = {8, 4};
   float best_ms = 3.4e38f;
   sphgpu_tuning bt = s->tune;
   int k = 0;
-  for (int a = 0; a < 2; a++)
+  for (int a = 0; a < 3; a++)
     for (int b = 0; b < 2; b++, k++) {
       sphgpu_tuning t{1, jt[a], 1, bw[b]};
       int rc = sphgpu_set_tuning(s, &t);

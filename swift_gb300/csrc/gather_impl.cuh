@@ -74,9 +74,9 @@ static __device__ __forceinline__ float h2_exact(float h) {
   return __fmul_rn(__fmul_rn(h, h), SPH_KG2);
 }
 
-// Per-warp shared memory: the staged partner block and each lane's queue
-// of pending hits (partner index and frame-offset index packed in 32 bits).
-#define QCAP 24
+// Per-warp shared memory: the staged partner block and each lane's ring of
+// pending hits (partner index and frame-offset index packed in 32 bits).
+#define QCAP 32  // power of two: ring positions wrap with & (QCAP - 1)
 struct LaneSmem {
   float4 jpos[32];     // staged block: offset xyz in the group's frame, (K h)^2
   int sfirst[32];      // surviving candidate blocks of the current chunk
@@ -85,7 +85,7 @@ struct LaneSmem {
   float4 sf[32];       // their frame offsets (w: frame-offset index)
   float4 slo[32];      // their boxes
   float4 shi[32];
-  int q[QCAP][32];     // per-lane hit queue
+  int q[QCAP][32];     // per-lane hit ring
 };
 
 // Frame offset of a partner top cell from its index in the 3x3x3
@@ -103,11 +103,13 @@ __device__ __forceinline__ float3 offset_of(int idx, float3 tw) {
 //      (skipped when no lane reaches it), then staged in shared memory with
 //      the frame offset applied;
 //   3. every lane tests its own particle against each staged partner
-//      (broadcast reads): FP32 r^2, and inside a 2^-12 band around H^2 the
-//      exact FP64 predicate in the reference frame; hits go to the lane's
-//      queue;
-//   4. when a queue is nearly full all lanes flush: each computes the
-//      interactions of its own queue.  Sums stay in the lane's registers.
+//      (broadcast reads): FP32 r^2 below a 2^-12 band around H^2 is a hit,
+//      pushed to the lane's ring; when any lane saw a candidate inside the
+//      band, the block is scanned again and those candidates are decided
+//      by the exact FP64 predicate in the reference frame;
+//   4. when a ring is nearly full, all lanes compute interactions from
+//      their rings for about as many passes as the rings hold on average;
+//      the last drain empties them.  Sums stay in the lane's registers.
 template <bool FORCE, int OUT = OUT_STORE, int WPB = WARPS_PER_BLOCK, int MINB = 3>
 __global__ void __launch_bounds__(WPB * 32, MINB)
 gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
@@ -172,7 +174,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           s7 = 0.f;
     if (FORCE) s5 = 2.f * fi.w;
     int ngb = 0;
-    int qn = 0;
+    int qh = 0, qt = 0;  // ring head / tail (pending hits: qt - qh)
 
     auto interact = [&](int packed) {
       const int j = packed & 0x07ffffff;
@@ -234,13 +236,32 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
       ngb++;
     };
 
-    auto flush = [&]() {
-      const int m = (int)__reduce_max_sync(FULL, (unsigned)qn);
+    // Hits are computed in passes over the rings: a pass takes the same
+    // ring position from every lane.  A partial drain (when a ring is
+    // nearly full) runs about as many positions as the lanes hold on
+    // average, so that most lanes have work in every pass; the rest stays
+    // queued.  The final drain empties every ring.
+    auto drain = [&](bool all) {
+      const int cnt = qt - qh;
+      const int mx = (int)__reduce_max_sync(FULL, (unsigned)cnt);
+      int m = mx;
+      if (!all) {
+        const int sum = (int)__reduce_add_sync(FULL, (unsigned)cnt);
+        m = min(mx, max(8, (sum + 31) / 32 + 4));
+      }
       __syncwarp();
       for (int k = 0; k < m; k++)
-        if (k < qn) interact(ws.q[k][lane]);
-      qn = 0;
+        if (k < cnt) interact(ws.q[(qh + k) & (QCAP - 1)][lane]);
+      qh += min(m, cnt);
       __syncwarp();
+    };
+    auto push = [&](int v) {
+      ws.q[qt & (QCAP - 1)][lane] = v;
+      qt++;
+    };
+    // at most 8 pushes per lane between two of these checks
+    auto room = [&]() {
+      if (__any_sync(FULL, qt - qh > QCAP - 8)) drain(false);
     };
 
     for (int c0 = U.z; c0 < U.w; c0 += 32) {
@@ -310,29 +331,51 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           ws.jpos[lane] = q;
         }
         __syncwarp();
+        // the lane's own particle never pairs with itself
+        const int tself = (i >= bfirst && i < bfirst + bcount) ? i - bfirst : -1;
+        const int pk = bfirst | (fidx << 27);
+        // Fast pass: FP32 r^2 below the band -> hit; candidates inside the
+        // band around H^2 are only noted, and decided exactly below.
+        bool band_seen = false;
         for (int t = 0; t < bcount; t++) {
           const float4 q = ws.jpos[t];
           const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
           const float r2 = dx * dx + dy * dy + dz * dz;
-          float L2 = lo2, U2 = hi2, H2 = hig2;
+          float L2 = lo2, U2 = hi2;
           if (FORCE) {
-            H2 = fmaxf(hig2, q.w);
+            const float H2 = fmaxf(hig2, q.w);
             L2 = H2 * (1.f - band);
             U2 = H2 * (1.f + band);
           }
-          const int j = bfirst + t;
-          if (mine && r2 < U2 && j != i &&
-              (r2 < L2 || exact_r2_2(P.xd, i, j, E) < H2)) {
-            ws.q[qn][lane] = j | (fidx << 27);
-            qn++;
-          }
-          if ((t & 7) == 7 && __any_sync(FULL, qn > QCAP - 8)) flush();
+          const bool ok = mine && t != tself;
+          if (ok && r2 < L2) push(pk + t);
+          band_seen |= ok && r2 < U2 && !(r2 < L2);
+          if ((t & 7) == 7) room();
         }
-        if (__any_sync(FULL, qn > QCAP - 8)) flush();
+        room();
+        if (__any_sync(FULL, band_seen)) {
+          // exact predicate in the reference frame for the band candidates
+          for (int t = 0; t < bcount; t++) {
+            const float4 q = ws.jpos[t];
+            const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            float L2 = lo2, U2 = hi2, H2 = hig2;
+            if (FORCE) {
+              H2 = fmaxf(hig2, q.w);
+              L2 = H2 * (1.f - band);
+              U2 = H2 * (1.f + band);
+            }
+            if (band_seen && mine && t != tself && r2 < U2 && !(r2 < L2) &&
+                exact_r2_2(P.xd, i, bfirst + t, E) < H2)
+              push(pk + t);
+            if ((t & 7) == 7) room();
+          }
+          room();
+        }
       }
       __syncwarp();
     }
-    flush();
+    drain(true);
     if (!valid) continue;
     if (OUT == OUT_CALLER) {
       const size_t k = (size_t)co.perm[i];

@@ -217,14 +217,18 @@ def run_reference_arm(args):
     return 0
 
 
-def traffic_from_profile():
-    """DRAM bytes per force-gather launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "force_gather_clustered128.md")
+def traffic_from_profile(workload, tuning):
+    """DRAM bytes per force-gather launch from the committed ncu summary of
+    this workload, when it was captured with the same j-block depth."""
+    path = os.path.join(ROOT, "profiles", f"force_gather_{workload}.md")
     try:
         with open(path) as f:
-            for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return float(line.split(":")[1].strip().split()[0])
+            text = f.read()
+        if f"jtile {tuning.get('jtile')}" not in text:
+            return None
+        for line in text.splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1].strip().split()[0])
     except Exception:
         pass
     return None
@@ -404,9 +408,15 @@ def run_ours(args):
     sh = ctypes_stream(stream)
     # plan (first step), autotune (tile shape x j-block depth), warm-up
     sp.step(stream=sh)
-    tuning, tune_ms = (sp.autotune(reps=2) if not args.no_tune else
-                       (dict(zip(("threads_per_particle", "jtile", "persistent",
-                                  "block_warps"), sp.tuning())), {}))
+    if args.tuning:
+        jt, bw = (int(v) for v in args.tuning.split(","))
+        sp.set_tuning(jtile=jt, block_warps=bw)
+        sp.step(stream=sh)
+    if args.no_tune or args.tuning:
+        tuning, tune_ms = (dict(zip(("threads_per_particle", "jtile", "persistent",
+                                     "block_warps"), sp.tuning())), {})
+    else:
+        tuning, tune_ms = sp.autotune(reps=2)
     for _ in range(args.warmup):
         sp.step(stream=sh)
     hits = sp.count_hits()
@@ -495,12 +505,15 @@ def run_ours(args):
                 "peak_note": f"derived: 152 SMs x 128 FP32 lanes x 2 x {mhz:.0f} MHz "
                              "(sm_max_mhz of MEASURED_PEAKS.json; no measured FP32 "
                              "figure there)",
-                "traffic": traffic_from_profile(),
+                "traffic": traffic_from_profile(args.workload, tuning),
             },
             "e2e": {"value": total_inter / e2e_s, "unit": UNIT,
                     "h2d_bytes_per_step": int(n * (24 + 12 + 4 + 4 + 4)),
                     "d2h_bytes_per_step": int(n * 24 * 4)},
-            "gpu_launches": 64 * args.steps,
+            # per step: begin-step, density units + gather, 30 ghost rounds
+            # (ghost, units, re-run gather; gated ones return at once),
+            # block h_max, force units + gather
+            "gpu_launches": 96 * args.steps,
             "clocks": clk,
             "cpu_baseline": cb,
         }
@@ -545,6 +558,8 @@ def main():
                     help="sparse workload: steps timed in the plain form")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default gather configuration")
+    ap.add_argument("--tuning", default="",
+                    help="JTILE,BLOCK_WARPS: fixed gather configuration, no autotune")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

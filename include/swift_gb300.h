@@ -109,6 +109,23 @@ int sphgpu_space_cells(const sphgpu_space *s, int32_t *out);
  * [leaves][3] = first, count, depth (may be NULL). */
 int sphgpu_space_leaves(const sphgpu_space *s, double *geom, int32_t *ints);
 
+/* The cell tree: int32 [ncells][5] = first particle (cell-sorted order),
+ * count, depth, parent cell (-1 at the top), top-level cell; records may be
+ * NULL to read *ncells only.  Cell ids index sphgpu_cell_sort. */
+int sphgpu_space_tree(const sphgpu_space *s, int32_t *ncells, int32_t *records);
+
+/* Replaces runner_do_hydro_sort (runner_sort.c:203) for the whole tree at
+ * once: for every non-empty cell and every axis j set in flags (13 axes,
+ * sort_part.h:42-57) the keys d = (float)(x . axis_j) of the cell's
+ * particles, ascending with their indices in the cell, plus a sentinel
+ * {FLT_MAX, 0} -- bit-identical to the reference's arrays (its leaf
+ * quicksort and 8-way merge, ties included).  Built on the device. */
+int sphgpu_hydro_sort(sphgpu_space *s, int32_t flags, void *stream);
+/* Copies sort array `axis` of one cell (count + 1 entries) to the host, the
+ * array cell_get_hydro_sorts (cell.h:1471) returns in the reference. */
+int sphgpu_cell_sort(sphgpu_space *s, int32_t cell, int32_t axis, float *d,
+                     int32_t *idx);
+
 /* Change the active set (particles with time_bin <= max_active_bin). */
 int sphgpu_set_active(sphgpu_space *s, int32_t max_active_bin);
 

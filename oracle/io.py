@@ -102,8 +102,29 @@ def ref_harness_path(mode="parity"):
     return os.path.join(here, "_ref", mode, "bin", "ref_harness")
 
 
-def run_reference(box, workdir, stages=ALL_STAGES, mode="parity", **overrides):
-    """Run the reference's own loops (oracle/_ref) on ``box``."""
+def read_sorts(path):
+    """Sort arrays written by the harness: a list of (first, count, depth,
+    d[13][count+1] float32, i[13][count+1] int32), cells depth first."""
+    out = []
+    with open(path, "rb") as f:
+        if f.read(8) != b"SPHSRT01":
+            raise ValueError("not a sort dump")
+        while True:
+            rec = f.read(12)
+            if len(rec) < 12:
+                break
+            first, count, depth = np.frombuffer(rec, np.int32)
+            ent = np.frombuffer(f.read(13 * (int(count) + 1) * 8), dtype=[("d", "<f4"), ("i", "<i4")])
+            ent = ent.reshape(13, int(count) + 1)
+            out.append((int(first), int(count), int(depth),
+                        np.ascontiguousarray(ent["d"]), np.ascontiguousarray(ent["i"])))
+    return out
+
+
+def run_reference(box, workdir, stages=ALL_STAGES, mode="parity", sorts=False,
+                  **overrides):
+    """Run the reference's own loops (oracle/_ref) on ``box``; with
+    ``sorts`` also return the reference's sort arrays (key "sorts")."""
     exe = ref_harness_path(mode)
     for k in ("max_active_bin",):
         if k in box and k not in overrides:
@@ -113,5 +134,11 @@ def run_reference(box, workdir, stages=ALL_STAGES, mode="parity", **overrides):
     inp = os.path.join(workdir, "ref_in.bin")
     out = os.path.join(workdir, "ref_out.bin")
     write_input(inp, box, stages, **overrides)
-    subprocess.run([exe, inp, out], check=True, capture_output=True)
-    return read_output(out)
+    args = [exe, inp, out]
+    if sorts:
+        args.append(os.path.join(workdir, "ref_sorts.bin"))
+    subprocess.run(args, check=True, capture_output=True)
+    res = read_output(out)
+    if sorts:
+        res["sorts"] = read_sorts(args[3])
+    return res

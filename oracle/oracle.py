@@ -134,3 +134,36 @@ def exact64(box, out):
                          *[_ptr(a, ctypes.c_float) for a in arrs],
                          _ptr(res, ctypes.c_double))
     return res
+
+
+def tree_sorts(box, **kw):
+    """The restated reference sort arrays of every non-empty cell, depth
+    first, as (first, count, depth, d[13][count+1], i[13][count+1])."""
+    L = lib()
+    n = box["x"].shape[0]
+    arrs = [np.ascontiguousarray(box["x"], np.float64),
+            np.ascontiguousarray(box["v"], np.float32),
+            np.ascontiguousarray(box["m"], np.float32),
+            np.ascontiguousarray(box["h"], np.float32),
+            np.ascontiguousarray(box["u"], np.float32)]
+    tb = np.ascontiguousarray(box["time_bin"], np.int8)
+    types = [ctypes.c_double] + [ctypes.c_float] * 4
+    ptrs = [_ptr(a, t) for a, t in zip(arrs, types)]
+    prm = make_params(box, **kw)
+    nc = ctypes.c_int32()
+    ne = ctypes.c_int64()
+    L.sph_oracle_tree_sorts(ctypes.byref(prm), ctypes.c_int(n), *ptrs, _ptr(tb, ctypes.c_byte),
+                            ctypes.byref(nc), ctypes.byref(ne), None, None, None)
+    rec = np.zeros((nc.value, 3), np.int32)
+    d = np.zeros(ne.value, np.float32)
+    idx = np.zeros(ne.value, np.int32)
+    L.sph_oracle_tree_sorts(ctypes.byref(prm), ctypes.c_int(n), *ptrs, _ptr(tb, ctypes.c_byte),
+                            ctypes.byref(nc), ctypes.byref(ne), _ptr(rec, ctypes.c_int32),
+                            _ptr(d, ctypes.c_float), _ptr(idx, ctypes.c_int32))
+    out, off = [], 0
+    for first, count, depth in rec:
+        k = 13 * (int(count) + 1)
+        out.append((int(first), int(count), int(depth),
+                    d[off:off + k].reshape(13, -1), idx[off:off + k].reshape(13, -1)))
+        off += k
+    return out

@@ -18,6 +18,10 @@
  * Input  (argv[1]): "SPHIN001" header + SoA arrays (see oracle/io.py).
  * Output (argv[2]): "SPHOUT01" header + per-particle results in input order,
  *                   followed by the cell tree in depth-first order.
+ * Optional (argv[3]): "SPHSRT01" + the 13 sort arrays of every non-empty
+ *                   cell, depth first: per cell int32 first (cell-sorted
+ *                   order), count, depth, then 13 x (count + 1) entries
+ *                   {float d; int i} as runner_do_hydro_sort left them.
  */
 #include <stdint.h>
 #include <stdio.h>
@@ -135,6 +139,18 @@ static void redrift(struct cell *c, const struct engine *e, const float *h_in) {
   c->hydro.h_max_active = h_max_active;
   c->hydro.h_max_old = h_max;
   c->hydro.dx_max_part_old = 0.f;
+}
+
+static void dump_sorts(FILE *f, const struct cell *c, const struct part *base) {
+  if (c->hydro.count == 0) return;
+  const int32_t rec[3] = {(int32_t)(c->hydro.parts - base), c->hydro.count, c->depth};
+  fwrite(rec, sizeof(int32_t), 3, f);
+  for (int j = 0; j < 13; j++)
+    fwrite(cell_get_hydro_sorts(c, j), sizeof(struct sort_entry),
+           (size_t)c->hydro.count + 1, f);
+  if (c->split)
+    for (int k = 0; k < 8; k++)
+      if (c->progeny[k] != NULL) dump_sorts(f, c->progeny[k], base);
 }
 
 int main(int argc, char **argv) {
@@ -272,6 +288,14 @@ int main(int argc, char **argv) {
   for (int c = 0; c < ncells; c++)
     if (s.cells_top[c].hydro.count > 0)
       runner_do_hydro_sort(&r, &s.cells_top[c], 0x1FFF, 0, 0, 0, 0);
+
+  if (argc > 3) {
+    FILE *fs = fopen(argv[3], "wb");
+    if (!fs) return 2;
+    fwrite("SPHSRT01", 1, 8, fs);
+    for (int c = 0; c < ncells; c++) dump_sorts(fs, &s.cells_top[c], s.parts);
+    fclose(fs);
+  }
 
   /* Task list: one self task per non-empty top cell, one pair task per
    * neighbouring non-empty top-cell pair (26-neighbourhood, periodic). */

@@ -1806,6 +1806,48 @@ int sph_oracle_run(const oracle_params *prm, int n, const double *x,
 }
 
 /* ------------------------------------------------------------------------ */
+/* Sort arrays of the whole tree (runner_sort.c:203-463), depth first over
+ * the non-empty cells: records [first, count, depth] and 13 arrays of
+ * count + 1 entries per cell.  With rec == NULL only the sizes are
+ * returned. */
+
+static void walk_sorts(const ospace *s, const ocell *c, int32_t *ncells,
+                       int64_t *nent, int32_t *rec, float *d, int32_t *idx) {
+  if (c->count == 0) return;
+  if (rec) {
+    int32_t *r = rec + 3 * (size_t)*ncells;
+    r[0] = (int32_t)(c->parts - s->parts);
+    r[1] = c->count;
+    r[2] = c->depth;
+    for (int j = 0; j < 13; j++)
+      for (int k = 0; k <= c->count; k++) {
+        d[*nent + (int64_t)j * (c->count + 1) + k] = c->sort[j][k].d;
+        idx[*nent + (int64_t)j * (c->count + 1) + k] = c->sort[j][k].i;
+      }
+  }
+  *ncells += 1;
+  *nent += 13 * (int64_t)(c->count + 1);
+  if (c->split)
+    for (int k = 0; k < 8; k++)
+      if (c->progeny[k]) walk_sorts(s, c->progeny[k], ncells, nent, rec, d, idx);
+}
+
+int sph_oracle_tree_sorts(const oracle_params *prm, int n, const double *x,
+                          const float *v, const float *m, const float *h,
+                          const float *u, const signed char *time_bin,
+                          int32_t *ncells, int64_t *nentries, int32_t *rec,
+                          float *d, int32_t *idx) {
+  ospace s;
+  build_space(&s, prm, n, x, v, m, h, u, time_bin);
+  const int ntop = s.cdim[0] * s.cdim[1] * s.cdim[2];
+  *ncells = 0;
+  *nentries = 0;
+  for (int c = 0; c < ntop; c++) walk_sorts(&s, &s.top[c], ncells, nentries, rec, d, idx);
+  free_space(&s);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* FP64 brute-force density/force over a cell list, for error statements.
  * Computes, for every particle with the given h, the double-precision
  * density sums and the force sums over all j != i with r < gamma*h (density)

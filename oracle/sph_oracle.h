@@ -44,6 +44,16 @@ int sph_oracle_run(const oracle_params *prm, int n, const double *x,
                    const float *u, const signed char *time_bin, int stages,
                    oracle_result *res);
 
+/* Sort arrays of every non-empty cell, depth first: rec [ncells][3] =
+ * first (cell-sorted order), count, depth; d / idx: per cell 13 arrays of
+ * count + 1 entries (keys ascending, FLT_MAX sentinel).  Call with
+ * rec == NULL for the sizes. */
+int sph_oracle_tree_sorts(const oracle_params *prm, int n, const double *x,
+                          const float *v, const float *m, const float *h,
+                          const float *u, const signed char *time_bin,
+                          int32_t *ncells, int64_t *nentries, int32_t *rec,
+                          float *d, int32_t *idx);
+
 void sph_oracle_exact64(const oracle_params *prm, int n, const double *x,
                         const float *v, const float *m, const float *h,
                         const float *rho, const float *f, const float *P,

@@ -87,6 +87,9 @@ SIGNATURES = {
     "sphgpu_count_hits": (ctypes.c_int, [_P, _P]),
     "sphgpu_density_noalloc": (ctypes.c_int, [_P, _P, _P, _P]),
     "sphgpu_autotune": (ctypes.c_int, [_P, _I32, _P, _P, _P]),
+    "sphgpu_hydro_sort": (ctypes.c_int, [_P, _I32, _P]),
+    "sphgpu_space_tree": (ctypes.c_int, [_P, _P, _P]),
+    "sphgpu_cell_sort": (ctypes.c_int, [_P, _I32, _I32, _P, _P]),
     "sphgpu_server_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64, _I32,
                                             ctypes.POINTER(_P)]),
     "sphgpu_server_destroy": (ctypes.c_int, [_P]),
@@ -219,6 +222,23 @@ class Space:
         t = Tuning()
         _check(lib().sphgpu_get_tuning(self._h, ctypes.byref(t)))
         return (t.threads_per_particle, t.jtile, t.persistent, t.block_warps)
+
+    def tree(self):
+        """Cell records: first, count, depth, parent, top (one row per cell)."""
+        n = ctypes.c_int32()
+        _check(lib().sphgpu_space_tree(self._h, ctypes.byref(n), None))
+        rec = np.zeros((n.value, 5), np.int32)
+        _check(lib().sphgpu_space_tree(self._h, ctypes.byref(n), _ptr(rec)))
+        return rec
+
+    def hydro_sort(self, flags=0x1FFF):
+        _check(lib().sphgpu_hydro_sort(self._h, int(flags), None))
+
+    def cell_sort(self, cell, axis, count):
+        d = np.zeros(count + 1, np.float32)
+        i = np.zeros(count + 1, np.int32)
+        _check(lib().sphgpu_cell_sort(self._h, int(cell), int(axis), _ptr(d), _ptr(i)))
+        return d, i
 
     def autotune(self, reps=3):
         """Pick the fastest gather configuration for this box (native

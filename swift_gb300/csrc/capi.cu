@@ -15,6 +15,7 @@
 #include "../../include/swift_gb300.h"
 #include "space.h"
 #include "capi_util.h"
+#include "sort.cuh"
 #include "sph_kernels.cuh"
 
 using namespace sphgpu;
@@ -100,6 +101,15 @@ struct sphgpu_space {
   long long phase_steps = 0;
   DBuf<unsigned long long> hit_ctr;
   bool count_hits = false;
+  // per-cell sort arrays (sphgpu_hydro_sort)
+  DBuf<SortCell> sort_cells;
+  DBuf<int> sort_leaf_ids, sort_split_ids, g_of_s_dev;
+  DBuf<float> sort_d;
+  DBuf<int> sort_i;
+  std::vector<int> sc_of_cell;            // cell -> SortCell index (-1: empty)
+  std::vector<SortCell> sc_host;
+  std::vector<int> split_begin, split_n;  // per depth, into sort_split_ids
+  int sort_nleaves = 0, sort_max_depth = 0, sorted_mask = 0;
 
   ~sphgpu_space() {
     for (auto& g : graph)
@@ -810,6 +820,118 @@ int sphgpu_force_from_state(sphgpu_space* s, const float* h, const float* rho,
     // the step's plans assume its own ghost: re-plan on the next step
     s->force_planned = false;
     drop_graph(s);
+    return SPHGPU_OK;
+  });
+}
+
+static void build_sort_tree(sphgpu_space* s, cudaStream_t st) {
+  const Space& sp = *s->space;
+  const auto& cells = sp.cells();
+  const int nc = (int)cells.size();
+  s->sc_of_cell.assign(nc, -1);
+  s->sc_host.clear();
+  long long off = 0;
+  int maxd = 0;
+  for (int c = 0; c < nc; c++) {
+    if (cells[c].count == 0) continue;
+    s->sc_of_cell[c] = (int)s->sc_host.size();
+    SortCell sc;
+    sc.off = off;
+    sc.first = cells[c].first;
+    sc.count = cells[c].count;
+    for (int k = 0; k < 8; k++) sc.progeny[k] = -1;
+    s->sc_host.push_back(sc);
+    off += 13LL * (cells[c].count + 1);
+    maxd = std::max(maxd, cells[c].depth);
+  }
+  std::vector<int> leaves;
+  std::vector<std::vector<int>> split(maxd + 1);
+  for (int c = 0; c < nc; c++) {
+    const int k = s->sc_of_cell[c];
+    if (k < 0) continue;
+    if (cells[c].split) {
+      for (int q = 0; q < 8; q++) {
+        const int p = cells[c].progeny[q];
+        if (p >= 0) s->sc_host[k].progeny[q] = s->sc_of_cell[p];
+      }
+      split[cells[c].depth].push_back(k);
+    } else {
+      leaves.push_back(k);
+    }
+  }
+  std::vector<int> sids;
+  s->split_begin.assign(maxd + 1, 0);
+  s->split_n.assign(maxd + 1, 0);
+  for (int d = 0; d <= maxd; d++) {
+    s->split_begin[d] = (int)sids.size();
+    s->split_n[d] = (int)split[d].size();
+    sids.insert(sids.end(), split[d].begin(), split[d].end());
+  }
+  s->sort_cells.upload(s->sc_host.data(), s->sc_host.size(), st);
+  s->sort_leaf_ids.upload(leaves.data(), leaves.size(), st);
+  s->sort_split_ids.upload(sids.data(), sids.size(), st);
+  const auto& gos = sp.gpu_of_sorted();
+  s->g_of_s_dev.upload(gos.data(), gos.size(), st);
+  s->sort_d.alloc(std::max<long long>(off, 1));
+  s->sort_i.alloc(std::max<long long>(off, 1));
+  s->sort_nleaves = (int)leaves.size();
+  s->sort_max_depth = maxd;
+  CK(cudaStreamSynchronize(st));
+}
+
+int sphgpu_hydro_sort(sphgpu_space* s, int32_t flags, void* stream) {
+  if (!s) return fail(SPHGPU_EINVAL, "null argument");
+  if (flags <= 0 || flags > 0x1FFF) return fail(SPHGPU_EINVAL, "flags: a non-empty set of the 13 axes");
+  return guard([&]() {
+    ensure_device(s);
+    cudaStream_t st = pick(s, stream);
+    if (!s->sort_cells.p) build_sort_tree(s, st);
+    SortTree t;
+    t.cells = s->sort_cells.p;
+    t.leaves = s->sort_leaf_ids.p;
+    t.nleaves = s->sort_nleaves;
+    t.g_of_s = s->g_of_s_dev.p;
+    t.xd = s->xd.p;
+    t.d = s->sort_d.p;
+    t.i = s->sort_i.p;
+    std::vector<const int*> by_depth(s->sort_max_depth + 1);
+    for (int d = 0; d <= s->sort_max_depth; d++)
+      by_depth[d] = s->sort_split_ids.p + s->split_begin[d];
+    CK(launch_hydro_sort(t, by_depth.data(), s->split_n.data(), s->sort_max_depth, flags, st));
+    s->sorted_mask |= flags;
+    return SPHGPU_OK;
+  });
+}
+
+int sphgpu_space_tree(const sphgpu_space* s, int32_t* ncells, int32_t* records) {
+  if (!s || !ncells) return fail(SPHGPU_EINVAL, "null argument");
+  const auto& cells = s->space->cells();
+  *ncells = (int32_t)cells.size();
+  if (records)
+    for (size_t c = 0; c < cells.size(); c++) {
+      int32_t* r = records + 5 * c;
+      r[0] = cells[c].first;
+      r[1] = cells[c].count;
+      r[2] = cells[c].depth;
+      r[3] = cells[c].parent;
+      r[4] = cells[c].top;
+    }
+  return SPHGPU_OK;
+}
+
+int sphgpu_cell_sort(sphgpu_space* s, int32_t cell, int32_t axis, float* d, int32_t* idx) {
+  if (!s || !d || !idx) return fail(SPHGPU_EINVAL, "null argument");
+  if (axis < 0 || axis >= 13) return fail(SPHGPU_EINVAL, "axis out of range");
+  if (!(s->sorted_mask & (1 << axis))) return fail(SPHGPU_ESTATE, "axis not sorted");
+  if (cell < 0 || cell >= (int32_t)s->sc_of_cell.size() || s->sc_of_cell[cell] < 0)
+    return fail(SPHGPU_EINVAL, "not a non-empty cell");
+  return guard([&]() {
+    const SortCell& c = s->sc_host[s->sc_of_cell[cell]];
+    const long long o = c.off + (long long)axis * (c.count + 1);
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaDeviceSynchronize());
+    CK(cudaMemcpy(d, s->sort_d.p + o, sizeof(float) * (c.count + 1), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(idx, s->sort_i.p + o, sizeof(int32_t) * (c.count + 1), cudaMemcpyDeviceToHost));
     return SPHGPU_OK;
   });
 }

@@ -45,6 +45,34 @@ CASES = [
 
 INT_NAMES = ["leaf_first", "leaf_count", "leaf_depth", "depth_h", "position", "top"]
 
+# sort arrays of runner_do_hydro_sort, as per-(cell, axis) digests
+# (the clustered generator's FFT is not bit-reproducible across numpy builds
+# and CPUs, so only the lattice boxes are regenerated bit for bit on another
+# host; the clustered fixture pins the oracle where it was made)
+SORT_CASES = [
+    # name, generator kind, n, generator kwargs, run parameters
+    ("sorts_clustered32_deep", "clustered", 32, {"seed": 9, "rms": 1.5},
+     {"max_top_level_cells": 3}),
+    ("sorts_lattice20", "lattice", 20, {"seed": 5}, {}),
+    ("sorts_lattice48_deep", "lattice", 48, {"seed": 6}, {"max_top_level_cells": 3}),
+]
+
+
+def sort_digest(d, i):
+    """8-byte digest of one cell's 13 sort arrays (key bits and indices)."""
+    import hashlib
+    h = hashlib.blake2b(digest_size=8)
+    h.update(np.ascontiguousarray(d, np.float32).tobytes())
+    h.update(np.ascontiguousarray(i, np.int32).tobytes())
+    return np.frombuffer(h.digest(), np.uint64)[0]
+
+
+def sort_table(sorts):
+    """(records [cells][3] = first, count, depth; digests [cells])."""
+    rec = np.array([s[:3] for s in sorts], np.int32).reshape(-1, 3)
+    dig = np.array([sort_digest(s[3], s[4]) for s in sorts], np.uint64)
+    return rec, dig
+
 
 def mask_fields(fields, box, run):
     """Zero the first-pass density columns (0-7) of the particles that the
@@ -84,6 +112,16 @@ def main(only=None):
             field_sums=fields.astype(np.float64).sum(axis=0),
             int_sums=ints.astype(np.int64).sum(axis=0))
         print(name, N, "particles, cdim", ref["cdim"], "->", name + ".npz")
+    for name, kind, n, kw, run in SORT_CASES:
+        if only and name not in only:
+            continue
+        box = make_box(kind, n, kw)
+        ref = io.run_reference(box, tempfile.mkdtemp(), stages=1, sorts=True, **run)
+        rec, dig = sort_table(ref["sorts"])
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), kind=kind, n=n,
+                            gen_kwargs=repr(kw), run_kwargs=repr(run), records=rec,
+                            digests=dig)
+        print(name, len(rec), "cells ->", name + ".npz")
 
 
 if __name__ == "__main__":

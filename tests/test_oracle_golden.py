@@ -16,7 +16,8 @@ sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
 from make_golden import mask_fields  # noqa: E402
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-CASES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+CASES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+       if not os.path.basename(p).startswith("sorts_"))
 INT_NAMES = ["leaf_first", "leaf_count", "leaf_depth", "depth_h", "position", "top"]
 
 

@@ -181,7 +181,11 @@ int sphgpu_density_noalloc(sphgpu_space *s, float *d_fields, int32_t *d_ngb,
 
 /* Same pass through host buffers: copies x, v, m, h, u (input order) from
  * host memory, runs the step, copies the results back.  `fields` receives
- * float [n][24] in the column layout of sphgpu_download; NULL skips it. */
+ * float [n][24] in the column layout of sphgpu_download; NULL skips it.
+ * v, m and u may change from step to step; x and h must be the space's own
+ * (its cell tree and gather lists are built from them): they are checked on
+ * the device and SPHGPU_EINVAL is returned, with no step run, when they
+ * differ. */
 int sphgpu_step_host(sphgpu_space *s, const double *x, const float *v,
                      const float *m, const float *h, const float *u,
                      float *fields, void *stream);

@@ -90,7 +90,8 @@ struct sphgpu_space {
   int n_active = 0;
   std::vector<int> s_of_g;             // store index -> reference sorted index
   // host staging for step_host
-  DBuf<double> x_stage;
+  DBuf<double> x_stage, x_ref;  // x_ref: the space's input positions
+  DBuf<int> differ;
   DBuf<float> v_stage, m_stage, h_stage, u_stage, out_stage;
   // The batched step is three graphs (density first pass, ghost rounds,
   // force) so that CUDA events between them time each loop of every step.
@@ -743,9 +744,21 @@ int sphgpu_step_host(sphgpu_space* s, const double* x, const float* v,
     CK(cudaMemcpyAsync(s->m_stage.p, m, sizeof(float) * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(s->h_stage.p, h, sizeof(float) * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(s->u_stage.p, u, sizeof(float) * n, cudaMemcpyHostToDevice, st));
-    CK(launch_permute_in(s->P, s->perm.p, s->x_stage.p, s->v_stage.p, s->m_stage.p,
-                         s->h_stage.p, s->u_stage.p, st));
-    CK(launch_prepare_posh(s->P, s->top_of.p, s->top_loc.p, st));
+    if (!s->x_ref.p) {
+      s->x_ref.upload(s->x_in.data(), s->x_in.size(), st);
+      s->differ.alloc(1);
+    }
+    CK(cudaMemsetAsync(s->differ.p, 0, sizeof(int), st));
+    CK(launch_permute_in(s->P, s->perm.p, s->x_stage.p, s->x_ref.p, s->v_stage.p,
+                         s->m_stage.p, s->h_stage.p, s->u_stage.p, s->differ.p, st));
+    int differ = 0;
+    CK(cudaMemcpyAsync(&differ, s->differ.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (differ)
+      return fail(SPHGPU_EINVAL,
+                  "sphgpu_step_host: positions or smoothing lengths differ from the "
+                  "space's (its cell tree and gather lists are built from them); "
+                  "create a new space");
     const int rc = sphgpu_step(s, SPHGPU_STAGE_ALL, (void*)st);
     if (rc != SPHGPU_OK && rc != SPHGPU_ENOCONV) return rc;
     if (fields) {

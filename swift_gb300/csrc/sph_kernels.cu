@@ -229,17 +229,19 @@ __global__ void prepare_posh(DevParticles P, const int32_t* __restrict__ top_of,
 
 // Host-order inputs -> cell-sorted store (perm: sorted index -> input index).
 __global__ void permute_in(DevParticles P, const int32_t* __restrict__ perm,
-                           const double* __restrict__ x, const float* __restrict__ v,
-                           const float* __restrict__ m, const float* __restrict__ h,
-                           const float* __restrict__ u, double* xd) {
+                           const double* __restrict__ x, const double* __restrict__ x_ref,
+                           const float* __restrict__ v, const float* __restrict__ m,
+                           const float* __restrict__ h, const float* __restrict__ u,
+                           int* differ) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n;
        i += gridDim.x * blockDim.x) {
     const size_t k = (size_t)perm[i];
-    xd[3 * (size_t)i + 0] = x[3 * k + 0];
-    xd[3 * (size_t)i + 1] = x[3 * k + 1];
-    xd[3 * (size_t)i + 2] = x[3 * k + 2];
+    // the cell tree and the gather lists were built from the space's own
+    // positions and smoothing lengths: only v, m and u may change
+    if (x[3 * k] != x_ref[3 * k] || x[3 * k + 1] != x_ref[3 * k + 1] ||
+        x[3 * k + 2] != x_ref[3 * k + 2] || h[k] != P.h0[i])
+      atomicExch(differ, 1);
     P.velm[i] = make_float4(v[3 * k], v[3 * k + 1], v[3 * k + 2], m[k]);
-    P.h0[i] = h[k];
     P.u[i] = u[k];
   }
 }
@@ -320,11 +322,12 @@ cudaError_t launch_end_force(const DevParticles& p, cudaStream_t s) {
 }
 
 cudaError_t launch_permute_in(DevParticles p, const int32_t* perm,
-                              const double* x_in, const float* v_in,
-                              const float* m_in, const float* h_in,
-                              const float* u_in, cudaStream_t s) {
-  permute_in<<<grid_for(p.n), 256, 0, s>>>(p, perm, x_in, v_in, m_in, h_in, u_in,
-                                           const_cast<double*>(p.xd));
+                              const double* x_in, const double* x_ref,
+                              const float* v_in, const float* m_in,
+                              const float* h_in, const float* u_in, int* differ,
+                              cudaStream_t s) {
+  permute_in<<<grid_for(p.n), 256, 0, s>>>(p, perm, x_in, x_ref, v_in, m_in, h_in, u_in,
+                                           differ);
   return cudaGetLastError();
 }
 

@@ -98,10 +98,13 @@ cudaError_t launch_sum_active_ngb(const DevParticles& p, unsigned long long* out
 cudaError_t launch_end_force(const DevParticles& p, cudaStream_t s);
 cudaError_t launch_prepare_posh(DevParticles p, const int32_t* top_of,
                                 const double* top_loc, cudaStream_t s);
+// Host-order v, m, u -> store; sets *differ when x or h differ from the
+// space's own (x_ref: the space's input positions, input order).
 cudaError_t launch_permute_in(DevParticles p, const int32_t* perm,
-                              const double* x_in, const float* v_in,
-                              const float* m_in, const float* h_in,
-                              const float* u_in, cudaStream_t s);
+                              const double* x_in, const double* x_ref,
+                              const float* v_in, const float* m_in,
+                              const float* h_in, const float* u_in, int* differ,
+                              cudaStream_t s);
 cudaError_t launch_collect_out(DevParticles p, const int32_t* perm,
                                float* fields, int32_t* ints, cudaStream_t s);
 

@@ -134,6 +134,29 @@ def test_autotune_picks_a_candidate():
         assert np.all(np.isfinite(sp.download()["ax"]))
 
 
+def test_step_host_matches_resident_step_and_checks_inputs():
+    box = ics.make("clustered:20", seed=3)
+    with api.Space(box) as sp:
+        sp.step()
+        ref = sp.download()
+        fields = np.zeros((box["x"].shape[0], 24), np.float32)
+        sp.step_host(None, fields)
+        assert np.array_equal(fields[:, api.FIELD_COLS["ax"]], ref["ax"])
+        faster = dict(box)
+        faster["v"] = box["v"] * 2.0      # velocities may change
+        sp.step_host(faster, fields)
+        assert not np.array_equal(fields[:, api.FIELD_COLS["ax"]], ref["ax"])
+        moved = dict(box)
+        moved["x"] = box["x"].copy()
+        moved["x"][7, 0] += 1e-3          # positions may not
+        with pytest.raises(api.SphGpuError):
+            sp.step_host(moved, fields)
+        grown = dict(box)
+        grown["h"] = box["h"] * 1.01      # nor smoothing lengths
+        with pytest.raises(api.SphGpuError):
+            sp.step_host(grown, fields)
+
+
 # --- sparse activity on carried state --------------------------------------
 
 @pytest.mark.parametrize("cfg,mab", [("sedov:24", 22), ("sedov:32", 21),

@@ -103,10 +103,10 @@ __device__ __forceinline__ float3 offset_of(int idx, float3 tw) {
 //      (skipped when no lane reaches it), then staged in shared memory with
 //      the frame offset applied;
 //   3. every lane tests its own particle against each staged partner
-//      (broadcast reads): FP32 r^2 below a 2^-12 band around H^2 is a hit,
-//      pushed to the lane's ring; when any lane saw a candidate inside the
-//      band, the block is scanned again and those candidates are decided
-//      by the exact FP64 predicate in the reference frame;
+//      (broadcast reads), eight at a time into bit masks: FP32 r^2 below a
+//      2^-12 band around H^2 is a hit, pushed to the lane's ring from the
+//      mask; candidates inside the band are decided by the exact FP64
+//      predicate in the reference frame;
 //   4. when a ring is nearly full, all lanes compute interactions from
 //      their rings for about as many passes as the rings hold on average;
 //      the last drain empties them.  Sums stay in the lane's registers.
@@ -333,44 +333,50 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         __syncwarp();
         // the lane's own particle never pairs with itself
         const int tself = (i >= bfirst && i < bfirst + bcount) ? i - bfirst : -1;
+        const unsigned okmask =
+            mine ? (tself >= 0 ? ~(1u << tself) : 0xffffffffu) : 0u;
         const int pk = bfirst | (fidx << 27);
-        // Fast pass: FP32 r^2 below the band -> hit; candidates inside the
-        // band around H^2 are only noted, and decided exactly below.
-        bool band_seen = false;
-        for (int t = 0; t < bcount; t++) {
-          const float4 q = ws.jpos[t];
-          const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          float L2 = lo2, U2 = hi2;
-          if (FORCE) {
-            const float H2 = fmaxf(hig2, q.w);
-            L2 = H2 * (1.f - band);
-            U2 = H2 * (1.f + band);
-          }
-          const bool ok = mine && t != tself;
-          if (ok && r2 < L2) push(pk + t);
-          band_seen |= ok && r2 < U2 && !(r2 < L2);
-          if ((t & 7) == 7) room();
-        }
-        room();
-        if (__any_sync(FULL, band_seen)) {
-          // exact predicate in the reference frame for the band candidates
-          for (int t = 0; t < bcount; t++) {
-            const float4 q = ws.jpos[t];
+        // Eight candidates at a time: FP32 r^2 below the band around H^2 sets
+        // a hit bit, inside the band a band bit; hits are pushed from the
+        // mask, band candidates are decided by the exact FP64 predicate in
+        // the reference frame (rare: the warp votes once per eight).
+        for (int t0 = 0; t0 < bcount; t0 += 8) {
+          unsigned hm = 0u, bm = 0u;
+#pragma unroll
+          for (int u = 0; u < 8; u++) {
+            const float4 q = ws.jpos[t0 + u];
             const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            float L2 = lo2, U2 = hi2, H2 = hig2;
+            float L2 = lo2, U2 = hi2;
             if (FORCE) {
-              H2 = fmaxf(hig2, q.w);
+              const float H2 = fmaxf(hig2, q.w);
               L2 = H2 * (1.f - band);
               U2 = H2 * (1.f + band);
             }
-            if (band_seen && mine && t != tself && r2 < U2 && !(r2 < L2) &&
-                exact_r2_2(P.xd, i, bfirst + t, E) < H2)
-              push(pk + t);
-            if ((t & 7) == 7) room();
+            if (r2 < L2)
+              hm |= 1u << u;
+            else if (r2 < U2)
+              bm |= 1u << u;
           }
-          room();
+          const int left = bcount - t0;
+          const unsigned live = (left >= 8 ? 0xffu : ((1u << left) - 1u)) & (okmask >> t0);
+          hm &= live;
+          bm &= live;
+          while (hm) {
+            const int u = __ffs(hm) - 1;
+            hm &= hm - 1u;
+            push(pk + t0 + u);
+          }
+          if (__any_sync(FULL, bm != 0u)) {
+            while (bm) {
+              const int u = __ffs(bm) - 1;
+              bm &= bm - 1u;
+              const int t = t0 + u;
+              const float H2 = FORCE ? fmaxf(hig2, ws.jpos[t].w) : hig2;
+              if (exact_r2_2(P.xd, i, bfirst + t, E) < H2) push(pk + t);
+            }
+          }
+          room();  // at most 8 pushes per lane since the last check
         }
       }
       __syncwarp();

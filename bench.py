@@ -320,9 +320,9 @@ def run_serving(args):
        through a fresh server -> boxes/s;
     2. the 2,000-request stream with Poisson arrivals at 80% of that
        capacity -> p50 / p99 latency (arrival to completion) and boxes/s;
-    3. the plain per-task form and the single-box batched form on a seeded
-       sample of the same stream, one box after another (host planning
-       included, as in the server) -> boxes/s."""
+    3. the plain per-task form and the single-box batched form on boxes of
+       the same stream taken at evenly spaced quantiles of N, one box after
+       another (host planning included, as in the server) -> boxes/s."""
     import numpy as np
     import torch
     from swift_gb300 import api, serve
@@ -350,8 +350,11 @@ def run_serving(args):
     thr = count / wall
     summ = serve.latency_summary(lat)
     # 3. one box at a time: plain per-task form and single-box batched form
-    rng = np.random.default_rng(args.seed + 1)
-    sample = sorted(rng.choice(count, size=min(args.plain_boxes, count), replace=False))
+    # boxes at evenly spaced quantiles of N, so that the sample's mean size
+    # is the stream's
+    k = min(args.plain_boxes, count)
+    by_n = np.argsort(nparts, kind="stable")
+    sample = sorted(int(by_n[int((q + 0.5) * count / k)]) for q in range(k))
 
     def one_by_one(plain):
         t0 = time.perf_counter()

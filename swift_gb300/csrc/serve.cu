@@ -117,10 +117,18 @@ struct Job {
   int nleaves = 0, nwin = 0, nblk = 0, ntop = 0;
   float4 tw{0.f, 0.f, 0.f, 0.f};
   std::string err;
+  // force lists, planned by a worker from the post-ghost h of a warm-up pass
+  const float4* ph = nullptr;       // pinned copy of the box's posh
+  std::atomic<int> pf_state{0};     // 0 pending, 1 planned, -1 failed
+  std::string pf_err;
 };
 
 struct Resident {
   std::unique_ptr<Job> job;
+  // 0: warming up (its first density + ghost pass gives the h the force
+  // recursion needs), 1: force lists being planned, 2: stepping
+  int phase = 0;
+  int64_t pin0 = -1;  // its slice of the pinned h buffer while planning
   int64_t p0 = -1, l0 = -1, w0 = -1, b0 = -1, t0 = -1;
   int64_t e0[3] = {-1, -1, -1}, ne[3] = {0, 0, 0};  // entries of the d, s, f lists
   int64_t q0[3] = {-1, -1, -1}, nq[3] = {0, 0, 0};  // candidate pairs
@@ -250,6 +258,9 @@ struct sphgpu_server {
   int64_t hwP = 0, hwL = 0, hwW = 0, hwB = 0;
   int64_t pumps = 0, retired = 0;
   int host_threads = 1;
+  float4* pin = nullptr;  // pinned host buffer for warm-up h read-backs
+  Ranges rPin;
+  std::deque<Job*> ftodo;  // force lists to plan
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double gpu_ms = 0, force_plan_s = 0, admit_s = 0, retire_s = 0;
 
@@ -263,18 +274,35 @@ struct sphgpu_server {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (st) cudaStreamDestroy(st);
+    if (pin) cudaFreeHost(pin);
   }
 
   void worker() {
     for (;;) {
       std::unique_ptr<Job> j;
+      Job* fj = nullptr;
       {
         std::unique_lock<std::mutex> lock(mu);
-        cv.wait(lock, [&] { return stop || !todo.empty(); });
+        cv.wait(lock, [&] { return stop || !todo.empty() || !ftodo.empty(); });
         if (stop) return;
-        j = std::move(todo.front());
-        todo.pop_front();
-        planning++;
+        if (!ftodo.empty()) {  // force lists first: a box waits on them
+          fj = ftodo.front();
+          ftodo.pop_front();
+        } else {
+          j = std::move(todo.front());
+          todo.pop_front();
+          planning++;
+        }
+      }
+      if (fj) {
+        try {
+          plan_force_lists(*fj);
+          fj->pf_state = 1;
+        } catch (const std::exception& e) {
+          fj->pf_err = e.what();
+          fj->pf_state = -1;
+        }
+        continue;
       }
       try {
         plan_job(*j);
@@ -289,6 +317,15 @@ struct sphgpu_server {
       }
       cv.notify_all();
     }
+  }
+
+  // The box's post-ghost h (pinned copy, store order) -> its planner, whose
+  // force recursion reads the new h_max.
+  static void plan_force_lists(Job& j) {
+    std::vector<float> hs(j.n);
+    for (int g = 0; g < j.n; g++) hs[j.s_of_g[g]] = j.ph[g].w;
+    j.sp->update_h_after_ghost(hs.data());
+    j.sp->plan_density(j.pf, true);
   }
 
   void recompute_high_water() {
@@ -614,6 +651,21 @@ struct sphgpu_server {
 
   // One step of every resident box.
   void step_all() {
+    // boxes whose force lists a worker finished: upload them; they step
+    // in full from this pump on
+    for (auto& kv : res) {
+      Resident& r = kv.second;
+      if (r.phase != 1) continue;
+      const int state = r.job->pf_state;
+      if (state == 0) continue;
+      if (state < 0) throw std::runtime_error("force lists: " + r.job->pf_err);
+      rPin.release(r.pin0, r.job->n);
+      r.pin0 = -1;
+      if (!place_plan(r, r.job->pf, 2))
+        throw std::runtime_error("serving arena: no room for a box's force lists");
+      r.force_planned = true;
+      r.phase = 2;
+    }
     CK(cudaEventRecord(ev[0], st));
     CK(launch_begin_step(view(0, (int)hwP), phys.max_iter, redo.p, st));
     gather(0, 0, MODE_FIRST, false, 1, nullptr);
@@ -624,15 +676,42 @@ struct sphgpu_server {
     int last = 0;
     CK(cudaMemcpyAsync(&last, redo.p + phys.max_iter - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ev[1], st));
-    std::vector<Resident*> fresh;
-    for (auto& kv : res)
-      if (!kv.second.force_planned) fresh.push_back(&kv.second);
-    if (!fresh.empty()) plan_forces(fresh);
+    // warming boxes: their h goes to pinned memory (in stream order, before
+    // the next pump resets it) and their force lists to the workers; when
+    // the pinned buffer is full, they are planned here instead
+    std::vector<Resident*> inline_plan, to_workers;
+    for (auto& kv : res) {
+      Resident& r = kv.second;
+      if (r.phase != 0) continue;
+      const int64_t off = rPin.alloc(r.job->n);
+      if (off < 0) {
+        inline_plan.push_back(&r);
+        continue;
+      }
+      r.pin0 = off;
+      r.job->ph = pin + off;
+      r.job->pf_state = 0;
+      CK(cudaMemcpyAsync(pin + off, posh.p + r.p0, sizeof(float4) * r.job->n,
+                         cudaMemcpyDeviceToHost, st));
+      r.phase = 1;
+      to_workers.push_back(&r);
+    }
+    if (!inline_plan.empty()) {
+      plan_forces(inline_plan);
+      for (Resident* r : inline_plan) r->phase = 2;
+    }
     CK(cudaEventRecord(ev[2], st));
     CK(launch_block_hmax(bb_fc.p, bb_lo.p, posh.p, (int)hwB, st));
     gather(2, 2, MODE_FIRST, true, 1, nullptr);  // writes the finished sums
     CK(cudaEventRecord(ev[3], st));
     CK(cudaStreamSynchronize(st));
+    if (!to_workers.empty()) {
+      {
+        std::lock_guard<std::mutex> lock(mu);
+        for (Resident* r : to_workers) ftodo.push_back(r->job.get());
+      }
+      cv.notify_all();
+    }
     float a = 0.f, b = 0.f;
     CK(cudaEventElapsedTime(&a, ev[0], ev[1]));
     CK(cudaEventElapsedTime(&b, ev[2], ev[3]));
@@ -642,6 +721,7 @@ struct sphgpu_server {
                                std::to_string(last) + " particles");
     std::vector<int64_t> fin;
     for (auto& kv : res) {
+      if (kv.second.phase != 2) continue;  // a warm-up pass is not a step
       kv.second.steps++;
       if (kv.second.steps >= kv.second.job->nsteps) fin.push_back(kv.first);
     }
@@ -786,6 +866,10 @@ int sphgpu_server_create(const sphgpu_params* prm, int64_t max_particles,
     int nt = planner_threads;
     if (nt == 0) nt = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
     s->host_threads = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
+    // pinned room for the warm-up h of up to 2^22 particles at a time
+    const int64_t npin = std::min<int64_t>(cap, (int64_t)1 << 22);
+    CK(cudaHostAlloc((void**)&s->pin, sizeof(float4) * npin, cudaHostAllocDefault));
+    s->rPin.init(npin);
     for (auto& e : s->ev) CK(cudaEventCreate(&e));
     for (int t = 0; t < nt; t++) s->workers.emplace_back([p = s.get()] { p->worker(); });
     *out = s.release();

@@ -360,7 +360,7 @@ void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st) {
 }
 
 void enqueue_density(sphgpu_space* s, cudaStream_t st, bool density) {
-  CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, st));
+  CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, s->prm.h_max, st));
   if (density) enqueue_gather(s, st, s->dplan_d, 0, MODE_FIRST, false, 1, nullptr);
 }
 
@@ -1157,7 +1157,7 @@ int sphgpu_begin_loops(sphgpu_space* s, void* stream) {
   return guard([&]() {
     ensure_device(s);
     ensure_task_plans(s, false);
-    CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, pick(s, stream)));
+    CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, s->prm.h_max, pick(s, stream)));
     return SPHGPU_OK;
   });
 }

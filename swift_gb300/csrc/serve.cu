@@ -667,7 +667,7 @@ struct sphgpu_server {
       r.phase = 2;
     }
     CK(cudaEventRecord(ev[0], st));
-    CK(launch_begin_step(view(0, (int)hwP), phys.max_iter, redo.p, st));
+    CK(launch_begin_step(view(0, (int)hwP), phys.max_iter, redo.p, phys.h_max, st));
     gather(0, 0, MODE_FIRST, false, 1, nullptr);
     for (int k = 0; k < phys.max_iter; k++) {
       CK(launch_ghost(ghargs(k), st));

@@ -153,7 +153,7 @@ __global__ void ghost_round(GhostArgs g) {
 // Start of a step: active particles restart from the input h with cleared
 // sums; inactive ones keep the state of their last step, which the loops of
 // their active neighbours read.
-__global__ void begin_step(DevParticles P, int max_iter, int* redo_count) {
+__global__ void begin_step(DevParticles P, int max_iter, int* redo_count, float h_max) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid < max_iter) redo_count[tid] = 0;
   for (int i = tid; i < P.n; i += gridDim.x * blockDim.x) {
@@ -166,8 +166,9 @@ __global__ void begin_step(DevParticles P, int max_iter, int* redo_count) {
     P.posh[i] = ph;
     P.flags[i] = 3;
     P.depth_h[i] = P.depth_h0[i];
+    // the ghost's bisection bracket starts at [0, h_max] (runner_ghost.c:1181-1182)
     P.left[i] = 0.f;
-    P.right[i] = 3.40282347e+38f;
+    P.right[i] = h_max;
     P.ghost_iters[i] = 0;
     P.dens0[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     P.dens1[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -291,8 +292,9 @@ cudaError_t launch_ghost(const GhostArgs& g, cudaStream_t s) {
 }
 
 cudaError_t launch_begin_step(const DevParticles& p, int max_iter,
-                              int* redo_count, cudaStream_t s) {
-  begin_step<<<grid_for(std::max(p.n, max_iter)), 256, 0, s>>>(p, max_iter, redo_count);
+                              int* redo_count, float h_max, cudaStream_t s) {
+  begin_step<<<grid_for(std::max(p.n, max_iter)), 256, 0, s>>>(p, max_iter, redo_count,
+                                                                h_max);
   return cudaGetLastError();
 }
 

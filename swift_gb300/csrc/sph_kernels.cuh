@@ -88,7 +88,7 @@ cudaError_t launch_block_hmax(const int2* fc, float4* lo, const float4* posh,
                               int nblocks, cudaStream_t s);
 cudaError_t launch_ghost(const GhostArgs& g, cudaStream_t s);
 cudaError_t launch_begin_step(const DevParticles& p, int max_iter,
-                              int* redo_count, cudaStream_t s);
+                              int* redo_count, float h_max, cudaStream_t s);
 cudaError_t launch_set_flags(uint8_t* flags, const int* idx, int n, uint8_t v,
                              cudaStream_t s);
 cudaError_t launch_gather_h(const float4* posh, const int* idx, int n, float* out,

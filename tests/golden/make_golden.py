@@ -36,6 +36,8 @@ CASES = [
     # conditions does not have
     ("sedov24_sparse", "sedov", 24, {"seed": 2}, {"max_active_bin": 21, "stages": 3},
      1024),
+    # an open (non-periodic) box, as the reference's cell tests use
+    ("lattice16_open", "lattice", 16, {"seed": 24}, {"periodic": 0}, 1024),
     # two steps: every particle active, then the 2% in bins 20-22 on the
     # state the first step leaves (inactive neighbours carry their density
     # and force state into the second step's loops)

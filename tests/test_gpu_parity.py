@@ -157,6 +157,60 @@ def test_step_host_matches_resident_step_and_checks_inputs():
             sp.step_host(grown, fields)
 
 
+# --- open boxes and tiny inputs --------------------------------------------
+
+@pytest.mark.parametrize("cfg,run", [("lattice:16", {"periodic": 0}),
+                                     ("clustered:20", {"periodic": 0,
+                                                       "max_top_level_cells": 3})])
+def test_open_box_parity(cfg, run, oracle_lib):
+    box = ics.make(cfg, seed=31)
+    ref = oracle_lib.run(box, **run)
+    with api.Space(box, **run) as sp:
+        sp.step(api.STAGE_DENSITY)
+        first = sp.download()
+        sp.step()
+        full = sp.download()
+        sp.force_from_state(ref["h"], ref["rho"], ref["f"], ref["pressure"],
+                            ref["soundspeed"], ref["balsara"])
+        force = sp.download()
+    assert np.array_equal(first["ngb_first"], ref["ngb_first"]), cfg
+    assert np.array_equal(force["ngb_force"], ref["ngb_force"]), cfg
+    assert rel_err(full["h"], ref["h"]).max() < 2e-4
+    for k in ("rho", "pressure", "soundspeed"):
+        assert rel_err(full[k], ref[k]).max() < 3e-4, k
+    for k in ("ax", "ay", "az", "u_dt", "h_dt"):
+        assert scaled_err(force[k], ref[k]).max() < REL, k
+
+
+def _tiny(n, seed):
+    box = ics.lattice(4, seed=seed)
+    for k in ("x", "v", "m", "h", "u", "time_bin"):
+        box[k] = box[k][:n].copy()
+    return box
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 17])
+def test_tiny_open_boxes(n, oracle_lib):
+    box = _tiny(n, seed=n)
+    run = {"periodic": 0, "h_max": 0.6}
+    ref = oracle_lib.run(box, **run)
+    with api.Space(box, **run) as sp:
+        sp.step()
+        out = sp.download()
+    assert np.array_equal(out["ngb_first"], ref["ngb_first"])
+    assert rel_err(out["h"], ref["h"]).max() < 2e-4
+    assert rel_err(out["rho"], ref["rho"]).max() < 3e-4
+    if n == 1:
+        assert out["h"][0] == np.float32(0.6)
+
+
+def test_lonely_particle_without_h_max_reports_nonconvergence():
+    with api.Space(_tiny(1, seed=1), periodic=0) as sp:
+        with pytest.raises(api.SphGpuError) as e:
+            sp.step()
+    assert e.value.code == api.ENOCONV
+
+
 # --- sparse activity on carried state --------------------------------------
 
 @pytest.mark.parametrize("cfg,mab", [("sedov:24", 22), ("sedov:32", 21),

@@ -20,7 +20,42 @@ CASES = [
     ("lattice", 16, {"seed": 21}, {}),
     ("clustered", 20, {"seed": 22, "rms": 0.8}, {"max_top_level_cells": 3}),
     ("sedov", 20, {"seed": 23}, {"max_active_bin": 22}),
+    # open (non-periodic) boxes, as the reference's test27cells / test125cells
+    ("lattice", 16, {"seed": 24}, {"periodic": 0}),
+    ("clustered", 20, {"seed": 25}, {"periodic": 0, "max_top_level_cells": 3}),
 ]
+
+
+def tiny(n, seed):
+    """The first n particles of a 4^3 lattice: one top cell, few or no
+    neighbours (h reaches h_max)."""
+    box = ics.lattice(4, seed=seed)
+    for k in ("x", "v", "m", "h", "u", "time_bin"):
+        box[k] = box[k][:n].copy()
+    return box
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 17])
+def test_tiny_open_boxes_bitwise(n, oracle_lib):
+    box = tiny(n, seed=n)
+    run = {"periodic": 0, "h_max": 0.6}
+    ref = io.run_reference(box, tempfile.mkdtemp(), **run)
+    orc = oracle_lib.run(box, **run)
+    assert orc["status"] == 0
+    for k in io.COLS:
+        assert np.array_equal(ref[k].view(np.uint32), orc[k].view(np.uint32)), k
+    if n == 1:
+        assert orc["h"][0] == np.float32(0.6)  # no neighbour: h climbs to h_max
+
+
+def test_lonely_particle_without_h_max_fails_like_the_reference(oracle_lib):
+    """No neighbours and no h_max: the reference aborts after max_iter
+    rounds (runner_ghost.c:1592); the oracle reports non-convergence."""
+    import subprocess
+    box = tiny(1, seed=1)
+    with pytest.raises(subprocess.CalledProcessError):
+        io.run_reference(box, tempfile.mkdtemp(), periodic=0)
+    assert oracle_lib.run(box, periodic=0)["status"] == 1
 
 
 @pytest.mark.parametrize("kind,n,gen,run", CASES)

@@ -88,6 +88,9 @@ int sphgpu_abi_version(void);
 const char *sphgpu_last_error(void);
 void sphgpu_default_params(sphgpu_params *p);
 
+/* Largest space: the gathers pack a partner's store index in 27 bits. */
+#define SPHGPU_MAX_PARTICLES ((1 << 27) - 1)
+
 /* Build the cell tree of a box (host) and keep its particles for the GPU.
  * Replaces space_init + space_rebuild.  No device is touched until the
  * first GPU call, so tree queries work without a GPU. */

@@ -54,7 +54,7 @@ def write_input(path, box, stages=ALL_STAGES, **overrides):
     hdr = np.zeros(1, HEADER_DTYPE)
     hdr["magic"] = b"SPHIN001"
     hdr["n"] = n
-    hdr["dim"] = [box["dim"]] * 3
+    hdr["dim"] = list(box["dim"]) if np.ndim(box["dim"]) else [box["dim"]] * 3
     for k in ("eta", "h_tolerance", "h_max", "h_min", "alpha", "max_iter",
               "max_active_bin", "periodic", "max_top_level_cells"):
         hdr[k] = p[k]

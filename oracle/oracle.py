@@ -70,7 +70,7 @@ def lib():
 def make_params(box, **kw):
     p = Params()
     d = box["dim"]
-    p.dim[:] = [d, d, d]
+    p.dim[:] = list(d) if np.ndim(d) else [d, d, d]
     p.periodic = kw.get("periodic", 1)
     p.eta = kw.get("eta", box.get("eta", 1.2348))
     p.h_tolerance = kw.get("h_tolerance", 1e-4)

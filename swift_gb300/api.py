@@ -140,7 +140,7 @@ def make_params(box, **kw):
     p = Params()
     L.sphgpu_default_params(ctypes.byref(p))
     d = box["dim"]
-    p.dim[:] = [d, d, d]
+    p.dim[:] = list(d) if np.ndim(d) else [d, d, d]
     p.eta = kw.get("eta", box.get("eta", p.eta))
     for k in ("periodic", "h_tolerance", "h_max", "h_min", "alpha", "max_iter",
               "max_top_level_cells"):

@@ -488,6 +488,9 @@ int sphgpu_space_create(const sphgpu_params* prm, int64_t n, const double* x,
                         sphgpu_space** out) {
   if (!prm || !x || !v || !m || !h || !u || !time_bin || !out || n <= 0)
     return fail(SPHGPU_EINVAL, "sphgpu_space_create: null argument or n <= 0");
+  if (n > SPHGPU_MAX_PARTICLES)
+    return fail(SPHGPU_EINVAL, "sphgpu_space_create: more than SPHGPU_MAX_PARTICLES "
+                               "particles (partner indices are packed in 27 bits)");
   if (prm->max_iter < 1 || prm->max_iter > 1000 || prm->max_top_level_cells < 3 ||
       !(prm->eta > 0.f) || !(prm->dim[0] > 0) || !(prm->dim[1] > 0) || !(prm->dim[2] > 0))
     return fail(SPHGPU_EINVAL, "sphgpu_space_create: invalid parameters");

@@ -58,6 +58,21 @@ def test_invalid_arguments_are_rejected():
     assert L.sphgpu_step(None, 7, None) == api.EINVAL
 
 
+def test_particle_count_ceiling():
+    """Partner indices are packed in 27 bits: larger spaces are refused
+    before any array is read."""
+    import ctypes
+    L = api.lib()
+    p = api.Params()
+    L.sphgpu_default_params(ctypes.byref(p))
+    dummy = np.zeros(8)
+    h = ctypes.c_void_p()
+    rc = L.sphgpu_space_create(ctypes.byref(p), 1 << 27, *([dummy.ctypes.data] * 6),
+                               ctypes.byref(h))
+    assert rc == api.EINVAL
+    assert b"27 bits" in L.sphgpu_last_error()
+
+
 def test_tiny_box_needs_three_cells_per_axis():
     box = ics.lattice(4, seed=1)   # h ~ box/3: fewer than 3 top cells
     with pytest.raises(api.SphGpuError):

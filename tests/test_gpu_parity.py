@@ -182,6 +182,30 @@ def test_open_box_parity(cfg, run, oracle_lib):
         assert scaled_err(force[k], ref[k]).max() < REL, k
 
 
+@pytest.mark.parametrize("kind", ["rectangular", "faces", "h_min"])
+def test_special_boxes(kind, oracle_lib):
+    import sys
+    sys.path.insert(0, __import__("os").path.dirname(__file__))
+    from test_oracle_reference import special_box
+    box, run = special_box(kind)
+    ref = oracle_lib.run(box, **run)
+    with api.Space(box, **run) as sp:
+        sp.step(api.STAGE_DENSITY)
+        first = sp.download()
+        sp.step()
+        full = sp.download()
+        sp.force_from_state(ref["h"], ref["rho"], ref["f"], ref["pressure"],
+                            ref["soundspeed"], ref["balsara"])
+        force = sp.download()
+    assert np.array_equal(first["ngb_first"], ref["ngb_first"]), kind
+    assert np.array_equal(force["ngb_force"], ref["ngb_force"]), kind
+    assert rel_err(full["h"], ref["h"]).max() < 2e-4
+    for k in ("rho", "pressure", "soundspeed"):
+        assert rel_err(full[k], ref[k]).max() < 3e-4, k
+    for k in ("ax", "ay", "az", "u_dt"):
+        assert scaled_err(force[k], ref[k]).max() < REL, k
+
+
 def _tiny(n, seed):
     box = ics.lattice(4, seed=seed)
     for k in ("x", "v", "m", "h", "u", "time_bin"):

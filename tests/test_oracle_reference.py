@@ -26,6 +26,40 @@ CASES = [
 ]
 
 
+def special_box(kind):
+    """Boxes that exercise the grid: a rectangular periodic box, particles
+    exactly on the box faces (x == 0 and x == dim, which wraps), h clamped at
+    h_min."""
+    if kind == "rectangular":
+        box = ics.lattice(16, seed=41)
+        box["x"][:, 2] *= 0.5
+        box["dim"] = (1.0, 1.0, 0.5)
+        return box, {}
+    if kind == "faces":
+        box = ics.lattice(16, seed=42)
+        box["x"][::97, 0] = 0.0
+        box["x"][5::101, 1] = 1.0
+        return box, {}
+    if kind == "h_min":
+        box = ics.clustered(20, seed=43, rms=0.8)
+        return box, {"h_min": 0.07}
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("kind", ["rectangular", "faces", "h_min"])
+def test_special_boxes_bitwise(kind, oracle_lib):
+    box, run = special_box(kind)
+    ref = io.run_reference(box, tempfile.mkdtemp(), **run)
+    orc = oracle_lib.run(box, **run)
+    assert orc["status"] == 0
+    for k in ("leaf_first", "leaf_count", "leaf_depth", "depth_h", "position", "top"):
+        assert np.array_equal(ref[k], orc[k]), k
+    for k in io.COLS:
+        assert np.array_equal(ref[k].view(np.uint32), orc[k].view(np.uint32)), k
+    if kind == "h_min":
+        assert np.any(orc["h"] == np.float32(0.07))
+
+
 def tiny(n, seed):
     """The first n particles of a 4^3 lattice: one top cell, few or no
     neighbours (h reaches h_max)."""

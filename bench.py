@@ -7,7 +7,7 @@ with P(k) ~ k^-2, rms displacement 0.3 of the spacing), Minimal SPH with the
 Wendland C2 kernel, all particles active.  A step is one full pass -- density
 loop, the ghost's Newton iterations on h with density re-runs, force loop --
 starting from h0 = eta * spacing, run by the batched form (one persistent
-gather launch per loop, three CUDA graphs per step).
+gather launch per loop, one CUDA graph per step).
 
   value   interactions/s with the particle state resident in HBM;
   e2e     the same through the C ABI with host buffers: every step copies the
@@ -488,7 +488,7 @@ def run_ours(args):
             "data": "synthetic (seeded generators, no dataset)",
             "config": {
                 "workload": WORKLOADS[args.workload][3],
-                "particles_per_gpu": n, "form": "batched persistent, 3 CUDA graphs/step",
+                "particles_per_gpu": n, "form": "batched persistent, one CUDA graph per step",
                 "active": "all", "h0": "eta*spacing (ghost iterates every step)",
                 "l2": "inputs larger than L2 (particle state ~150 B/particle)",
                 "parallelism": "replicas" if world > 1 else "single",

@@ -93,9 +93,9 @@ struct sphgpu_space {
   DBuf<double> x_stage, x_ref;  // x_ref: the space's input positions
   DBuf<int> differ;
   DBuf<float> v_stage, m_stage, h_stage, u_stage, out_stage;
-  // The batched step is three graphs (density first pass, ghost rounds,
-  // force) so that CUDA events between them time each loop of every step.
-  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+  // The batched step is one CUDA graph (density first pass, ghost rounds,
+  // force); event-record nodes inside it time each loop of every step.
+  cudaGraphExec_t graph[1] = {nullptr};
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double plan_ms = 0;  // host planning inside steps (force re-plans)
   double phase_ms[3] = {0, 0, 0};
@@ -681,16 +681,18 @@ int sphgpu_step(sphgpu_space* s, int32_t stages, void* stream) {
       return SPHGPU_OK;
     }
     s->h_stale = true;
-    if (!s->graph[0]) {
-      s->graph[0] = capture(st, [&]() { enqueue_density(s, st, true); });
-      s->graph[1] = capture(st, [&]() { enqueue_ghost_rounds(s, st); });
-      s->graph[2] = capture(st, [&]() { enqueue_force(s, st); });
-    }
+    if (!s->graph[0])
+      s->graph[0] = capture(st, [&]() {
+        // external event-record nodes: the events can be timed from the host
+        enqueue_density(s, st, true);
+        CK(cudaEventRecordWithFlags(s->ev[1], st, cudaEventRecordExternal));
+        enqueue_ghost_rounds(s, st);
+        CK(cudaEventRecordWithFlags(s->ev[2], st, cudaEventRecordExternal));
+        enqueue_force(s, st);
+      });
     CK(cudaEventRecord(s->ev[0], st));
-    for (int k = 0; k < 3; k++) {
-      CK(cudaGraphLaunch(s->graph[k], st));
-      CK(cudaEventRecord(s->ev[k + 1], st));
-    }
+    CK(cudaGraphLaunch(s->graph[0], st));
+    CK(cudaEventRecord(s->ev[3], st));
     const int rc = check_conv(s, st);  // synchronises the stream
     for (int k = 0; k < 3; k++) {
       float ms = 0.f;

@@ -58,6 +58,7 @@ inline int guard(const std::function<int()>& f) {
   try {
     return f();
   } catch (const CudaError& e) {
+    cudaGetLastError();  // a reported non-sticky error must not reach the next check
     return fail(SPHGPU_ECUDA, e.what());
   } catch (const std::bad_alloc&) {
     return fail(SPHGPU_ENOMEM, "host allocation failed");

@@ -416,7 +416,7 @@ def run_ours(args):
         sp.set_tuning(jtile=jt, block_warps=bw)
         sp.step(stream=sh)
     if args.no_tune or args.tuning:
-        tuning, tune_ms = (dict(zip(("threads_per_particle", "jtile", "persistent",
+        tuning, tune_ms = (dict(zip(("threads_per_particle", "jtile", "rerun_lists",
                                      "block_warps"), sp.tuning())), {})
     else:
         tuning, tune_ms = sp.autotune(reps=2)

@@ -79,7 +79,11 @@ typedef struct {
                                    serves a group of up to 32 particles) */
   int32_t jtile;                /* partner particles per culled j-block:
                                    8, 16 or 32 */
-  int32_t persistent;           /* 1: resident grid + device work queue */
+  int32_t rerun_lists;          /* 1: the ghost's first density re-run
+                                   records each particle's neighbour list
+                                   and the later re-runs compute from it
+                                   (when the lists fit in a quarter of the
+                                   free HBM); 0: every re-run gathers */
   int32_t block_warps;          /* tile shape: 8 warps x 3 blocks per SM,
                                    or 4 warps x 6 blocks per SM */
 } sphgpu_tuning;

@@ -50,7 +50,7 @@ class Params(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("threads_per_particle", ctypes.c_int32),
-                ("jtile", ctypes.c_int32), ("persistent", ctypes.c_int32),
+                ("jtile", ctypes.c_int32), ("rerun_lists", ctypes.c_int32),
                 ("block_warps", ctypes.c_int32)]
 
 
@@ -214,14 +214,14 @@ class Space:
         return geom, ints
 
     # -- configuration -----------------------------------------------------
-    def set_tuning(self, tpi=1, jtile=32, persistent=1, block_warps=8):
-        t = Tuning(tpi, jtile, persistent, block_warps)
+    def set_tuning(self, tpi=1, jtile=32, rerun_lists=1, block_warps=8):
+        t = Tuning(tpi, jtile, rerun_lists, block_warps)
         _check(lib().sphgpu_set_tuning(self._h, ctypes.byref(t)))
 
     def tuning(self):
         t = Tuning()
         _check(lib().sphgpu_get_tuning(self._h, ctypes.byref(t)))
-        return (t.threads_per_particle, t.jtile, t.persistent, t.block_warps)
+        return (t.threads_per_particle, t.jtile, t.rerun_lists, t.block_warps)
 
     def tree(self):
         """Cell records: first, count, depth, parent, top (one row per cell)."""
@@ -252,7 +252,8 @@ class Space:
         table = {f"jtile={jt},block_warps={bw}": float(ms[k])
                  for k, (jt, bw) in enumerate(cands[:n.value])}
         return ({"threads_per_particle": best.threads_per_particle,
-                 "jtile": best.jtile, "block_warps": best.block_warps}, table)
+                 "jtile": best.jtile, "rerun_lists": best.rerun_lists,
+                 "block_warps": best.block_warps}, table)
 
     def set_active(self, max_active_bin):
         _check(lib().sphgpu_set_active(self._h, int(max_active_bin)))

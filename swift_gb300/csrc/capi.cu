@@ -79,6 +79,10 @@ struct sphgpu_space {
   DBuf<int2> bb_fc;
   int bb_n = 0;
   DBuf<int4> units;              // gather work groups (device-built)
+  // neighbour lists of the ghost's re-runs (when they fit in HBM)
+  bool lists = false;
+  DBuf<int> nl, nl_cnt, blk_of;
+  DBuf<float> nl_T;
   int max_units = 0;             // 32-particle windows of all leaves
   DBuf<int> leaf_window_begin;   // per leaf: its first window
   std::vector<int> lwb_host;
@@ -130,6 +134,12 @@ void build_plans(sphgpu_space* s) {
 
 void upload_activity(sphgpu_space* s, cudaStream_t st);
 
+// Re-run neighbour lists: at most kListCap items per particle, recorded for
+// r^2 < kListScale (gamma h)^2 (a radius 2 % above the first re-run's, which
+// the later re-runs' h stay within for almost every particle).
+constexpr int kListCap = 128;
+constexpr float kListScale = 1.0404f;
+
 // j-block boxes and particle ranges of the current j-block depth.
 void upload_blocks(sphgpu_space* s, cudaStream_t st) {
   const JBlocks& jb = s->space->jblocks();
@@ -145,6 +155,11 @@ void upload_blocks(sphgpu_space* s, cudaStream_t st) {
   s->bb_hi.upload(bhi.data(), nb, st);
   s->bb_fc.upload(bfc.data(), nb, st);
   s->bb_n = (int)nb;
+  std::vector<int> bo(s->space->n());
+  for (size_t b = 0; b < nb; b++)
+    for (int k = jb.first[b]; k < jb.first[b] + jb.count[b]; k++) bo[k] = (int)b;
+  s->blk_of.upload(bo.data(), bo.size(), st);
+  CK(cudaStreamSynchronize(st));  // the host vectors above die here
 }
 
 void ensure_device(sphgpu_space* s) {
@@ -244,6 +259,18 @@ void ensure_device(sphgpu_space* s) {
   s->queue.alloc(16);  // [0..7] work counters, [8..15] unit counts
   s->redo.alloc(std::max(1, s->prm.max_iter));
   s->hit_ctr.alloc(4);
+  {
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    const size_t bytes = (size_t)n * kListCap * sizeof(int);
+    if (bytes <= fr / 4) {
+      s->nl.alloc((size_t)n * kListCap);
+      s->nl_cnt.alloc(n);
+      s->nl_T.alloc(n);
+      CK(cudaMemsetAsync(s->nl_cnt.p, 0xff, sizeof(int) * n, st));  // -1: no list
+      s->lists = true;
+    }
+  }
   for (auto& e : s->ev) CK(cudaEventCreate(&e));
   CK(cudaMemsetAsync(s->fin0.p, 0, sizeof(float4) * n, st));
   CK(cudaMemsetAsync(s->fin1.p, 0, sizeof(float2) * n, st));
@@ -308,19 +335,27 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   if (s->count_hits) a.hits = s->hit_ctr.p + (qslot == 0 ? 0 : (qslot == 2 ? 2 : 1));
   a.band = kBand;
   a.mode = mode;
+  a.nl = nullptr;
+  a.nl_cnt = nullptr;
+  a.nl_T = nullptr;
+  a.nl_cap = 0;
+  a.nl_scale = 1.f;
   return a;
 }
 
 // Build the work groups of a loop (windows whose particles carry `need`
 // in their flags) and run the gather over them.
+// veto: skip particles with any of these flag bits; lists: record the re-run
+// neighbour lists (density re-run mode)
 void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
                     int mode, bool force, int need, const int* gate,
-                    int leaf_begin = 0, int leaf_end = -1) {
+                    int leaf_begin = 0, int leaf_end = -1, int veto = 0,
+                    bool lists = false) {
   const int nl = (int)s->space->leaves().size();
   if (leaf_end < 0) leaf_end = nl;
   CK(cudaMemsetAsync(s->queue.p + qslot, 0, sizeof(int), st));
   CK(launch_build_units(s->leaves.p + leaf_begin, leaf_end - leaf_begin,
-                        s->leaf_window_begin.p + leaf_begin, s->flags.p, need,
+                        s->leaf_window_begin.p + leaf_begin, s->flags.p, need, veto,
                         dp.lpb.p + leaf_begin, s->units.p, gate, st));
   // the groups of this leaf range occupy [w0, w1) of the window slots
   G2Args a = gargs(s, dp, qslot, mode);
@@ -329,7 +364,34 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
   a.count = w1 - w0;
   a.count_ptr = nullptr;
   a.gate = gate;  // gated loops (ghost re-runs) do nothing when it reads 0
-  CK(launch_gather(a, force, s->num_sms, w1 - w0, st, s->tune.block_warps));
+  if (lists) {
+    a.nl = s->nl.p;
+    a.nl_cnt = s->nl_cnt.p;
+    a.nl_T = s->nl_T.p;
+    a.nl_cap = kListCap;
+    a.nl_scale = kListScale;
+  }
+  CK(launch_gather(a, force, s->num_sms, w1 - w0, st, s->tune.block_warps, lists));
+}
+
+ListArgs largs(sphgpu_space* s, const int* gate) {
+  ListArgs l;
+  l.p = s->P;
+  l.nl = s->nl.p;
+  l.nl_cnt = s->nl_cnt.p;
+  l.nl_T = s->nl_T.p;
+  l.nl_cap = kListCap;
+  l.leaf_pair_begin = s->dplan_s.lpb.p;
+  l.pair_block = s->dplan_s.pb.p;
+  l.pair_entry = s->dplan_s.pe.p;
+  l.entries = s->dplan_s.entries.p;
+  l.blk_of = s->blk_of.p;
+  const double* w = s->space->width();
+  l.top_width = make_float3((float)w[0], (float)w[1], (float)w[2]);
+  l.band = kBand;
+  l.gate = gate;
+  l.hits = s->count_hits ? s->hit_ctr.p + 1 : nullptr;
+  return l;
 }
 
 GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
@@ -355,7 +417,16 @@ GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
 void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st) {
   for (int k = 0; k < s->prm.max_iter; k++) {
     CK(launch_ghost(ghargs(s, k, 0, s->P.n), st));
-    enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k);
+    if (!s->lists || !s->tune.rerun_lists) {
+      enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k);
+    } else if (k == 0) {
+      // the first re-run records each particle's neighbour list
+      enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k, 0, -1, 0, true);
+    } else {
+      // later re-runs: from the lists where they cover h, the gather for the rest
+      CK(launch_redo_from_lists(largs(s, s->redo.p + k), st));
+      enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k, 0, -1, 8);
+    }
   }
 }
 
@@ -588,7 +659,7 @@ int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
     if (s->dev) CK(cudaStreamSynchronize(s->stream));
     const bool reblock = t->jtile != s->tune.jtile;
     s->tune = *t;
-    s->tune.persistent = 1;
+    s->tune.rerun_lists = t->rerun_lists ? 1 : 0;
     drop_graph(s);
     if (reblock) {
       // blocks, candidate lists and every plan referring to them change
@@ -964,7 +1035,7 @@ int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms
   int k = 0;
   for (int a = 0; a < 3; a++)
     for (int b = 0; b < 2; b++, k++) {
-      sphgpu_tuning t{1, jt[a], 1, bw[b]};
+      sphgpu_tuning t{1, jt[a], s->tune.rerun_lists, bw[b]};
       int rc = sphgpu_set_tuning(s, &t);
       if (rc) return rc;
       rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);  // plan + capture + warm

@@ -38,15 +38,15 @@ __global__ void block_hmax(const int2* __restrict__ fc, float4* __restrict__ lo,
   }
 }
 
-template <bool FORCE, int WPB, int MINB>
+template <bool FORCE, int WPB, int MINB, bool LISTS = false>
 static cudaError_t launch_variant(const G2Args& a, int num_sms, int max_units,
                                   cudaStream_t s) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, gather_lanes<FORCE, OUT_STORE, WPB, MINB>, WPB * 32, 0);
+      &per_sm, gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS>, WPB * 32, 0);
   int grid = std::max(1, per_sm) * num_sms;
   grid = std::max(1, std::min(grid, (max_units + WPB - 1) / WPB));
-  gather_lanes<FORCE, OUT_STORE, WPB, MINB><<<grid, WPB * 32, 0, s>>>(a);
+  gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS><<<grid, WPB * 32, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -54,7 +54,10 @@ static cudaError_t launch_variant(const G2Args& a, int num_sms, int max_units,
 // 85 registers) or 4 warps x 6 blocks per SM (up to 85 registers, finer
 // blocks for the tail of the work queue).
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
-                          cudaStream_t s, int block_warps) {
+                          cudaStream_t s, int block_warps, bool lists) {
+  if (lists && !force)
+    return block_warps == 4 ? launch_variant<false, 4, 6, true>(a, num_sms, max_units, s)
+                            : launch_variant<false, 8, 3, true>(a, num_sms, max_units, s);
   if (block_warps == 4)
     return force ? launch_variant<true, 4, 6>(a, num_sms, max_units, s)
                  : launch_variant<false, 4, 6>(a, num_sms, max_units, s);
@@ -64,12 +67,19 @@ cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_unit
 
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                const int* leaf_window_begin, const uint8_t* flags,
-                               int need, const int* leaf_pair_begin, int4* units,
-                               const int* gate, cudaStream_t s) {
+                               int need, int veto, const int* leaf_pair_begin,
+                               int4* units, const int* gate, cudaStream_t s) {
   int g = (nleaves * 32 + 255) / 256;
   g = std::max(1, std::min(g, 152 * 16));
-  build_units<<<g, 256, 0, s>>>(leaves, nleaves, leaf_window_begin, flags, need,
+  build_units<<<g, 256, 0, s>>>(leaves, nleaves, leaf_window_begin, flags, need, veto,
                                 leaf_pair_begin, units, gate);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_redo_from_lists(const ListArgs& a, cudaStream_t s) {
+  int g = (a.p.n + 255) / 256;
+  g = std::max(1, std::min(g, 152 * 16));
+  redo_from_lists<<<g, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -74,6 +74,35 @@ static __device__ __forceinline__ float h2_exact(float h) {
   return __fmul_rn(__fmul_rn(h, h), SPH_KG2);
 }
 
+// Density sums of one hit (runner_iact_nonsym_density, hydro_iact.h:137-189);
+// dx = x_i - x_j in the group's frame.
+static __device__ __forceinline__ void density_hit(float dx, float dy, float dz, float r2,
+                                                   const float4& vi, const float4& vm,
+                                                   float hi_inv, float& s0, float& s1,
+                                                   float& s2, float& s3, float& s4,
+                                                   float& s5, float& s6, float& s7) {
+  const float mj = vm.w;
+  // hardware reciprocal square root (MUFU.RSQ, ~2 ulp): the sums are held
+  // to 1e-4 relative, and the neighbour decision was made exactly
+  const float r_inv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+  const float r = r2 * r_inv;
+  const float dvx = vi.x - vm.x, dvy = vi.y - vm.y, dvz = vi.z - vm.z;
+  const float dvdr = dvx * dx + dvy * dy + dvz * dz;
+  const float ui = r * hi_inv;
+  float W, dW;
+  wendland(ui, W, dW);
+  const float t3 = SPH_HDIM * W + ui * dW;
+  s0 += mj * W;
+  s1 -= mj * t3;
+  s2 += W;
+  s3 -= t3;
+  const float fac = mj * dW * r_inv;
+  s4 -= fac * dvdr;
+  s5 += fac * (dvy * dz - dvz * dy);
+  s6 += fac * (dvz * dx - dvx * dz);
+  s7 += fac * (dvx * dy - dvy * dx);
+}
+
 // Per-warp shared memory: the staged partner block and each lane's ring of
 // pending hits (partner index and frame-offset index packed in 32 bits).
 #define QCAP 32  // power of two: ring positions wrap with & (QCAP - 1)
@@ -86,6 +115,7 @@ struct LaneSmem {
   float4 slo[32];      // their boxes
   float4 shi[32];
   int q[QCAP][32];     // per-lane hit ring
+  int lb[8][32];       // per-lane staging of neighbour-list items (LISTS)
 };
 
 // Frame offset of a partner top cell from its index in the 3x3x3
@@ -110,7 +140,10 @@ __device__ __forceinline__ float3 offset_of(int idx, float3 tw) {
 //   4. when a ring is nearly full, all lanes compute interactions from
 //      their rings for about as many passes as the rings hold on average;
 //      the last drain empties them.  Sums stay in the lane's registers.
-template <bool FORCE, int OUT = OUT_STORE, int WPB = WARPS_PER_BLOCK, int MINB = 3>
+// LISTS (density re-runs): also record every candidate below the list bound
+// into the particle's neighbour list (G2Args::nl), the culls using that bound.
+template <bool FORCE, int OUT = OUT_STORE, int WPB = WARPS_PER_BLOCK, int MINB = 3,
+          bool LISTS = false>
 __global__ void __launch_bounds__(WPB * 32, MINB)
 gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
   __shared__ LaneSmem smem[WPB];
@@ -154,12 +187,15 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     const float hid_inv = (hi_inv * hi_inv) * (hi_inv * hi_inv);
     const float mi_inv = 1.f / vi.w;
     const float lo2 = hig2 * (1.f - band), hi2 = hig2 * (1.f + band);
+    // list bound (recording re-run): the culls below use it instead of H^2
+    const float trec = LISTS ? hig2 * a.nl_scale : hig2;
+    int lcnt = 0;
     // group box grown by the group's largest radius
     float gx0 = valid ? pi.x : 3.4e38f, gy0 = valid ? pi.y : 3.4e38f,
           gz0 = valid ? pi.z : 3.4e38f;
     float gx1 = valid ? pi.x : -3.4e38f, gy1 = valid ? pi.y : -3.4e38f,
           gz1 = valid ? pi.z : -3.4e38f;
-    float gh2 = hig2;
+    float gh2 = trec;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       gx0 = fminf(gx0, __shfl_xor_sync(FULL, gx0, off));
@@ -184,28 +220,16 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
                   dz = pi.z - (q.z + fd.z);
       const float r2 = dx * dx + dy * dy + dz * dz;
       const float4 vm = P.velm[j];
-      const float mj = vm.w;
-      // hardware reciprocal square root (MUFU.RSQ, ~2 ulp): the sums are
-      // held to 1e-4 relative, and the neighbour decision was made exactly
-      const float r_inv = r2 > 0.f ? rsqrtf(r2) : 0.f;
-      const float r = r2 * r_inv;
-      const float dvx = vi.x - vm.x, dvy = vi.y - vm.y, dvz = vi.z - vm.z;
-      const float dvdr = dvx * dx + dvy * dy + dvz * dz;
       if (!FORCE) {
-        const float ui = r * hi_inv;
-        float W, dW;
-        wendland(ui, W, dW);
-        const float t3 = SPH_HDIM * W + ui * dW;
-        s0 += mj * W;
-        s1 -= mj * t3;
-        s2 += W;
-        s3 -= t3;
-        const float fac = mj * dW * r_inv;
-        s4 -= fac * dvdr;
-        s5 += fac * (dvy * dz - dvz * dy);
-        s6 += fac * (dvz * dx - dvx * dz);
-        s7 += fac * (dvx * dy - dvy * dx);
+        density_hit(dx, dy, dz, r2, vi, vm, hi_inv, s0, s1, s2, s3, s4, s5, s6, s7);
       } else {
+        const float mj = vm.w;
+        // hardware reciprocal square root (MUFU.RSQ, ~2 ulp): the sums are
+        // held to 1e-4 relative, and the neighbour decision was made exactly
+        const float r_inv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+        const float r = r2 * r_inv;
+        const float dvx = vi.x - vm.x, dvy = vi.y - vm.y, dvz = vi.z - vm.z;
+        const float dvdr = dvx * dx + dvy * dy + dvz * dz;
         const float hj = q.w;
         const float4 fj = P.fin0[j];
         const float bj = P.fin1[j].x;
@@ -315,7 +339,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           const float dx = fmaxf(fmaxf(slo.x - px, px - shi.x), 0.f);
           const float dy = fmaxf(fmaxf(slo.y - py, py - shi.y), 0.f);
           const float dz = fmaxf(fmaxf(slo.z - pz, pz - shi.z), 0.f);
-          const float R2 = FORCE ? fmaxf(hig2, slo.w) : hig2;
+          const float R2 = FORCE ? fmaxf(hig2, slo.w) : trec;
           mine = dx * dx + dy * dy + dz * dz < R2 * (1.f + 4.f * band) + 1e-30f;
         }
         if (!__any_sync(FULL, mine)) continue;
@@ -341,7 +365,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         // mask, band candidates are decided by the exact FP64 predicate in
         // the reference frame (rare: the warp votes once per eight).
         for (int t0 = 0; t0 < bcount; t0 += 8) {
-          unsigned hm = 0u, bm = 0u;
+          unsigned hm = 0u, bm = 0u, lm = 0u;
 #pragma unroll
           for (int u = 0; u < 8; u++) {
             const float4 q = ws.jpos[t0 + u];
@@ -357,11 +381,27 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
               hm |= 1u << u;
             else if (r2 < U2)
               bm |= 1u << u;
+            if (LISTS && r2 < trec) lm |= 1u << u;
           }
           const int left = bcount - t0;
           const unsigned live = (left >= 8 ? 0xffu : ((1u << left) - 1u)) & (okmask >> t0);
           hm &= live;
           bm &= live;
+          if (LISTS) {
+            // items go to the lane's row of the list 8 at a time (32 bytes)
+            lm &= live;
+            while (lm) {
+              const int u = __ffs(lm) - 1;
+              lm &= lm - 1u;
+              ws.lb[lcnt & 7][lane] = pk + t0 + u;
+              lcnt++;
+              if ((lcnt & 7) == 0 && lcnt <= a.nl_cap) {
+                int4* row = reinterpret_cast<int4*>(a.nl + (size_t)i * a.nl_cap + (lcnt - 8));
+                row[0] = make_int4(ws.lb[0][lane], ws.lb[1][lane], ws.lb[2][lane], ws.lb[3][lane]);
+                row[1] = make_int4(ws.lb[4][lane], ws.lb[5][lane], ws.lb[6][lane], ws.lb[7][lane]);
+              }
+            }
+          }
           while (hm) {
             const int u = __ffs(hm) - 1;
             hm &= hm - 1u;
@@ -383,6 +423,13 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     }
     drain(true);
     if (!valid) continue;
+    if (LISTS) {
+      if (lcnt <= a.nl_cap)
+        for (int k = lcnt & ~7; k < lcnt; k++)
+          a.nl[(size_t)i * a.nl_cap + k] = ws.lb[k & 7][lane];
+      a.nl_cnt[i] = lcnt <= a.nl_cap ? lcnt : -1;
+      a.nl_T[i] = trec;
+    }
     if (OUT == OUT_CALLER) {
       const size_t k = (size_t)co.perm[i];
       float* o = co.fields + 8 * k;
@@ -434,7 +481,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
 // mask are skipped by the gathers.
 static __global__ void build_units(const LeafInfo* __restrict__ leaves, int nleaves,
                                    const int* __restrict__ leaf_window_begin,
-                                   const uint8_t* __restrict__ flags, int need,
+                                   const uint8_t* __restrict__ flags, int need, int veto,
                                    const int* __restrict__ leaf_pair_begin,
                                    int4* __restrict__ units, const int* gate) {
   if (gate && *gate == 0) return;
@@ -446,10 +493,76 @@ static __global__ void build_units(const LeafInfo* __restrict__ leaves, int nlea
     const int p0 = leaf_pair_begin[l], p1 = leaf_pair_begin[l + 1];
     int slot = leaf_window_begin[l];
     for (int w0 = 0; w0 < count; w0 += 32, slot++) {
-      const bool ok = w0 + lane < count && (flags[first + w0 + lane] & need) == need;
+      const int f = w0 + lane < count ? flags[first + w0 + lane] : 0;
+      const bool ok = w0 + lane < count && (f & need) == need && !(f & veto);
       const unsigned m = __ballot_sync(FULL, ok);
       if (lane == 0) units[slot] = make_int4(first + w0, p0 == p1 ? 0 : (int)m, p0, p1);
     }
+  }
+}
+
+// The re-run list entry that pairs particle i (depth_h dh, in `leaf`) with
+// j-block b, or null (runner_ghost.c:1548-1579 pairs each (i, j) once).
+static __device__ const Entry* rerun_entry(const ListArgs& a, int leaf, int b, int dh) {
+  for (int p = a.leaf_pair_begin[leaf]; p < a.leaf_pair_begin[leaf + 1]; p++) {
+    if (a.pair_block[p] != b) continue;
+    const Entry* E = &a.entries[a.pair_entry[p]];
+    if (dh >= E->min_depth && dh <= E->max_depth) return E;
+  }
+  return nullptr;
+}
+
+static __global__ void redo_from_lists(ListArgs a) {
+  if (a.gate && *a.gate == 0) return;
+  const DevParticles& P = a.p;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n;
+       i += gridDim.x * blockDim.x) {
+    const uint8_t fl = P.flags[i];
+    if ((fl & 3) != 3) continue;  // active and re-run this round
+    const float4 pi = P.posh[i];
+    const float hig2 = h2_exact(pi.w);
+    const float L2 = hig2 * (1.f - a.band), U2 = hig2 * (1.f + a.band);
+    const int cnt = a.nl_cnt[i];
+    if (cnt < 0 || !(U2 <= a.nl_T[i])) {  // the list does not cover h: gather
+      P.flags[i] = fl & ~8;
+      continue;
+    }
+    P.flags[i] = fl | 8;
+    const float4 vi = P.velm[i];
+    const float hi_inv = 1.f / pi.w;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f, s5 = 0.f, s6 = 0.f, s7 = 0.f;
+    int ngb = 0;
+    const int4* row = reinterpret_cast<const int4*>(a.nl + (size_t)i * a.nl_cap);
+    for (int t0 = 0; t0 < cnt; t0 += 8) {
+      // eight items and their partners' positions in flight at once
+      const int4 p0 = row[t0 / 4], p1 = row[t0 / 4 + 1];
+      const int pk[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+      float4 q[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        q[u] = t0 + u < cnt ? P.posh[pk[u] & 0x07ffffff] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        if (t0 + u >= cnt) break;
+        const int j = pk[u] & 0x07ffffff;
+        const float3 fd = offset_of((int)((unsigned)pk[u] >> 27), a.top_width);
+        const float dx = pi.x - (q[u].x + fd.x), dy = pi.y - (q[u].y + fd.y),
+                    dz = pi.z - (q[u].z + fd.z);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        bool hit = r2 < L2;
+        if (!hit && r2 < U2) {
+          const Entry* E = rerun_entry(a, P.leaf_of[i], a.blk_of[j], P.depth_h[i]);
+          hit = E != nullptr && exact_r2_2(P.xd, i, j, E) < hig2;
+        }
+        if (!hit) continue;
+        density_hit(dx, dy, dz, r2, vi, P.velm[j], hi_inv, s0, s1, s2, s3, s4, s5, s6, s7);
+        ngb++;
+      }
+    }
+    P.dens0[i] = make_float4(s0, s1, s2, s3);
+    P.dens1[i] = make_float4(s4, s5, s6, s7);
+    P.ngb_d[i] = ngb;
+    if (a.hits) atomicAdd(a.hits, (unsigned long long)ngb);
   }
 }
 

@@ -73,7 +73,7 @@ cudaError_t launch_density_noalloc(const G2Args& base, const LeafInfo* leaves,
   int4* units = reinterpret_cast<int4*>(scratch + NOALLOC_UNITS_OFFSET);
   const int g = std::max(1, std::min((nleaves * 32 + 255) / 256, num_sms * 16));
   build_units<<<g, 256, 0, s>>>(leaves, nleaves, leaf_window_begin, base.p.flags,
-                                1, leaf_pair_begin, units, nullptr);
+                                1, 0, leaf_pair_begin, units, nullptr);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   G2Args a = base;

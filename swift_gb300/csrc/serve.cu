@@ -555,12 +555,18 @@ struct sphgpu_server {
     a.gate = gate;
     a.band = kServeBand;
     a.mode = mode;
+    a.nl = nullptr;  // no re-run lists in the arena
+    a.nl_cnt = nullptr;
+    a.nl_T = nullptr;
+    a.nl_cap = 0;
+    a.nl_scale = 1.f;
     return a;
   }
 
   void gather(int k, int qslot, int mode, bool force, int need, const int* gate) {
     CK(cudaMemsetAsync(queue.p + qslot, 0, sizeof(int), st));
-    CK(launch_build_units(leaves.p, (int)hwL, lwb.p, flags.p, need, lpb[k].p, units.p, gate, st));
+    CK(launch_build_units(leaves.p, (int)hwL, lwb.p, flags.p, need, 0, lpb[k].p, units.p, gate,
+                          st));
     CK(launch_gather(gargs(k, qslot, mode, gate), force, num_sms, (int)hwW, st, 8));
   }
 

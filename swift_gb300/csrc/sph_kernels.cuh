@@ -59,6 +59,37 @@ struct G2Args {
   const int* gate;              // optional: do nothing when *gate == 0
   float band;                   // relative band of the exact predicate
   int mode;                     // GatherMode
+  // Neighbour lists of the ghost's re-runs, recorded by the first re-run
+  // (gathers launched with lists): item t of particle i at
+  // nl[i * nl_cap + t] (partner index | frame-offset index << 27), for
+  // every candidate with FP32 r^2 below nl_scale * (gamma h)^2; nl_cap is a
+  // multiple of 8 (items are written 8 at a time).
+  int* nl;
+  int* nl_cnt;                  // items per particle, -1 when they overflowed
+  float* nl_T;                  // the r^2 bound the items were recorded under
+  int nl_cap;
+  float nl_scale;
+};
+
+// Later re-runs from the lists: particles whose list covers their new
+// search radius are computed from it (and flagged 8); the others are left
+// to the gather.  Candidates inside the band around H^2 are decided exactly
+// in the frame of the re-run list entry that pairs them.
+struct ListArgs {
+  DevParticles p;
+  const int* nl;
+  const int* nl_cnt;
+  const float* nl_T;
+  int nl_cap;
+  const int* leaf_pair_begin;   // the re-run (subset) lists, per leaf
+  const int* pair_block;
+  const int* pair_entry;
+  const Entry* entries;
+  const int* blk_of;            // j-block of every particle
+  float3 top_width;
+  float band;
+  const int* gate;              // do nothing when *gate == 0
+  unsigned long long* hits;     // optional: total neighbour hits
 };
 
 struct GhostArgs {
@@ -70,12 +101,16 @@ struct GhostArgs {
   int* redo_count;              // [max_iter] particles sent to another round
 };
 
+// lists: record the re-run neighbour lists (density re-run mode, a.nl set)
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
-                          cudaStream_t s, int block_warps = 8);
+                          cudaStream_t s, int block_warps = 8, bool lists = false);
+// Work groups of the particles whose flags hold every bit of `need` and no
+// bit of `veto`.
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                const int* leaf_window_begin, const uint8_t* flags,
-                               int need, const int* leaf_pair_begin, int4* units,
-                               const int* gate, cudaStream_t s);
+                               int need, int veto, const int* leaf_pair_begin,
+                               int4* units, const int* gate, cudaStream_t s);
+cudaError_t launch_redo_from_lists(const ListArgs& a, cudaStream_t s);
 int noalloc_max_particles();
 int noalloc_max_units();
 cudaError_t launch_density_noalloc(const G2Args& base, const LeafInfo* leaves,

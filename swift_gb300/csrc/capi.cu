@@ -134,11 +134,8 @@ void build_plans(sphgpu_space* s) {
 
 void upload_activity(sphgpu_space* s, cudaStream_t st);
 
-// Re-run neighbour lists: at most kListCap items per particle, recorded for
-// r^2 < kListScale (gamma h)^2 (a radius 2 % above the first re-run's, which
-// the later re-runs' h stay within for almost every particle).
+// Re-run neighbour lists: at most kListCap items per particle.
 constexpr int kListCap = 128;
-constexpr float kListScale = 1.0404f;
 
 // j-block boxes and particle ranges of the current j-block depth.
 void upload_blocks(sphgpu_space* s, cudaStream_t st) {
@@ -339,7 +336,6 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   a.nl_cnt = nullptr;
   a.nl_T = nullptr;
   a.nl_cap = 0;
-  a.nl_scale = 1.f;
   return a;
 }
 
@@ -369,7 +365,6 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
     a.nl_cnt = s->nl_cnt.p;
     a.nl_T = s->nl_T.p;
     a.nl_cap = kListCap;
-    a.nl_scale = kListScale;
   }
   CK(launch_gather(a, force, s->num_sms, w1 - w0, st, s->tune.block_warps, lists));
 }

@@ -140,8 +140,8 @@ __device__ __forceinline__ float3 offset_of(int idx, float3 tw) {
 //   4. when a ring is nearly full, all lanes compute interactions from
 //      their rings for about as many passes as the rings hold on average;
 //      the last drain empties them.  Sums stay in the lane's registers.
-// LISTS (density re-runs): also record every candidate below the list bound
-// into the particle's neighbour list (G2Args::nl), the culls using that bound.
+// LISTS (density re-runs): also record every candidate below the band's top
+// into the particle's neighbour list (G2Args::nl).
 template <bool FORCE, int OUT = OUT_STORE, int WPB = WARPS_PER_BLOCK, int MINB = 3,
           bool LISTS = false>
 __global__ void __launch_bounds__(WPB * 32, MINB)
@@ -187,15 +187,17 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     const float hid_inv = (hi_inv * hi_inv) * (hi_inv * hi_inv);
     const float mi_inv = 1.f / vi.w;
     const float lo2 = hig2 * (1.f - band), hi2 = hig2 * (1.f + band);
-    // list bound (recording re-run): the culls below use it instead of H^2
-    const float trec = LISTS ? hig2 * a.nl_scale : hig2;
+    // Recording re-run: the list keeps every candidate below the band's top,
+    // which covers any later re-run whose h is not larger (Newton's iterates
+    // on the increasing, convex n(h) - eta^3 fall towards the root after the
+    // first step, so almost all of them are)
     int lcnt = 0;
     // group box grown by the group's largest radius
     float gx0 = valid ? pi.x : 3.4e38f, gy0 = valid ? pi.y : 3.4e38f,
           gz0 = valid ? pi.z : 3.4e38f;
     float gx1 = valid ? pi.x : -3.4e38f, gy1 = valid ? pi.y : -3.4e38f,
           gz1 = valid ? pi.z : -3.4e38f;
-    float gh2 = trec;
+    float gh2 = hig2;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       gx0 = fminf(gx0, __shfl_xor_sync(FULL, gx0, off));
@@ -339,7 +341,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           const float dx = fmaxf(fmaxf(slo.x - px, px - shi.x), 0.f);
           const float dy = fmaxf(fmaxf(slo.y - py, py - shi.y), 0.f);
           const float dz = fmaxf(fmaxf(slo.z - pz, pz - shi.z), 0.f);
-          const float R2 = FORCE ? fmaxf(hig2, slo.w) : trec;
+          const float R2 = FORCE ? fmaxf(hig2, slo.w) : hig2;
           mine = dx * dx + dy * dy + dz * dz < R2 * (1.f + 4.f * band) + 1e-30f;
         }
         if (!__any_sync(FULL, mine)) continue;
@@ -365,7 +367,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         // mask, band candidates are decided by the exact FP64 predicate in
         // the reference frame (rare: the warp votes once per eight).
         for (int t0 = 0; t0 < bcount; t0 += 8) {
-          unsigned hm = 0u, bm = 0u, lm = 0u;
+          unsigned hm = 0u, bm = 0u;
 #pragma unroll
           for (int u = 0; u < 8; u++) {
             const float4 q = ws.jpos[t0 + u];
@@ -381,7 +383,6 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
               hm |= 1u << u;
             else if (r2 < U2)
               bm |= 1u << u;
-            if (LISTS && r2 < trec) lm |= 1u << u;
           }
           const int left = bcount - t0;
           const unsigned live = (left >= 8 ? 0xffu : ((1u << left) - 1u)) & (okmask >> t0);
@@ -389,7 +390,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           bm &= live;
           if (LISTS) {
             // items go to the lane's row of the list 8 at a time (32 bytes)
-            lm &= live;
+            unsigned lm = hm | bm;
             while (lm) {
               const int u = __ffs(lm) - 1;
               lm &= lm - 1u;
@@ -428,7 +429,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         for (int k = lcnt & ~7; k < lcnt; k++)
           a.nl[(size_t)i * a.nl_cap + k] = ws.lb[k & 7][lane];
       a.nl_cnt[i] = lcnt <= a.nl_cap ? lcnt : -1;
-      a.nl_T[i] = trec;
+      a.nl_T[i] = hi2;
     }
     if (OUT == OUT_CALLER) {
       const size_t k = (size_t)co.perm[i];

@@ -62,13 +62,12 @@ struct G2Args {
   // Neighbour lists of the ghost's re-runs, recorded by the first re-run
   // (gathers launched with lists): item t of particle i at
   // nl[i * nl_cap + t] (partner index | frame-offset index << 27), for
-  // every candidate with FP32 r^2 below nl_scale * (gamma h)^2; nl_cap is a
+  // every candidate with FP32 r^2 below (gamma h)^2 (1 + band); nl_cap is a
   // multiple of 8 (items are written 8 at a time).
   int* nl;
   int* nl_cnt;                  // items per particle, -1 when they overflowed
   float* nl_T;                  // the r^2 bound the items were recorded under
   int nl_cap;
-  float nl_scale;
 };
 
 // Later re-runs from the lists: particles whose list covers their new

@@ -1,6 +1,6 @@
 /* Oracle link stubs.  The reference's hydro path never reaches these
  * symbols; they live in I/O, mesh-gravity, lightcone and neutrino units that
- * need HDF5/FFTW/GSL, which this build leaves out.  Each one aborts, so any
+ * need HDF5/FFTW/GSL, which the oracle does not compile.  Each one aborts, so any
  * unexpected use fails loudly instead of returning garbage. */
 #include <stdio.h>
 #include <stdlib.h>

@@ -2,7 +2,7 @@
 
 ``build()`` compiles swift_gb300/csrc/*.cu and *.cpp with nvcc into
 swift_gb300/_build/libswiftgb300.so (git-ignored, rebuilt on every machine:
-the x86 container and the aarch64 GPU hosts each build their own).  The
+x86 and aarch64 hosts each build their own).  The
 translation units compile in parallel; one -gencode, no cmake.
 """
 from __future__ import annotations

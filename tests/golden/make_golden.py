@@ -8,7 +8,7 @@ full-box sums of every output field (float64 sums of the float32 values) and
 the complete outputs of a seeded sample of particles.  Inputs are
 regenerated by swift_gb300.ics from the recipe, so the fixtures stay small.
 
-Run in a container that has the reference tree:
+Run on a machine that has the reference tree (oracle/build_ref.sh builds it):
     python tests/golden/make_golden.py
 """
 import os

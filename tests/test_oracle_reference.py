@@ -1,7 +1,7 @@
 """Oracle vs the reference's own loops run here (oracle/_ref), on fresh
 seeds: cell assignment, particle order and every density / ghost / force
 output must be bit-identical.  Skipped where the reference build is absent
-(the GPU hosts carry no reference tree)."""
+(machines without the reference tree)."""
 import os
 import tempfile
 

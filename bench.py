@@ -273,6 +273,7 @@ def run_sparse(args):
     for b in seq[:args.warmup]:
         one(b, False)
     sp.phase_times(reset=True)
+    sp.host_times(reset=True)
     clocks = ClockSampler(local_rank)
     t_b, inter = [], []
     for b in seq[args.warmup:]:
@@ -281,6 +282,7 @@ def run_sparse(args):
         inter.append(int(hits[3]) + int(hits[2]))
     clk = clocks.stop()
     phase_ms, nsteps = sp.phase_times(reset=True)
+    host_ms = {k: v / max(1, len(t_b)) for k, v in sp.host_times(reset=True).items()}
     # plain form: same state origin, same steps
     prime()
     for b in seq[:min(args.warmup, 1)]:
@@ -304,6 +306,7 @@ def run_sparse(args):
         "phases_ms_gpu": {"density": phase_ms[0] / max(1, nsteps),
                           "ghost_rounds": phase_ms[1] / max(1, nsteps),
                           "force": phase_ms[2] / max(1, nsteps)},
+        "host_ms_per_step": host_ms,
         "batched_ms_per_step": [round(1e3 * t, 3) for t in t_b],
         "plain_ms_per_step": [round(1e3 * t, 3) for t in t_p],
         "plain_over_batched": ms_p / ms_p_same,
@@ -514,9 +517,10 @@ def run_ours(args):
                     "h2d_bytes_per_step": int(n * (24 + 12 + 4 + 4 + 4)),
                     "d2h_bytes_per_step": int(n * 24 * 4)},
             # per step: begin-step, density units + gather, 30 ghost rounds
-            # (ghost, units, re-run gather; gated ones return at once),
-            # block h_max, force units + gather
-            "gpu_launches": 96 * args.steps,
+            # (ghost, units, re-run gather, and the list kernel after the
+            # first; gated ones return at once), block h_max, force units +
+            # gather
+            "gpu_launches": (96 + (29 if tuning.get("rerun_lists") else 0)) * args.steps,
             "clocks": clk,
             "cpu_baseline": cb,
         }

@@ -154,6 +154,11 @@ int sphgpu_autotune(sphgpu_space *s, int32_t reps, sphgpu_tuning *best,
  * SPHGPU_ENOCONV if some h did not converge in max_iter rounds. */
 int sphgpu_step(sphgpu_space *s, int32_t stages, void *stream);
 
+/* Host time (ms, summed since the last reset) of the planning that steps
+ * need: [0] sphgpu_set_active's cell refresh and list building, [1] its
+ * uploads, [2] the force lists planned inside steps after a ghost. */
+int sphgpu_host_times(sphgpu_space *s, double ms[3], int32_t reset);
+
 /* Per-loop device time of the batched steps run so far (CUDA events on the
  * step's stream): ms_sum[0] density first pass, [1] ghost rounds (Newton
  * updates + density re-runs), [2] force loop; *steps = steps timed. */

@@ -84,6 +84,7 @@ SIGNATURES = {
     "sphgpu_dosub_pair2_force": (ctypes.c_int, [_P, _I32, _I32, _P]),
     "sphgpu_do_end_hydro_force": (ctypes.c_int, [_P, _P]),
     "sphgpu_phase_times": (ctypes.c_int, [_P, _P, _P, _I32]),
+    "sphgpu_host_times": (ctypes.c_int, [_P, _P, _I32]),
     "sphgpu_count_hits": (ctypes.c_int, [_P, _P]),
     "sphgpu_density_noalloc": (ctypes.c_int, [_P, _P, _P, _P]),
     "sphgpu_autotune": (ctypes.c_int, [_P, _I32, _P, _P, _P]),
@@ -214,7 +215,7 @@ class Space:
         return geom, ints
 
     # -- configuration -----------------------------------------------------
-    def set_tuning(self, tpi=1, jtile=32, rerun_lists=1, block_warps=8):
+    def set_tuning(self, tpi=1, jtile=16, rerun_lists=1, block_warps=8):
         t = Tuning(tpi, jtile, rerun_lists, block_warps)
         _check(lib().sphgpu_set_tuning(self._h, ctypes.byref(t)))
 
@@ -289,6 +290,14 @@ class Space:
                                       _ptr(b["m"]), _ptr(b["h"]), _ptr(b["u"]),
                                       _ptr(fields), stream))
         return fields
+
+    def host_times(self, reset=False):
+        """Host planning in ms: activation lists, activation uploads, force
+        lists planned inside steps."""
+        ms = np.zeros(3, np.float64)
+        _check(lib().sphgpu_host_times(self._h, _ptr(ms), int(bool(reset))))
+        return {"activation_planning": ms[0], "activation_upload": ms[1],
+                "force_planning": ms[2]}
 
     def phase_times(self, reset=False):
         """(ms summed per loop [density, ghost, force], steps timed)."""

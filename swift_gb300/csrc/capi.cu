@@ -6,10 +6,12 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <functional>
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/swift_gb300.h"
@@ -44,7 +46,7 @@ struct sphgpu_space {
   std::vector<double> x_in;
   std::vector<float> v_in, m_in, h_in, u_in;
   std::vector<int8_t> tb_in;
-  sphgpu_tuning tune{1, 32, 1, 8};
+  sphgpu_tuning tune{1, SPH_JBLOCK, 1, 8};
 
   // host plans
   Plan plan_d, plan_s, plan_f;
@@ -102,6 +104,7 @@ struct sphgpu_space {
   cudaGraphExec_t graph[1] = {nullptr};
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double plan_ms = 0;  // host planning inside steps (force re-plans)
+  double act_plan_ms = 0, act_upload_ms = 0;  // sphgpu_set_active
   double phase_ms[3] = {0, 0, 0};
   long long phase_steps = 0;
   DBuf<unsigned long long> hit_ctr;
@@ -127,9 +130,26 @@ struct sphgpu_space {
 
 namespace {
 
+// The first-pass and re-run lists depend only on the tree and the activity:
+// they are built side by side (each also spreads over the host cores, but at
+// low activity few of their work blocks hold active cells).
 void build_plans(sphgpu_space* s) {
-  s->space->plan_density(s->plan_d, false);
-  s->space->plan_subset(s->plan_s);
+  std::exception_ptr err;
+  std::thread t([&]() {
+    try {
+      s->space->plan_subset(s->plan_s);
+    } catch (...) {
+      err = std::current_exception();
+    }
+  });
+  try {
+    s->space->plan_density(s->plan_d, false);
+  } catch (...) {
+    t.join();
+    throw;
+  }
+  t.join();
+  if (err) std::rethrow_exception(err);
 }
 
 void upload_activity(sphgpu_space* s, cudaStream_t st);
@@ -685,9 +705,12 @@ int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
   return guard([&]() {
     if (s->dev) CK(cudaStreamSynchronize(s->stream));
     if (s->dev && s->h_stale) fetch_active_h(s, s->stream);
+    const auto t0 = std::chrono::steady_clock::now();
     s->prm.max_active_bin = max_active_bin;
     s->space->set_activity(max_active_bin);
     build_plans(s);
+    const auto t1 = std::chrono::steady_clock::now();
+    s->act_plan_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
     s->force_planned = false;
     s->task_d.clear();
     s->task_f.clear();
@@ -697,6 +720,8 @@ int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
       s->dplan_d.upload(s->plan_d, s->stream);
       s->dplan_s.upload(s->plan_s, s->stream);
       CK(cudaStreamSynchronize(s->stream));
+      s->act_upload_ms += std::chrono::duration<double, std::milli>(
+                              std::chrono::steady_clock::now() - t1).count();
     }
     return SPHGPU_OK;
   });
@@ -1053,6 +1078,15 @@ int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms
   const int rc = sphgpu_set_tuning(s, &bt);
   if (rc) return rc;
   *best = bt;
+  return SPHGPU_OK;
+}
+
+int sphgpu_host_times(sphgpu_space* s, double ms[3], int32_t reset) {
+  if (!s || !ms) return fail(SPHGPU_EINVAL, "null argument");
+  ms[0] = s->act_plan_ms;
+  ms[1] = s->act_upload_ms;
+  ms[2] = s->plan_ms;
+  if (reset) s->act_plan_ms = s->act_upload_ms = s->plan_ms = 0;
   return SPHGPU_OK;
 }
 

@@ -29,6 +29,43 @@
 
 namespace sphgpu {
 
+// Planning runs on the host cores: work items are handed out in blocks by an
+// atomic counter; each block keeps its own output, merged in block order so
+// that the plan is the same for any number of threads.
+namespace {
+int planner_threads() {
+  const unsigned t = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(t, 16u));
+}
+
+template <class F>
+void parallel_blocks(int nthreads, int nblocks, F&& body) {
+  const int nt = std::min(nthreads, nblocks);
+  if (nt <= 1) {
+    for (int b = 0; b < nblocks; b++) body(b);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::exception_ptr err;
+  std::mutex mu;
+  auto run = [&]() {
+    try {
+      for (int b = next++; b < nblocks; b = next++) body(b);
+    } catch (...) {
+      std::lock_guard<std::mutex> lock(mu);
+      if (!err) err = std::current_exception();
+      next = nblocks;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; t++) pool.emplace_back(run);
+  run();
+  for (auto& th : pool) th.join();
+  if (err) std::rethrow_exception(err);
+}
+}  // namespace
+
+
 static inline float fmaxr(float a, float b) { return a > b ? a : b; }
 static inline float fminr(float a, float b) { return a < b ? a : b; }
 
@@ -523,7 +560,11 @@ void Space::set_activity(int max_active_bin) {
       mark_leaf(k);
     }
   }
-  for (int c : dirty) redrift_leaf(c);
+  constexpr int kLeafBlock = 64;  // dirty leaves per work block
+  parallel_blocks(threads(), (int)((dirty.size() + kLeafBlock - 1) / kLeafBlock), [&](int blk) {
+    const size_t e = std::min(dirty.size(), (size_t)(blk + 1) * kLeafBlock);
+    for (size_t q = (size_t)blk * kLeafBlock; q < e; q++) redrift_leaf(dirty[q]);
+  });
   // ancestors, deepest first, each once
   std::vector<std::vector<int>> by_depth;
   std::vector<int> anc;
@@ -534,22 +575,28 @@ void Space::set_activity(int max_active_bin) {
       if ((int)by_depth.size() <= d) by_depth.resize(d + 1);
       by_depth[d].push_back(p);
     }
-  for (int d = (int)by_depth.size() - 1; d >= 0; d--)
-    anc.insert(anc.end(), by_depth[d].begin(), by_depth[d].end());
-  for (int c : anc) {
-    float h_max = 0.f, h_max_active = 0.f;
-    int any = 0;
-    for (int k = 0; k < 8; k++) {
-      const int p = cells_[c].progeny[k];
-      if (p < 0) continue;
-      h_max = fmaxr(h_max, cells_[p].h_max);
-      h_max_active = fmaxr(h_max_active, cells_[p].h_max_active);
-      any |= cells_[p].active;
-    }
-    cells_[c].h_max = h_max;
-    cells_[c].h_max_active = h_max_active;
-    cells_[c].active = any;
-    cells_[c].h_max_old = h_max;
+  for (int d = (int)by_depth.size() - 1; d >= 0; d--) {
+    const std::vector<int>& lev = by_depth[d];
+    parallel_blocks(threads(), (int)((lev.size() + kLeafBlock - 1) / kLeafBlock), [&](int blk) {
+      const size_t e = std::min(lev.size(), (size_t)(blk + 1) * kLeafBlock);
+      for (size_t q = (size_t)blk * kLeafBlock; q < e; q++) {
+        const int c = lev[q];
+        float h_max = 0.f, h_max_active = 0.f;
+        int any = 0;
+        for (int k = 0; k < 8; k++) {
+          const int p = cells_[c].progeny[k];
+          if (p < 0) continue;
+          h_max = fmaxr(h_max, cells_[p].h_max);
+          h_max_active = fmaxr(h_max_active, cells_[p].h_max_active);
+          any |= cells_[p].active;
+        }
+        cells_[c].h_max = h_max;
+        cells_[c].h_max_active = h_max_active;
+        cells_[c].active = any;
+        cells_[c].h_max_old = h_max;
+      }
+    });
+    anc.insert(anc.end(), lev.begin(), lev.end());
   }
   for (int c : dirty) cell_mark_[c] = 0;
   for (int c : anc) cell_mark_[c] = 0;
@@ -868,42 +915,6 @@ void Space::items_to_entry_list(const std::vector<Item>& items,
   }
 }
 
-// Planning runs on the host cores: work items are handed out in blocks by an
-// atomic counter; each block keeps its own output, merged in block order so
-// that the plan is the same for any number of threads.
-namespace {
-int planner_threads() {
-  const unsigned t = std::thread::hardware_concurrency();
-  return (int)std::max(1u, std::min(t, 16u));
-}
-
-template <class F>
-void parallel_blocks(int nthreads, int nblocks, F&& body) {
-  const int nt = std::min(nthreads, nblocks);
-  if (nt <= 1) {
-    for (int b = 0; b < nblocks; b++) body(b);
-    return;
-  }
-  std::atomic<int> next{0};
-  std::exception_ptr err;
-  std::mutex mu;
-  auto run = [&]() {
-    try {
-      for (int b = next++; b < nblocks; b = next++) body(b);
-    } catch (...) {
-      std::lock_guard<std::mutex> lock(mu);
-      if (!err) err = std::current_exception();
-      next = nblocks;
-    }
-  };
-  std::vector<std::thread> pool;
-  for (int t = 1; t < nt; t++) pool.emplace_back(run);
-  run();
-  for (auto& th : pool) th.join();
-  if (err) std::rethrow_exception(err);
-}
-}  // namespace
-
 int Space::threads() const { return threads_ > 0 ? threads_ : planner_threads(); }
 
 void Space::plan_density(Plan& plan, bool second) const {
@@ -964,40 +975,39 @@ void Space::plan_subset(Plan& plan) const {
   flatten(outs, plan);
 }
 
-// Plan arrays from (leaf, entry) lists in emission order: entries grouped
-// by leaf (stable), then every leaf's (j-block, entry) candidate pairs.
+// Plan arrays from (leaf, entry) lists in emission order: the entries stay
+// in that order; every leaf's (j-block, entry) candidate pairs are grouped by
+// leaf, in the order its entries were emitted.
 void Space::flatten(const std::vector<std::vector<std::pair<int, Entry>>>& outs,
                     Plan& plan) const {
   const size_t nl = leaves_.size();
-  auto& leb = plan.leaf_entry_begin;
-  leb.assign(nl + 1, 0);
-  for (const auto& o : outs)
-    for (const auto& le : o) leb[le.first + 1]++;
-  for (size_t l = 0; l < nl; l++) leb[l + 1] += leb[l];
-  plan.entries.resize(leb[nl]);
-  std::vector<int> pos(leb.begin(), leb.end() - 1);
-  for (const auto& o : outs)
-    for (const auto& le : o) plan.entries[pos[le.first]++] = le.second;
+  size_t ne = 0;
+  for (const auto& o : outs) ne += o.size();
+  plan.entries.resize(ne);
+  std::vector<int> leaf(ne);
   auto& lpb = plan.leaf_pair_begin;
   lpb.assign(nl + 1, 0);
-  for (size_t l = 0; l < nl; l++) {
-    int np = 0;
-    for (int e = leb[l]; e < leb[l + 1]; e++) np += plan.entries[e].bcount;
-    lpb[l + 1] = lpb[l] + np;
-  }
+  size_t e = 0;
+  for (const auto& o : outs)
+    for (const auto& le : o) {
+      plan.entries[e] = le.second;
+      leaf[e] = le.first;
+      lpb[le.first + 1] += le.second.bcount;
+      e++;
+    }
+  for (size_t l = 0; l < nl; l++) lpb[l + 1] += lpb[l];
   plan.pair_block.resize(lpb[nl]);
   plan.pair_entry.resize(lpb[nl]);
-  for (size_t l = 0; l < nl; l++) {
-    int w = lpb[l];
-    for (int e = leb[l]; e < leb[l + 1]; e++) {
-      const Entry& E = plan.entries[e];
-      for (int b = E.bfirst; b < E.bfirst + E.bcount; b++, w++) {
-        plan.pair_block[w] = b;
-        plan.pair_entry[w] = e;
-      }
+  std::vector<int> pos(lpb.begin(), lpb.end() - 1);
+  for (size_t k = 0; k < ne; k++) {
+    const Entry& E = plan.entries[k];
+    int w = pos[leaf[k]];
+    for (int b = E.bfirst; b < E.bfirst + E.bcount; b++, w++) {
+      plan.pair_block[w] = b;
+      plan.pair_entry[w] = (int)k;
     }
+    pos[leaf[k]] = w;
   }
-  plan.units.clear();
 }
 
 void Space::leaf_infos(std::vector<LeafInfo>& out) const {

@@ -44,11 +44,9 @@ struct Item {
 };
 
 struct Plan {
-  std::vector<Entry> entries;
-  std::vector<Unit> units;
-  std::vector<int> leaf_entry_begin;
+  std::vector<Entry> entries;  // in the order the recursions emit them
   // Flattened candidate list: every (j-block, entry) a leaf's particles may
-  // interact with, per leaf.
+  // interact with, grouped by leaf.
   std::vector<int32_t> pair_block, pair_entry;
   std::vector<int> leaf_pair_begin;
 };
@@ -81,7 +79,6 @@ class Space {
   const std::vector<int>& active_list() const { return active_list_; }
   // depth_h that cell_set_part_h_depth (cell.h:1787) gives h in this leaf.
   int8_t h_depth_of(float h, int leaf_cell) const;
-  void set_unit_chunk(int c) { unit_chunk_ = c; }
   // j-block depth (partner particles per culled block, <= 32)
   void set_jblock(int jb) {
     jblock_ = jb;
@@ -178,7 +175,6 @@ class Space {
   int n_ = 0;
   int cdim_[3] = {0, 0, 0};
   double width_[3] = {0, 0, 0};
-  int unit_chunk_ = 128;
   int jblock_ = SPH_JBLOCK;
   int threads_ = 0;
   std::vector<double> x_;

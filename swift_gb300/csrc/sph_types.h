@@ -64,15 +64,7 @@ static_assert(sizeof(Entry) == 80, "Entry layout");
 // j-block: up to kJBlock consecutive particles of one leaf (spatially
 // sorted), with their bounding box in the top-cell frame; the gather culls
 // whole blocks against each particle's search sphere.
-#define SPH_JBLOCK 32
-
-// Work unit: a chunk of a leaf's particles gathering over a list of entries.
-struct Unit {
-  int32_t i_first, i_count;   // particle range (chunk of one leaf)
-  int32_t e_begin, e_end;     // entry range
-  int32_t leaf;               // leaf index
-  int32_t pad;
-};
+#define SPH_JBLOCK 16  // default j-block depth (the autotuner tries 8, 16, 32)
 
 // Per-leaf geometry needed on the device by the ghost (cell_set_part_h_depth,
 // cell.h:1787): the (h_min_allowed, h_max_allowed, depth) chain from the

@@ -98,7 +98,7 @@ def test_server_matches_single_space_and_oracle(oracle_lib):
         srv.submit(7, box, nsteps=3)
         out = _run_until_done(srv, [7])[7]
     with api.Space(box) as sp:
-        sp.set_tuning(jtile=32, rerun_lists=0, block_warps=8)  # the arena's configuration
+        sp.set_tuning(jtile=16, rerun_lists=0, block_warps=8)  # the arena's configuration
         sp.step()
         one = sp.download()
     # the same lists and kernels as the single-box batched form

@@ -226,6 +226,8 @@ def traffic_from_profile(workload, tuning):
             text = f.read()
         if f"jtile {tuning.get('jtile')}" not in text:
             return None
+        if f"threads_per_particle {tuning.get('threads_per_particle', 1)}" not in text:
+            return None
         for line in text.splitlines():
             if line.startswith("traffic_bytes_per_launch:"):
                 return float(line.split(":")[1].strip().split()[0])
@@ -415,8 +417,8 @@ def run_ours(args):
     # plan (first step), autotune (tile shape x j-block depth), warm-up
     sp.step(stream=sh)
     if args.tuning:
-        jt, bw = (int(v) for v in args.tuning.split(","))
-        sp.set_tuning(jtile=jt, block_warps=bw)
+        jt, bw, *tp = (int(v) for v in args.tuning.split(","))
+        sp.set_tuning(tpp=tp[0] if tp else 1, jtile=jt, block_warps=bw)
         sp.step(stream=sh)
     if args.no_tune or args.tuning:
         tuning, tune_ms = (dict(zip(("threads_per_particle", "jtile", "rerun_lists",
@@ -566,7 +568,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default gather configuration")
     ap.add_argument("--tuning", default="",
-                    help="JTILE,BLOCK_WARPS: fixed gather configuration, no autotune")
+                    help="JTILE,BLOCK_WARPS[,TPP]: fixed gather configuration, no autotune")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -76,7 +76,10 @@ typedef struct {
 /* Launch configuration of the gather kernels (what the autotuner picks). */
 typedef struct {
   int32_t threads_per_particle; /* lanes per updated particle: 1 (one warp
-                                   serves a group of up to 32 particles) */
+                                   serves a group of up to 32 particles)
+                                   or 2 (a group of up to 16, the two
+                                   lanes split each j-block's candidates;
+                                   the list-recording re-run keeps 1) */
   int32_t jtile;                /* partner particles per culled j-block:
                                    8, 16 or 32 */
   int32_t rerun_lists;          /* 1: the ghost's first density re-run
@@ -141,11 +144,12 @@ int sphgpu_get_tuning(const sphgpu_space *s, sphgpu_tuning *t);
 
 /* Autotuner: times the batched step of this space (CUDA events, `reps`
  * steps per candidate after one warm-up) for every candidate configuration
- * (j-block depth x tile shape), keeps the fastest and returns it in *best;
- * ms[k] receives the mean step time of candidate k (up to 8 candidates,
- * order: jtile 32/16/8 x block_warps 8/4), *ncand their number. */
+ * (j-block depth x lanes per particle x tile shape), keeps the fastest and
+ * returns it in *best; ms[k] receives the mean step time of candidate k (up
+ * to 16 candidates, order: jtile 32/16/8 x threads_per_particle 1/2 x
+ * block_warps 8/4), *ncand their number. */
 int sphgpu_autotune(sphgpu_space *s, int32_t reps, sphgpu_tuning *best,
-                    float ms[8], int32_t *ncand);
+                    float ms[16], int32_t *ncand);
 
 /* Batched form: density -> ghost -> force over the whole box, one
  * persistent launch per loop, captured as one CUDA graph on the first call

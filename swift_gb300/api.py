@@ -152,6 +152,11 @@ def make_params(box, **kw):
     return p
 
 
+def tuning_key(jtile, tpp, block_warps):
+    """Name of an autotuner candidate."""
+    return f"jtile={jtile},tpp={tpp},block_warps={block_warps}"
+
+
 class Space:
     """A box of SPH particles with its cell tree, resident on the GPU once a
     GPU call is made.  Mirrors the reference's space + runner entry points."""
@@ -215,8 +220,8 @@ class Space:
         return geom, ints
 
     # -- configuration -----------------------------------------------------
-    def set_tuning(self, tpi=1, jtile=16, rerun_lists=1, block_warps=8):
-        t = Tuning(tpi, jtile, rerun_lists, block_warps)
+    def set_tuning(self, tpp=1, jtile=16, rerun_lists=1, block_warps=8):
+        t = Tuning(tpp, jtile, rerun_lists, block_warps)
         _check(lib().sphgpu_set_tuning(self._h, ctypes.byref(t)))
 
     def tuning(self):
@@ -245,13 +250,13 @@ class Space:
         """Pick the fastest gather configuration for this box (native
         autotuner); returns ({jtile, block_warps, ...}, {config: ms})."""
         best = Tuning()
-        ms = np.zeros(8, np.float32)
+        ms = np.zeros(16, np.float32)
         n = ctypes.c_int32()
         _check(lib().sphgpu_autotune(self._h, int(reps), ctypes.byref(best),
                                      _ptr(ms), ctypes.byref(n)))
-        cands = [(jt, bw) for jt in (32, 16, 8) for bw in (8, 4)]
-        table = {f"jtile={jt},block_warps={bw}": float(ms[k])
-                 for k, (jt, bw) in enumerate(cands[:n.value])}
+        cands = [(jt, tpp, bw) for jt in (32, 16, 8) for tpp in (1, 2) for bw in (8, 4)]
+        table = {tuning_key(jt, tpp, bw): float(ms[k])
+                 for k, (jt, tpp, bw) in enumerate(cands[:n.value])}
         return ({"threads_per_particle": best.threads_per_particle,
                  "jtile": best.jtile, "rerun_lists": best.rerun_lists,
                  "block_warps": best.block_warps}, table)

@@ -88,6 +88,9 @@ struct sphgpu_space {
   int max_units = 0;             // 32-particle windows of all leaves
   DBuf<int> leaf_window_begin;   // per leaf: its first window
   std::vector<int> lwb_host;
+  int max_units16 = 0;           // the same for 16-particle windows (two
+  DBuf<int> leaf_window_begin16; // lanes per particle)
+  std::vector<int> lwb16_host;
   std::vector<int> top_leaf;     // per top cell: first leaf (+1 sentinel)
   DBuf<int4> task_units_d, task_units_f;
   DBuf<Entry> task_entries_d, task_entries_f;
@@ -225,14 +228,18 @@ void ensure_device(sphgpu_space* s) {
   s->n_active = 0;
   for (int g = 0; g < n; g++) s->n_active += fl[g];
   // one work group per 32-particle window of every leaf at most
-  s->max_units = 0;
-  std::vector<int> lwb(lvs.size() + 1, 0);
+  s->max_units = s->max_units16 = 0;
+  std::vector<int> lwb(lvs.size() + 1, 0), lwb16(lvs.size() + 1, 0);
   for (size_t l = 0; l < lvs.size(); l++) {
     lwb[l] = s->max_units;
+    lwb16[l] = s->max_units16;
     s->max_units += (cells[lvs[l]].count + 31) / 32;
+    s->max_units16 += (cells[lvs[l]].count + 15) / 16;
   }
   lwb[lvs.size()] = s->max_units;
+  lwb16[lvs.size()] = s->max_units16;
   s->lwb_host = lwb;
+  s->lwb16_host = lwb16;
   s->top_leaf.assign(ntop + 1, (int)lvs.size());
   for (int l = (int)lvs.size() - 1; l >= 0; l--) s->top_leaf[cells[lvs[l]].top] = l;
   for (int t = ntop - 1; t >= 0; t--)
@@ -258,8 +265,9 @@ void ensure_device(sphgpu_space* s) {
   s->top_loc.upload(tl.data(), tl.size(), st);
   s->leaves.upload(li.data(), li.size(), st);
   upload_blocks(s, st);
-  s->units.alloc(std::max(1, s->max_units));
+  s->units.alloc(std::max(1, std::max(s->max_units, s->max_units16)));
   s->leaf_window_begin.upload(lwb.data(), lwb.size(), st);
+  s->leaf_window_begin16.upload(lwb16.data(), lwb16.size(), st);
   s->posh.alloc(n);
   s->dens0.alloc(n);
   s->dens1.alloc(n);
@@ -369,13 +377,17 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
                     bool lists = false) {
   const int nl = (int)s->space->leaves().size();
   if (leaf_end < 0) leaf_end = nl;
+  // two lanes per particle: 16-particle windows (a recording gather keeps one)
+  const int tpp = lists ? 1 : s->tune.threads_per_particle;
+  const DBuf<int>& lwb = tpp == 2 ? s->leaf_window_begin16 : s->leaf_window_begin;
+  const std::vector<int>& lwbh = tpp == 2 ? s->lwb16_host : s->lwb_host;
   CK(cudaMemsetAsync(s->queue.p + qslot, 0, sizeof(int), st));
-  CK(launch_build_units(s->leaves.p + leaf_begin, leaf_end - leaf_begin,
-                        s->leaf_window_begin.p + leaf_begin, s->flags.p, need, veto,
-                        dp.lpb.p + leaf_begin, s->units.p, gate, st));
+  CK(launch_build_units(s->leaves.p + leaf_begin, leaf_end - leaf_begin, lwb.p + leaf_begin,
+                        s->flags.p, need, veto, dp.lpb.p + leaf_begin, s->units.p, gate, st,
+                        32 / tpp));
   // the groups of this leaf range occupy [w0, w1) of the window slots
   G2Args a = gargs(s, dp, qslot, mode);
-  const int w0 = s->lwb_host[leaf_begin], w1 = s->lwb_host[leaf_end];
+  const int w0 = lwbh[leaf_begin], w1 = lwbh[leaf_end];
   a.units = s->units.p + w0;
   a.count = w1 - w0;
   a.count_ptr = nullptr;
@@ -386,7 +398,7 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
     a.nl_T = s->nl_T.p;
     a.nl_cap = kListCap;
   }
-  CK(launch_gather(a, force, s->num_sms, w1 - w0, st, s->tune.block_warps, lists));
+  CK(launch_gather(a, force, s->num_sms, w1 - w0, st, s->tune.block_warps, lists, tpp));
 }
 
 ListArgs largs(sphgpu_space* s, const int* gate) {
@@ -666,10 +678,11 @@ int sphgpu_space_leaves(const sphgpu_space* s, double* geom, int32_t* ints) {
 
 int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
   if (!s || !t) return fail(SPHGPU_EINVAL, "null argument");
-  if (t->threads_per_particle != 1 || !(t->jtile == 8 || t->jtile == 16 || t->jtile == 32) ||
+  if (!(t->threads_per_particle == 1 || t->threads_per_particle == 2) ||
+      !(t->jtile == 8 || t->jtile == 16 || t->jtile == 32) ||
       !(t->block_warps == 4 || t->block_warps == 8))
     return fail(SPHGPU_EINVAL,
-                "tuning: threads_per_particle 1, jtile 8, 16 or 32, block_warps 4 or 8");
+                "tuning: threads_per_particle 1 or 2, jtile 8, 16 or 32, block_warps 4 or 8");
   return guard([&]() {
     if (s->dev) CK(cudaStreamSynchronize(s->stream));
     const bool reblock = t->jtile != s->tune.jtile;
@@ -1045,7 +1058,7 @@ int sphgpu_cell_sort(sphgpu_space* s, int32_t cell, int32_t axis, float* d, int3
   });
 }
 
-int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms[8],
+int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms[16],
                     int32_t* ncand) {
   if (!s || !best || !ms || !ncand || reps < 1)
     return fail(SPHGPU_EINVAL, "sphgpu_autotune: null argument or reps < 1");
@@ -1053,9 +1066,10 @@ int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms
   float best_ms = 3.4e38f;
   sphgpu_tuning bt = s->tune;
   int k = 0;
+  // j-tile outermost: only a new j-tile re-plans the blocks
   for (int a = 0; a < 3; a++)
-    for (int b = 0; b < 2; b++, k++) {
-      sphgpu_tuning t{1, jt[a], s->tune.rerun_lists, bw[b]};
+    for (int c = 0; c < 4; c++, k++) {
+      sphgpu_tuning t{1 + (c >> 1), jt[a], s->tune.rerun_lists, bw[c & 1]};
       int rc = sphgpu_set_tuning(s, &t);
       if (rc) return rc;
       rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);  // plan + capture + warm

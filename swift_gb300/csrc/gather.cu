@@ -38,41 +38,49 @@ __global__ void block_hmax(const int2* __restrict__ fc, float4* __restrict__ lo,
   }
 }
 
-template <bool FORCE, int WPB, int MINB, bool LISTS = false>
+template <bool FORCE, int WPB, int MINB, bool LISTS = false, int TPP = 1>
 static cudaError_t launch_variant(const G2Args& a, int num_sms, int max_units,
                                   cudaStream_t s) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS>, WPB * 32, 0);
+      &per_sm, gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS, TPP>, WPB * 32, 0);
   int grid = std::max(1, per_sm) * num_sms;
   grid = std::max(1, std::min(grid, (max_units + WPB - 1) / WPB));
-  gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS><<<grid, WPB * 32, 0, s>>>(a);
+  gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS, TPP><<<grid, WPB * 32, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+template <int TPP>
+static cudaError_t launch_shape(const G2Args& a, bool force, int num_sms, int max_units,
+                                cudaStream_t s, int block_warps) {
+  if (block_warps == 4)
+    return force ? launch_variant<true, 4, 6, false, TPP>(a, num_sms, max_units, s)
+                 : launch_variant<false, 4, 6, false, TPP>(a, num_sms, max_units, s);
+  return force ? launch_variant<true, 8, 3, false, TPP>(a, num_sms, max_units, s)
+               : launch_variant<false, 8, 3, false, TPP>(a, num_sms, max_units, s);
 }
 
 // Tile shapes the autotuner chooses from: 8 warps x 3 blocks per SM (up to
 // 85 registers) or 4 warps x 6 blocks per SM (up to 85 registers, finer
-// blocks for the tail of the work queue).
+// blocks for the tail of the work queue); one or two lanes per particle (two:
+// the work groups are 16-particle windows).  Recording gathers use one lane.
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
-                          cudaStream_t s, int block_warps, bool lists) {
+                          cudaStream_t s, int block_warps, bool lists, int tpp) {
   if (lists && !force)
     return block_warps == 4 ? launch_variant<false, 4, 6, true>(a, num_sms, max_units, s)
                             : launch_variant<false, 8, 3, true>(a, num_sms, max_units, s);
-  if (block_warps == 4)
-    return force ? launch_variant<true, 4, 6>(a, num_sms, max_units, s)
-                 : launch_variant<false, 4, 6>(a, num_sms, max_units, s);
-  return force ? launch_variant<true, 8, 3>(a, num_sms, max_units, s)
-               : launch_variant<false, 8, 3>(a, num_sms, max_units, s);
+  return tpp == 2 ? launch_shape<2>(a, force, num_sms, max_units, s, block_warps)
+                  : launch_shape<1>(a, force, num_sms, max_units, s, block_warps);
 }
 
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                const int* leaf_window_begin, const uint8_t* flags,
                                int need, int veto, const int* leaf_pair_begin,
-                               int4* units, const int* gate, cudaStream_t s) {
+                               int4* units, const int* gate, cudaStream_t s, int win) {
   int g = (nleaves * 32 + 255) / 256;
   g = std::max(1, std::min(g, 152 * 16));
   build_units<<<g, 256, 0, s>>>(leaves, nleaves, leaf_window_begin, flags, need, veto,
-                                leaf_pair_begin, units, gate);
+                                leaf_pair_begin, units, gate, win);
   return cudaGetLastError();
 }
 

@@ -142,12 +142,18 @@ __device__ __forceinline__ float3 offset_of(int idx, float3 tw) {
 //      the last drain empties them.  Sums stay in the lane's registers.
 // LISTS (density re-runs): also record every candidate below the band's top
 // into the particle's neighbour list (G2Args::nl).
+// TPP (threads per particle, 1 or 2): a warp serves 32 / TPP particles of a
+// window; the TPP lanes of a particle split each staged block's candidates
+// and add their partial sums at the end.
 template <bool FORCE, int OUT = OUT_STORE, int WPB = WARPS_PER_BLOCK, int MINB = 3,
-          bool LISTS = false>
+          bool LISTS = false, int TPP = 1>
 __global__ void __launch_bounds__(WPB * 32, MINB)
 gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
+  static_assert(TPP == 1 || TPP == 2, "one or two lanes per particle");
+  static_assert(TPP == 1 || (!LISTS && OUT == OUT_STORE), "two lanes: stored sums, no lists");
   __shared__ LaneSmem smem[WPB];
   const int lane = threadIdx.x & 31;
+  const int sub = lane % TPP, pl = lane / TPP;  // lane within the particle, particle
   LaneSmem& ws = smem[threadIdx.x >> 5];
   const DevParticles& P = a.p;
   if (a.gate && *a.gate == 0) return;
@@ -166,8 +172,8 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
       const float4 t = a.leaf_tw[P.leaf_of[U.x]];
       tw = make_float3(t.x, t.y, t.z);
     }
-    const bool valid = (U.y >> lane) & 1;
-    const int i = U.x + lane;
+    const bool valid = (U.y >> pl) & 1;
+    const int i = U.x + pl;
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), vi = make_float4(0.f, 0.f, 0.f, 1.f);
     float4 fi = make_float4(1.f, 0.f, 0.f, 0.f);
     float bi = 0.f;
@@ -359,18 +365,17 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         __syncwarp();
         // the lane's own particle never pairs with itself
         const int tself = (i >= bfirst && i < bfirst + bcount) ? i - bfirst : -1;
-        const unsigned okmask =
-            mine ? (tself >= 0 ? ~(1u << tself) : 0xffffffffu) : 0u;
         const int pk = bfirst | (fidx << 27);
-        // Eight candidates at a time: FP32 r^2 below the band around H^2 sets
-        // a hit bit, inside the band a band bit; hits are pushed from the
-        // mask, band candidates are decided by the exact FP64 predicate in
-        // the reference frame (rare: the warp votes once per eight).
-        for (int t0 = 0; t0 < bcount; t0 += 8) {
+        // Eight candidates per lane at a time (candidate t0 + u * TPP + sub):
+        // FP32 r^2 below the band around H^2 sets a hit bit, inside the band
+        // a band bit; hits are pushed from the mask, band candidates are
+        // decided by the exact FP64 predicate in the reference frame (rare:
+        // the warp votes once per chunk).
+        for (int t0 = 0; t0 < bcount; t0 += 8 * TPP) {
           unsigned hm = 0u, bm = 0u;
 #pragma unroll
           for (int u = 0; u < 8; u++) {
-            const float4 q = ws.jpos[t0 + u];
+            const float4 q = ws.jpos[t0 + u * TPP + sub];
             const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
             float L2 = lo2, U2 = hi2;
@@ -384,8 +389,11 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
             else if (r2 < U2)
               bm |= 1u << u;
           }
-          const int left = bcount - t0;
-          const unsigned live = (left >= 8 ? 0xffu : ((1u << left) - 1u)) & (okmask >> t0);
+          const int left = (bcount - t0 - sub + TPP - 1) / TPP;  // my candidates here
+          unsigned live = left >= 8 ? 0xffu : (left > 0 ? (1u << left) - 1u : 0u);
+          const int ds = tself - t0 - sub;
+          if (tself >= 0 && ds >= 0 && ds % TPP == 0 && ds / TPP < 8) live &= ~(1u << (ds / TPP));
+          if (!mine) live = 0u;
           hm &= live;
           bm &= live;
           if (LISTS) {
@@ -394,7 +402,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
             while (lm) {
               const int u = __ffs(lm) - 1;
               lm &= lm - 1u;
-              ws.lb[lcnt & 7][lane] = pk + t0 + u;
+              ws.lb[lcnt & 7][lane] = pk + t0 + u * TPP + sub;
               lcnt++;
               if ((lcnt & 7) == 0 && lcnt <= a.nl_cap) {
                 int4* row = reinterpret_cast<int4*>(a.nl + (size_t)i * a.nl_cap + (lcnt - 8));
@@ -406,13 +414,13 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           while (hm) {
             const int u = __ffs(hm) - 1;
             hm &= hm - 1u;
-            push(pk + t0 + u);
+            push(pk + t0 + u * TPP + sub);
           }
           if (__any_sync(FULL, bm != 0u)) {
             while (bm) {
               const int u = __ffs(bm) - 1;
               bm &= bm - 1u;
-              const int t = t0 + u;
+              const int t = t0 + u * TPP + sub;
               const float H2 = FORCE ? fmaxf(hig2, ws.jpos[t].w) : hig2;
               if (exact_r2_2(P.xd, i, bfirst + t, E) < H2) push(pk + t);
             }
@@ -423,7 +431,18 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
       __syncwarp();
     }
     drain(true);
-    if (!valid) continue;
+    if (TPP == 2) {  // the particle's two lanes add their partial sums
+      s0 += __shfl_xor_sync(FULL, s0, 1);
+      s1 += __shfl_xor_sync(FULL, s1, 1);
+      s2 += __shfl_xor_sync(FULL, s2, 1);
+      s3 += __shfl_xor_sync(FULL, s3, 1);
+      s4 += __shfl_xor_sync(FULL, s4, 1);
+      s5 = FORCE ? fmaxf(s5, __shfl_xor_sync(FULL, s5, 1)) : s5 + __shfl_xor_sync(FULL, s5, 1);
+      s6 += __shfl_xor_sync(FULL, s6, 1);
+      s7 += __shfl_xor_sync(FULL, s7, 1);
+      ngb += __shfl_xor_sync(FULL, ngb, 1);
+    }
+    if (!valid || sub != 0) continue;
     if (LISTS) {
       if (lcnt <= a.nl_cap)
         for (int k = lcnt & ~7; k < lcnt; k++)
@@ -484,7 +503,7 @@ static __global__ void build_units(const LeafInfo* __restrict__ leaves, int nlea
                                    const int* __restrict__ leaf_window_begin,
                                    const uint8_t* __restrict__ flags, int need, int veto,
                                    const int* __restrict__ leaf_pair_begin,
-                                   int4* __restrict__ units, const int* gate) {
+                                   int4* __restrict__ units, const int* gate, int win = 32) {
   if (gate && *gate == 0) return;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -493,9 +512,10 @@ static __global__ void build_units(const LeafInfo* __restrict__ leaves, int nlea
     const int first = leaves[l].first, count = leaves[l].count;
     const int p0 = leaf_pair_begin[l], p1 = leaf_pair_begin[l + 1];
     int slot = leaf_window_begin[l];
-    for (int w0 = 0; w0 < count; w0 += 32, slot++) {
-      const int f = w0 + lane < count ? flags[first + w0 + lane] : 0;
-      const bool ok = w0 + lane < count && (f & need) == need && !(f & veto);
+    for (int w0 = 0; w0 < count; w0 += win, slot++) {
+      const bool in = lane < win && w0 + lane < count;
+      const int f = in ? flags[first + w0 + lane] : 0;
+      const bool ok = in && (f & need) == need && !(f & veto);
       const unsigned m = __ballot_sync(FULL, ok);
       if (lane == 0) units[slot] = make_int4(first + w0, p0 == p1 ? 0 : (int)m, p0, p1);
     }

@@ -100,15 +100,18 @@ struct GhostArgs {
   int* redo_count;              // [max_iter] particles sent to another round
 };
 
-// lists: record the re-run neighbour lists (density re-run mode, a.nl set)
+// lists: record the re-run neighbour lists (density re-run mode, a.nl set);
+// tpp: lanes per particle, 1 (32-particle work groups) or 2 (16-particle
+// groups; not with lists)
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
-                          cudaStream_t s, int block_warps = 8, bool lists = false);
-// Work groups of the particles whose flags hold every bit of `need` and no
-// bit of `veto`.
+                          cudaStream_t s, int block_warps = 8, bool lists = false,
+                          int tpp = 1);
+// Work groups (windows of `win` particles, 32 or 16) of the particles whose
+// flags hold every bit of `need` and no bit of `veto`.
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                const int* leaf_window_begin, const uint8_t* flags,
                                int need, int veto, const int* leaf_pair_begin,
-                               int4* units, const int* gate, cudaStream_t s);
+                               int4* units, const int* gate, cudaStream_t s, int win = 32);
 cudaError_t launch_redo_from_lists(const ListArgs& a, cudaStream_t s);
 int noalloc_max_particles();
 int noalloc_max_units();

@@ -101,13 +101,15 @@ def test_plain_equals_batched(case):
         assert scaled_err(b[k], a[k]).max() < 1e-3, (name, k)
 
 
-@pytest.mark.parametrize("jtile,block_warps", [(32, 4), (16, 8), (16, 4), (8, 8)])
-def test_every_tuning_keeps_parity(case, jtile, block_warps):
+@pytest.mark.parametrize("jtile,block_warps,tpp", [(32, 4, 1), (16, 8, 1), (16, 4, 1),
+                                                   (8, 8, 1), (32, 8, 2), (16, 8, 2),
+                                                   (8, 4, 2)])
+def test_every_tuning_keeps_parity(case, jtile, block_warps, tpp):
     """Each configuration the autotuner may pick holds the exact-count bar."""
     name, box, ref = case
     with api.Space(box) as sp:
-        sp.set_tuning(jtile=jtile, block_warps=block_warps)
-        assert sp.tuning()[1:] == (jtile, 1, block_warps)  # re-run lists on
+        sp.set_tuning(tpp=tpp, jtile=jtile, block_warps=block_warps)
+        assert sp.tuning() == (tpp, jtile, 1, block_warps)  # re-run lists on
         sp.step(api.STAGE_DENSITY)
         first = sp.download()
         sp.step(api.STAGE_ALL)
@@ -148,8 +150,9 @@ def test_autotune_picks_a_candidate():
     with api.Space(box) as sp:
         sp.step()
         best, table = sp.autotune(reps=1)
-        assert len(table) == 6 and all(v > 0 for v in table.values())
-        key = f"jtile={best['jtile']},block_warps={best['block_warps']}"
+        assert len(table) == 12 and all(v > 0 for v in table.values())
+        key = api.tuning_key(best["jtile"], best["threads_per_particle"],
+                             best["block_warps"])
         assert table[key] == min(table.values())
         assert sp.tuning()[1] == best["jtile"]
         sp.step()

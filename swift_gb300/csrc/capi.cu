@@ -88,9 +88,11 @@ struct sphgpu_space {
   int max_units = 0;             // 32-particle windows of all leaves
   DBuf<int> leaf_window_begin;   // per leaf: its first window
   std::vector<int> lwb_host;
-  int max_units16 = 0;           // the same for 16-particle windows (two
-  DBuf<int> leaf_window_begin16; // lanes per particle)
-  std::vector<int> lwb16_host;
+  // the same for 16- and 8-particle windows (two and four lanes per
+  // particle), index tpp / 2 - 0 or 1
+  int max_units_n[2] = {0, 0};
+  DBuf<int> leaf_window_begin_n[2];
+  std::vector<int> lwb_host_n[2];
   std::vector<int> top_leaf;     // per top cell: first leaf (+1 sentinel)
   DBuf<int4> task_units_d, task_units_f;
   DBuf<Entry> task_entries_d, task_entries_f;
@@ -228,18 +230,24 @@ void ensure_device(sphgpu_space* s) {
   s->n_active = 0;
   for (int g = 0; g < n; g++) s->n_active += fl[g];
   // one work group per 32-particle window of every leaf at most
-  s->max_units = s->max_units16 = 0;
-  std::vector<int> lwb(lvs.size() + 1, 0), lwb16(lvs.size() + 1, 0);
+  s->max_units = s->max_units_n[0] = s->max_units_n[1] = 0;
+  std::vector<int> lwb(lvs.size() + 1, 0), lwbn[2];
+  lwbn[0].assign(lvs.size() + 1, 0);
+  lwbn[1].assign(lvs.size() + 1, 0);
   for (size_t l = 0; l < lvs.size(); l++) {
     lwb[l] = s->max_units;
-    lwb16[l] = s->max_units16;
     s->max_units += (cells[lvs[l]].count + 31) / 32;
-    s->max_units16 += (cells[lvs[l]].count + 15) / 16;
+    for (int w = 0; w < 2; w++) {
+      lwbn[w][l] = s->max_units_n[w];
+      s->max_units_n[w] += (cells[lvs[l]].count + (15 >> w)) / (16 >> w);
+    }
   }
   lwb[lvs.size()] = s->max_units;
-  lwb16[lvs.size()] = s->max_units16;
   s->lwb_host = lwb;
-  s->lwb16_host = lwb16;
+  for (int w = 0; w < 2; w++) {
+    lwbn[w][lvs.size()] = s->max_units_n[w];
+    s->lwb_host_n[w] = lwbn[w];
+  }
   s->top_leaf.assign(ntop + 1, (int)lvs.size());
   for (int l = (int)lvs.size() - 1; l >= 0; l--) s->top_leaf[cells[lvs[l]].top] = l;
   for (int t = ntop - 1; t >= 0; t--)
@@ -265,9 +273,10 @@ void ensure_device(sphgpu_space* s) {
   s->top_loc.upload(tl.data(), tl.size(), st);
   s->leaves.upload(li.data(), li.size(), st);
   upload_blocks(s, st);
-  s->units.alloc(std::max(1, std::max(s->max_units, s->max_units16)));
+  s->units.alloc(std::max(1, std::max(s->max_units, s->max_units_n[1])));
   s->leaf_window_begin.upload(lwb.data(), lwb.size(), st);
-  s->leaf_window_begin16.upload(lwb16.data(), lwb16.size(), st);
+  for (int w = 0; w < 2; w++)
+    s->leaf_window_begin_n[w].upload(lwbn[w].data(), lwbn[w].size(), st);
   s->posh.alloc(n);
   s->dens0.alloc(n);
   s->dens1.alloc(n);
@@ -367,6 +376,10 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   return a;
 }
 
+// Lanes per particle of the gather that records the re-run lists (one row
+// segment per lane).
+int rec_tpp(const sphgpu_space* s) { return std::min(2, s->tune.threads_per_particle); }
+
 // Build the work groups of a loop (windows whose particles carry `need`
 // in their flags) and run the gather over them.
 // veto: skip particles with any of these flag bits; lists: record the re-run
@@ -377,10 +390,10 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
                     bool lists = false) {
   const int nl = (int)s->space->leaves().size();
   if (leaf_end < 0) leaf_end = nl;
-  // two lanes per particle: 16-particle windows (a recording gather keeps one)
-  const int tpp = lists ? 1 : s->tune.threads_per_particle;
-  const DBuf<int>& lwb = tpp == 2 ? s->leaf_window_begin16 : s->leaf_window_begin;
-  const std::vector<int>& lwbh = tpp == 2 ? s->lwb16_host : s->lwb_host;
+  // two or four lanes per particle: 16- or 8-particle windows
+  const int tpp = lists ? rec_tpp(s) : s->tune.threads_per_particle;
+  const DBuf<int>& lwb = tpp == 1 ? s->leaf_window_begin : s->leaf_window_begin_n[tpp / 4];
+  const std::vector<int>& lwbh = tpp == 1 ? s->lwb_host : s->lwb_host_n[tpp / 4];
   CK(cudaMemsetAsync(s->queue.p + qslot, 0, sizeof(int), st));
   CK(launch_build_units(s->leaves.p + leaf_begin, leaf_end - leaf_begin, lwb.p + leaf_begin,
                         s->flags.p, need, veto, dp.lpb.p + leaf_begin, s->units.p, gate, st,
@@ -408,6 +421,7 @@ ListArgs largs(sphgpu_space* s, const int* gate) {
   l.nl_cnt = s->nl_cnt.p;
   l.nl_T = s->nl_T.p;
   l.nl_cap = kListCap;
+  l.nl_seg = rec_tpp(s);
   l.leaf_pair_begin = s->dplan_s.lpb.p;
   l.pair_block = s->dplan_s.pb.p;
   l.pair_entry = s->dplan_s.pe.p;
@@ -678,11 +692,12 @@ int sphgpu_space_leaves(const sphgpu_space* s, double* geom, int32_t* ints) {
 
 int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
   if (!s || !t) return fail(SPHGPU_EINVAL, "null argument");
-  if (!(t->threads_per_particle == 1 || t->threads_per_particle == 2) ||
+  if (!(t->threads_per_particle == 1 || t->threads_per_particle == 2 ||
+        t->threads_per_particle == 4) ||
       !(t->jtile == 8 || t->jtile == 16 || t->jtile == 32) ||
       !(t->block_warps == 4 || t->block_warps == 8))
     return fail(SPHGPU_EINVAL,
-                "tuning: threads_per_particle 1 or 2, jtile 8, 16 or 32, block_warps 4 or 8");
+                "tuning: threads_per_particle 1, 2 or 4, jtile 8, 16 or 32, block_warps 4 or 8");
   return guard([&]() {
     if (s->dev) CK(cudaStreamSynchronize(s->stream));
     const bool reblock = t->jtile != s->tune.jtile;

@@ -62,13 +62,19 @@ static cudaError_t launch_shape(const G2Args& a, bool force, int num_sms, int ma
 
 // Tile shapes the autotuner chooses from: 8 warps x 3 blocks per SM (up to
 // 85 registers) or 4 warps x 6 blocks per SM (up to 85 registers, finer
-// blocks for the tail of the work queue); one or two lanes per particle (two:
-// the work groups are 16-particle windows).  Recording gathers use one lane.
+// blocks for the tail of the work queue); one, two or four lanes per particle
+// (work groups of 32-, 16- or 8-particle windows).  Recording gathers use one
+// or two lanes.
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
                           cudaStream_t s, int block_warps, bool lists, int tpp) {
-  if (lists && !force)
+  if (lists && !force) {
+    if (tpp == 2)
+      return block_warps == 4 ? launch_variant<false, 4, 6, true, 2>(a, num_sms, max_units, s)
+                              : launch_variant<false, 8, 3, true, 2>(a, num_sms, max_units, s);
     return block_warps == 4 ? launch_variant<false, 4, 6, true>(a, num_sms, max_units, s)
                             : launch_variant<false, 8, 3, true>(a, num_sms, max_units, s);
+  }
+  if (tpp == 4) return launch_shape<4>(a, force, num_sms, max_units, s, block_warps);
   return tpp == 2 ? launch_shape<2>(a, force, num_sms, max_units, s, block_warps)
                   : launch_shape<1>(a, force, num_sms, max_units, s, block_warps);
 }
@@ -85,9 +91,9 @@ cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
 }
 
 cudaError_t launch_redo_from_lists(const ListArgs& a, cudaStream_t s) {
-  int g = (a.p.n + 255) / 256;
-  g = std::max(1, std::min(g, 152 * 16));
-  redo_from_lists<<<g, 256, 0, s>>>(a);
+  long long g = ((long long)a.p.n * 8 + 255) / 256;  // eight lanes per particle
+  g = std::max(1LL, std::min(g, 152LL * 16));
+  redo_from_lists<<<(int)g, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

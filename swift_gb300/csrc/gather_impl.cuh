@@ -107,10 +107,13 @@ static __device__ __forceinline__ void density_hit(float dx, float dy, float dz,
 // pending hits (partner index and frame-offset index packed in 32 bits).
 #define QCAP 32  // power of two: ring positions wrap with & (QCAP - 1)
 struct LaneSmem {
-  float4 jpos[32];     // staged block: offset xyz in the group's frame, (K h)^2
+  float4 jp[32];       // staged block, candidates in pairs (2p, 2p+1):
+                       // jp[2p] = -(x, x', y, y'), jp[2p+1] = (-z, -z', (K h)^2,
+                       // (K h')^2), positions offset into the group's frame
   int sfirst[32];      // surviving candidate blocks of the current chunk
   int scount[32];
   int se[32];
+  int sdep[32];        // their entries' depth window: min | max << 8
   float4 sf[32];       // their frame offsets (w: frame-offset index)
   float4 slo[32];      // their boxes
   float4 shi[32];
@@ -149,8 +152,9 @@ template <bool FORCE, int OUT = OUT_STORE, int WPB = WARPS_PER_BLOCK, int MINB =
           bool LISTS = false, int TPP = 1>
 __global__ void __launch_bounds__(WPB * 32, MINB)
 gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
-  static_assert(TPP == 1 || TPP == 2, "one or two lanes per particle");
-  static_assert(TPP == 1 || (!LISTS && OUT == OUT_STORE), "two lanes: stored sums, no lists");
+  static_assert(TPP == 1 || TPP == 2 || TPP == 4, "one, two or four lanes per particle");
+  static_assert(TPP == 1 || (OUT == OUT_STORE && (!LISTS || TPP == 2)),
+                "several lanes: stored sums; lists with one or two lanes");
   __shared__ LaneSmem smem[WPB];
   const int lane = threadIdx.x & 31;
   const int sub = lane % TPP, pl = lane / TPP;  // lane within the particle, particle
@@ -193,6 +197,10 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     const float hid_inv = (hi_inv * hi_inv) * (hi_inv * hi_inv);
     const float mi_inv = 1.f / vi.w;
     const float lo2 = hig2 * (1.f - band), hi2 = hig2 * (1.f + band);
+    const float2 pix2 = make_float2(pi.x, pi.x), piy2 = make_float2(pi.y, pi.y),
+                 piz2 = make_float2(pi.z, pi.z);
+    const float2 lo22 = make_float2(lo2, lo2), hi22 = make_float2(hi2, hi2);
+    const float2 omb2 = make_float2(1.f - band, 1.f - band), opb2 = make_float2(1.f + band, 1.f + band);
     // Recording re-run: the list keeps every candidate below the band's top,
     // which covers any later re-run whose h is not larger (Newton's iterates
     // on the increasing, convex n(h) - eta^3 fall towards the root after the
@@ -204,8 +212,11 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     float gx1 = valid ? pi.x : -3.4e38f, gy1 = valid ? pi.y : -3.4e38f,
           gz1 = valid ? pi.z : -3.4e38f;
     float gh2 = hig2;
+    int gd0 = valid ? dh : 1 << 20, gd1 = valid ? dh : -(1 << 20);  // depth range
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
+      gd0 = min(gd0, __shfl_xor_sync(FULL, gd0, off));
+      gd1 = max(gd1, __shfl_xor_sync(FULL, gd1, off));
       gx0 = fminf(gx0, __shfl_xor_sync(FULL, gx0, off));
       gy0 = fminf(gy0, __shfl_xor_sync(FULL, gy0, off));
       gz0 = fminf(gz0, __shfl_xor_sync(FULL, gz0, off));
@@ -302,18 +313,22 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
       int e = 0;
       float4 fd = make_float4(0.f, 0.f, 0.f, 0.f), lo = fd, hb = fd;
       int2 fc = make_int2(0, 0);
+      int dep = 0;
       if (p < U.w) {
         const int b = a.pair_block[p];
         e = a.pair_entry[p];
         const Entry* E = &a.entries[e];
         fd = make_float4(E->fdx, E->fdy, E->fdz, 0.f);
+        dep = (int)(uint8_t)E->min_depth | (int)(uint8_t)E->max_depth << 8;
         lo = a.bb_lo[b];
         hb = a.bb_hi[b];
         const float dx = fmaxf(fmaxf(lo.x + fd.x - gx1, gx0 - hb.x - fd.x), 0.f);
         const float dy = fmaxf(fmaxf(lo.y + fd.y - gy1, gy0 - hb.y - fd.y), 0.f);
         const float dz = fmaxf(fmaxf(lo.z + fd.z - gz1, gz0 - hb.z - fd.z), 0.f);
         const float R2 = FORCE ? fmaxf(gh2, lo.w) : gh2;
-        ov = dx * dx + dy * dy + dz * dz < R2 * (1.f + 4.f * band) + 1e-30f;
+        // the box reaches the group and some lane's depth may use the entry
+        ov = dx * dx + dy * dy + dz * dz < R2 * (1.f + 4.f * band) + 1e-30f &&
+             gd1 >= E->min_depth && gd0 <= E->max_depth;
         if (ov) {
           fc = a.bb_fc[b];
           // frame-offset index of the partner top cell (for the queues)
@@ -328,21 +343,28 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         ws.sfirst[slot] = fc.x;
         ws.scount[slot] = fc.y;
         ws.se[slot] = e;
+        ws.sdep[slot] = dep;
         ws.sf[slot] = fd;
         ws.slo[slot] = lo;
         ws.shi[slot] = hb;
       }
       __syncwarp();
       const int nsurv = __popc(mask);
+      // positions of the next surviving block, loaded one block ahead
+      float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (nsurv > 0 && lane < ws.scount[0]) qn = P.posh[ws.sfirst[0] + lane];
       for (int k = 0; k < nsurv; k++) {
+        const float4 q = qn;
+        if (k + 1 < nsurv && lane < ws.scount[k + 1]) qn = P.posh[ws.sfirst[k + 1] + lane];
         const float4 sfd = ws.sf[k];
         const float4 slo = ws.slo[k], shi = ws.shi[k];
         const int eidx = ws.se[k];
         const Entry* E = &a.entries[eidx];
+        const int sdep = ws.sdep[k];
         // does this lane's own sphere reach the block, and may it use the
         // entry (depth filter)?
         bool mine = false;
-        if (valid && dh >= E->min_depth && dh <= E->max_depth) {
+        if (valid && dh >= (sdep & 0xff) && dh <= (sdep >> 8)) {
           const float px = pi.x - sfd.x, py = pi.y - sfd.y, pz = pi.z - sfd.z;
           const float dx = fmaxf(fmaxf(slo.x - px, px - shi.x), 0.f);
           const float dy = fmaxf(fmaxf(slo.y - py, py - shi.y), 0.f);
@@ -355,44 +377,55 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         const int fidx = __float_as_int(sfd.w);
         __syncwarp();
         if (lane < bcount) {
-          float4 q = P.posh[bfirst + lane];
-          q.x += sfd.x;
-          q.y += sfd.y;
-          q.z += sfd.z;
-          q.w = FORCE ? h2_exact(q.w) : 0.f;
-          ws.jpos[lane] = q;
+          float* f = reinterpret_cast<float*>(ws.jp) + (lane >> 1) * 8 + (lane & 1);
+          f[0] = -(q.x + sfd.x);
+          f[2] = -(q.y + sfd.y);
+          f[4] = -(q.z + sfd.z);
+          f[6] = FORCE ? h2_exact(q.w) : 0.f;
         }
         __syncwarp();
         // the lane's own particle never pairs with itself
         const int tself = (i >= bfirst && i < bfirst + bcount) ? i - bfirst : -1;
         const int pk = bfirst | (fidx << 27);
-        // Eight candidates per lane at a time (candidate t0 + u * TPP + sub):
-        // FP32 r^2 below the band around H^2 sets a hit bit, inside the band
-        // a band bit; hits are pushed from the mask, band candidates are
-        // decided by the exact FP64 predicate in the reference frame (rare:
-        // the warp votes once per chunk).
+        // Eight candidates per lane at a time, as four pairs: bit u is
+        // candidate t0 + 2 TPP (u / 2) + 2 sub + u % 2, and a pair's distances
+        // are evaluated with packed FP32 operations (the same IEEE roundings
+        // as scalar ones).  FP32 r^2 below the band around H^2 sets a hit bit,
+        // inside the band a band bit; hits are pushed from the mask, band
+        // candidates are decided by the exact FP64 predicate in the reference
+        // frame (rare: the warp votes once per chunk).
+        auto cidx = [&](int t0, int u) { return t0 + 2 * TPP * (u >> 1) + 2 * sub + (u & 1); };
         for (int t0 = 0; t0 < bcount; t0 += 8 * TPP) {
-          unsigned hm = 0u, bm = 0u;
+          unsigned hm = 0u, cm = 0u;
 #pragma unroll
-          for (int u = 0; u < 8; u++) {
-            const float4 q = ws.jpos[t0 + u * TPP + sub];
-            const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            float L2 = lo2, U2 = hi2;
+          for (int v = 0; v < 4; v++) {
+            const int pp = (t0 >> 1) + v * TPP + sub;
+            const float4 qa = ws.jp[2 * pp], qb = ws.jp[2 * pp + 1];
+            const float2 dx = __fadd2_rn(pix2, make_float2(qa.x, qa.y));
+            const float2 dy = __fadd2_rn(piy2, make_float2(qa.z, qa.w));
+            const float2 dz = __fadd2_rn(piz2, make_float2(qb.x, qb.y));
+            float2 r2 = __fmul2_rn(dx, dx);
+            r2 = __ffma2_rn(dy, dy, r2);
+            r2 = __ffma2_rn(dz, dz, r2);
+            float2 L2 = lo22, U2 = hi22;
             if (FORCE) {
-              const float H2 = fmaxf(hig2, q.w);
-              L2 = H2 * (1.f - band);
-              U2 = H2 * (1.f + band);
+              const float2 H2 = make_float2(fmaxf(hig2, qb.z), fmaxf(hig2, qb.w));
+              L2 = __fmul2_rn(H2, omb2);
+              U2 = __fmul2_rn(H2, opb2);
             }
-            if (r2 < L2)
-              hm |= 1u << u;
-            else if (r2 < U2)
-              bm |= 1u << u;
+            if (r2.x < L2.x) hm |= 1u << (2 * v);
+            if (r2.y < L2.y) hm |= 2u << (2 * v);
+            if (r2.x < U2.x) cm |= 1u << (2 * v);
+            if (r2.y < U2.y) cm |= 2u << (2 * v);
           }
-          const int left = (bcount - t0 - sub + TPP - 1) / TPP;  // my candidates here
-          unsigned live = left >= 8 ? 0xffu : (left > 0 ? (1u << left) - 1u : 0u);
-          const int ds = tself - t0 - sub;
-          if (tself >= 0 && ds >= 0 && ds % TPP == 0 && ds / TPP < 8) live &= ~(1u << (ds / TPP));
+          unsigned bm = cm & ~hm;
+          // this lane's candidates in the block come first in bit order
+          const int L = bcount - t0 - 2 * sub;
+          const int nl = L <= 0 ? 0 : min(8, 2 * (L / (2 * TPP)) + min(L % (2 * TPP), 2));
+          unsigned live = (1u << nl) - 1u;
+          const int ds = tself - t0 - 2 * sub;
+          if (tself >= 0 && ds >= 0 && ds % (2 * TPP) < 2 && ds / (2 * TPP) < 4)
+            live &= ~(1u << (2 * (ds / (2 * TPP)) + ds % (2 * TPP)));
           if (!mine) live = 0u;
           hm &= live;
           bm &= live;
@@ -402,10 +435,11 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
             while (lm) {
               const int u = __ffs(lm) - 1;
               lm &= lm - 1u;
-              ws.lb[lcnt & 7][lane] = pk + t0 + u * TPP + sub;
+              ws.lb[lcnt & 7][lane] = pk + cidx(t0, u);
               lcnt++;
-              if ((lcnt & 7) == 0 && lcnt <= a.nl_cap) {
-                int4* row = reinterpret_cast<int4*>(a.nl + (size_t)i * a.nl_cap + (lcnt - 8));
+              if ((lcnt & 7) == 0 && lcnt <= a.nl_cap / TPP) {
+                int4* row = reinterpret_cast<int4*>(a.nl + (size_t)i * a.nl_cap +
+                                                    sub * (a.nl_cap / TPP) + (lcnt - 8));
                 row[0] = make_int4(ws.lb[0][lane], ws.lb[1][lane], ws.lb[2][lane], ws.lb[3][lane]);
                 row[1] = make_int4(ws.lb[4][lane], ws.lb[5][lane], ws.lb[6][lane], ws.lb[7][lane]);
               }
@@ -414,14 +448,16 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           while (hm) {
             const int u = __ffs(hm) - 1;
             hm &= hm - 1u;
-            push(pk + t0 + u * TPP + sub);
+            push(pk + cidx(t0, u));
           }
           if (__any_sync(FULL, bm != 0u)) {
             while (bm) {
               const int u = __ffs(bm) - 1;
               bm &= bm - 1u;
-              const int t = t0 + u * TPP + sub;
-              const float H2 = FORCE ? fmaxf(hig2, ws.jpos[t].w) : hig2;
+              const int t = cidx(t0, u);
+              const float H2 =
+                  FORCE ? fmaxf(hig2, reinterpret_cast<const float*>(ws.jp)[(t >> 1) * 8 + 6 + (t & 1)])
+                        : hig2;
               if (exact_r2_2(P.xd, i, bfirst + t, E) < H2) push(pk + t);
             }
           }
@@ -431,23 +467,29 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
       __syncwarp();
     }
     drain(true);
-    if (TPP == 2) {  // the particle's two lanes add their partial sums
-      s0 += __shfl_xor_sync(FULL, s0, 1);
-      s1 += __shfl_xor_sync(FULL, s1, 1);
-      s2 += __shfl_xor_sync(FULL, s2, 1);
-      s3 += __shfl_xor_sync(FULL, s3, 1);
-      s4 += __shfl_xor_sync(FULL, s4, 1);
-      s5 = FORCE ? fmaxf(s5, __shfl_xor_sync(FULL, s5, 1)) : s5 + __shfl_xor_sync(FULL, s5, 1);
-      s6 += __shfl_xor_sync(FULL, s6, 1);
-      s7 += __shfl_xor_sync(FULL, s7, 1);
-      ngb += __shfl_xor_sync(FULL, ngb, 1);
+    // the particle's lanes add their partial sums
+#pragma unroll
+    for (int o = 1; o < TPP; o <<= 1) {
+      s0 += __shfl_xor_sync(FULL, s0, o);
+      s1 += __shfl_xor_sync(FULL, s1, o);
+      s2 += __shfl_xor_sync(FULL, s2, o);
+      s3 += __shfl_xor_sync(FULL, s3, o);
+      s4 += __shfl_xor_sync(FULL, s4, o);
+      s5 = FORCE ? fmaxf(s5, __shfl_xor_sync(FULL, s5, o)) : s5 + __shfl_xor_sync(FULL, s5, o);
+      s6 += __shfl_xor_sync(FULL, s6, o);
+      s7 += __shfl_xor_sync(FULL, s7, o);
+      ngb += __shfl_xor_sync(FULL, ngb, o);
     }
+    // lists: each lane of a particle fills its own segment of the row
+    // (nl_cap / TPP items); the count word holds both segments' counts
+    const int segcap = LISTS ? a.nl_cap / TPP : 0;
+    if (LISTS && valid && lcnt <= segcap)
+      for (int k = lcnt & ~7; k < lcnt; k++)
+        a.nl[(size_t)i * a.nl_cap + sub * segcap + k] = ws.lb[k & 7][lane];
+    const int lc1 = TPP == 2 ? __shfl_xor_sync(FULL, lcnt, 1) : 0;
     if (!valid || sub != 0) continue;
     if (LISTS) {
-      if (lcnt <= a.nl_cap)
-        for (int k = lcnt & ~7; k < lcnt; k++)
-          a.nl[(size_t)i * a.nl_cap + k] = ws.lb[k & 7][lane];
-      a.nl_cnt[i] = lcnt <= a.nl_cap ? lcnt : -1;
+      a.nl_cnt[i] = lcnt <= segcap && lc1 <= segcap ? (lcnt | lc1 << 16) : -1;
       a.nl_T[i] = hi2;
     }
     if (OUT == OUT_CALLER) {
@@ -533,57 +575,101 @@ static __device__ const Entry* rerun_entry(const ListArgs& a, int leaf, int b, i
   return nullptr;
 }
 
-static __global__ void redo_from_lists(ListArgs a) {
+// Eight lanes per particle: lane k of a particle takes items k, k + 8, ...
+// of its list (a particle's row is read 32 bytes at a time), and the lanes
+// add their partial sums at the end (fixed order: deterministic).
+static __global__ void __launch_bounds__(256, 3) redo_from_lists(ListArgs a) {
+  constexpr int LPP = 8;  // lanes per particle
   if (a.gate && *a.gate == 0) return;
   const DevParticles& P = a.p;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n;
-       i += gridDim.x * blockDim.x) {
-    const uint8_t fl = P.flags[i];
-    if ((fl & 3) != 3) continue;  // active and re-run this round
-    const float4 pi = P.posh[i];
-    const float hig2 = h2_exact(pi.w);
-    const float L2 = hig2 * (1.f - a.band), U2 = hig2 * (1.f + a.band);
-    const int cnt = a.nl_cnt[i];
-    if (cnt < 0 || !(U2 <= a.nl_T[i])) {  // the list does not cover h: gather
-      P.flags[i] = fl & ~8;
-      continue;
-    }
-    P.flags[i] = fl | 8;
-    const float4 vi = P.velm[i];
-    const float hi_inv = 1.f / pi.w;
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f, s5 = 0.f, s6 = 0.f, s7 = 0.f;
-    int ngb = 0;
-    const int4* row = reinterpret_cast<const int4*>(a.nl + (size_t)i * a.nl_cap);
-    for (int t0 = 0; t0 < cnt; t0 += 8) {
-      // eight items and their partners' positions in flight at once
-      const int4 p0 = row[t0 / 4], p1 = row[t0 / 4 + 1];
-      const int pk[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
-      float4 q[8];
-#pragma unroll
-      for (int u = 0; u < 8; u++)
-        q[u] = t0 + u < cnt ? P.posh[pk[u] & 0x07ffffff] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        if (t0 + u >= cnt) break;
-        const int j = pk[u] & 0x07ffffff;
-        const float3 fd = offset_of((int)((unsigned)pk[u] >> 27), a.top_width);
-        const float dx = pi.x - (q[u].x + fd.x), dy = pi.y - (q[u].y + fd.y),
-                    dz = pi.z - (q[u].z + fd.z);
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        bool hit = r2 < L2;
-        if (!hit && r2 < U2) {
-          const Entry* E = rerun_entry(a, P.leaf_of[i], a.blk_of[j], P.depth_h[i]);
-          hit = E != nullptr && exact_r2_2(P.xd, i, j, E) < hig2;
+  const int sub = threadIdx.x % LPP;
+  const int stride = gridDim.x * blockDim.x / LPP;
+  // the warp's four particles advance together (the shuffles below need
+  // every lane)
+  for (int base = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / LPP; base < P.n;
+       base += stride) {
+    const int i = base + (threadIdx.x & 31) / LPP;
+    bool work = false;
+    float4 pi = make_float4(0.f, 0.f, 0.f, 1.f);
+    float L2 = 0.f, U2 = 0.f, hig2 = 0.f;
+    int cnt = 0, c0 = 0;
+    if (i < P.n) {
+      const uint8_t fl = P.flags[i];
+      if ((fl & 3) == 3) {  // active and re-run this round
+        pi = P.posh[i];
+        hig2 = h2_exact(pi.w);
+        L2 = hig2 * (1.f - a.band);
+        U2 = hig2 * (1.f + a.band);
+        cnt = a.nl_cnt[i];
+        work = cnt >= 0 && U2 <= a.nl_T[i];  // else the list does not cover h: gather
+        if (work) {  // segment 0 holds c0 items, segment 1 (at nl_cap / 2) the rest
+          c0 = a.nl_seg == 2 ? (cnt & 0xffff) : cnt;
+          cnt = c0 + (a.nl_seg == 2 ? cnt >> 16 : 0);
         }
-        if (!hit) continue;
-        density_hit(dx, dy, dz, r2, vi, P.velm[j], hi_inv, s0, s1, s2, s3, s4, s5, s6, s7);
-        ngb++;
+        if (sub == 0) P.flags[i] = work ? (fl | 8) : (fl & ~8);
       }
     }
-    P.dens0[i] = make_float4(s0, s1, s2, s3);
-    P.dens1[i] = make_float4(s4, s5, s6, s7);
-    P.ngb_d[i] = ngb;
-    if (a.hits) atomicAdd(a.hits, (unsigned long long)ngb);
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f, s5 = 0.f, s6 = 0.f, s7 = 0.f;
+    int ngb = 0;
+    if (work) {
+      const float4 vi = P.velm[i];
+      const float hi_inv = 1.f / pi.w;
+      const int* row = a.nl + (size_t)i * a.nl_cap;
+      // four items per lane at a time, their loads all in flight together; a
+      // miss is evaluated too, at a distance beyond the kernel's support
+      // (zero contributions), so the lanes do not diverge
+      for (int t0 = sub; t0 < cnt; t0 += 4 * LPP) {
+        int pk[4];
+        float4 q[4], vm[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int t = t0 + u * LPP;
+          pk[u] = t < cnt ? row[t < c0 ? t : t - c0 + a.nl_cap / 2] : i;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          q[u] = P.posh[pk[u] & 0x07ffffff];
+          vm[u] = P.velm[pk[u] & 0x07ffffff];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int j = pk[u] & 0x07ffffff;
+          const float3 fd = offset_of((int)((unsigned)pk[u] >> 27), a.top_width);
+          const float dx = pi.x - (q[u].x + fd.x), dy = pi.y - (q[u].y + fd.y),
+                      dz = pi.z - (q[u].z + fd.z);
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          const bool item = t0 + u * LPP < cnt;
+          bool hit = item && r2 < L2;
+          if (item && !hit && r2 < U2) {  // inside the band: exact decision (rare)
+            const Entry* E = rerun_entry(a, P.leaf_of[i], a.blk_of[j], P.depth_h[i]);
+            hit = E != nullptr && exact_r2_2(P.xd, i, j, E) < hig2;
+          }
+          density_hit(dx, dy, dz, hit ? r2 : 4.f * U2, vi, vm[u], hi_inv, s0, s1, s2, s3, s4,
+                      s5, s6, s7);
+          ngb += hit;
+        }
+      }
+    }
+    // the particle's lanes add their partial sums (lanes of a group share
+    // `work`, so whole groups take part)
+#pragma unroll
+    for (int o = 1; o < LPP; o <<= 1) {
+      s0 += __shfl_xor_sync(FULL, s0, o);
+      s1 += __shfl_xor_sync(FULL, s1, o);
+      s2 += __shfl_xor_sync(FULL, s2, o);
+      s3 += __shfl_xor_sync(FULL, s3, o);
+      s4 += __shfl_xor_sync(FULL, s4, o);
+      s5 += __shfl_xor_sync(FULL, s5, o);
+      s6 += __shfl_xor_sync(FULL, s6, o);
+      s7 += __shfl_xor_sync(FULL, s7, o);
+      ngb += __shfl_xor_sync(FULL, ngb, o);
+    }
+    if (work && sub == 0) {
+      P.dens0[i] = make_float4(s0, s1, s2, s3);
+      P.dens1[i] = make_float4(s4, s5, s6, s7);
+      P.ngb_d[i] = ngb;
+      if (a.hits) atomicAdd(a.hits, (unsigned long long)ngb);
+    }
   }
 }
 

@@ -60,12 +60,15 @@ struct G2Args {
   float band;                   // relative band of the exact predicate
   int mode;                     // GatherMode
   // Neighbour lists of the ghost's re-runs, recorded by the first re-run
-  // (gathers launched with lists): item t of particle i at
-  // nl[i * nl_cap + t] (partner index | frame-offset index << 27), for
-  // every candidate with FP32 r^2 below (gamma h)^2 (1 + band); nl_cap is a
-  // multiple of 8 (items are written 8 at a time).
+  // (gathers launched with lists), for every candidate with FP32 r^2 below
+  // (gamma h)^2 (1 + band): items (partner index | frame-offset index << 27)
+  // of particle i in nl[i * nl_cap ...], one segment of nl_cap / TPP items
+  // per lane of the particle; segment sizes are multiples of 8 (items are
+  // written 8 at a time).
   int* nl;
-  int* nl_cnt;                  // items per particle, -1 when they overflowed
+  int* nl_cnt;                  // items per particle (two lanes: segment 0's
+                                // count | segment 1's << 16), -1 when a
+                                // segment overflowed
   float* nl_T;                  // the r^2 bound the items were recorded under
   int nl_cap;
 };
@@ -80,6 +83,8 @@ struct ListArgs {
   const int* nl_cnt;
   const float* nl_T;
   int nl_cap;
+  int nl_seg;                   // segments per row (lanes per particle of the
+                                // recording gather: 1 or 2)
   const int* leaf_pair_begin;   // the re-run (subset) lists, per leaf
   const int* pair_block;
   const int* pair_entry;

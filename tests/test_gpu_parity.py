@@ -103,7 +103,7 @@ def test_plain_equals_batched(case):
 
 @pytest.mark.parametrize("jtile,block_warps,tpp", [(32, 4, 1), (16, 8, 1), (16, 4, 1),
                                                    (8, 8, 1), (32, 8, 2), (16, 8, 2),
-                                                   (8, 4, 2)])
+                                                   (8, 4, 2), (32, 8, 4)])
 def test_every_tuning_keeps_parity(case, jtile, block_warps, tpp):
     """Each configuration the autotuner may pick holds the exact-count bar."""
     name, box, ref = case
@@ -123,14 +123,16 @@ def test_every_tuning_keeps_parity(case, jtile, block_warps, tpp):
         assert scaled_err(out[k], ref[k]).max() < REL, (name, k)
 
 
-def test_rerun_lists_match_rerun_gathers():
-    """Re-runs from the neighbour lists give the neighbour sets of re-runs
-    that gather (same counts), sums within FP32 summation-order noise."""
+@pytest.mark.parametrize("tpp", [1, 2])
+def test_rerun_lists_match_rerun_gathers(tpp):
+    """Re-runs from the neighbour lists (recorded by one or two lanes per
+    particle) give the neighbour sets of re-runs that gather (same counts),
+    sums within FP32 summation-order noise."""
     box = ics.make("clustered:40", seed=9)
     outs = []
     for lists in (1, 0):
         with api.Space(box) as sp:
-            sp.set_tuning(jtile=16, rerun_lists=lists, block_warps=8)
+            sp.set_tuning(tpp=tpp, jtile=16, rerun_lists=lists, block_warps=8)
             sp.step()
             sp.step()          # graph replay
             outs.append(sp.download())

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define SPHGPU_ABI_VERSION 1
+#define SPHGPU_ABI_VERSION 2
 
 #define SPHGPU_OK 0
 #define SPHGPU_EINVAL -1   /* bad argument */
@@ -226,6 +226,12 @@ int sphgpu_force_from_state(sphgpu_space *s, const float *h, const float *rho,
                             const float *soundspeed, const float *balsara,
                             void *stream);
 
+/* After a force pass: each particle's smallest time bin > 0 among its force
+ * neighbours (limiter_data.min_ngb_time_bin, set by runner_iact_timebin,
+ * timestep_limiter_iact.h:34-72; num_time_bins + 1 = 57 when it has none),
+ * input order.  Valid for the active particles of the last force pass. */
+int sphgpu_download_min_ngb_bin(sphgpu_space *s, int8_t *out);
+
 /* Drop-in per-task entry points (plain form).  `cell` / `ci`, `cj` are
  * top-level cell ids (cell_getid order).  Density and force accumulate into
  * the particle sums like the reference's loops; call sphgpu_begin_loops()
@@ -283,6 +289,60 @@ int sphgpu_server_stats(sphgpu_server *s, int64_t stats[8]);
  * rounds, force launches), [1] host planning of new boxes' force lists,
  * [2] admissions (uploads), [3] retirements (read-back). */
 int sphgpu_server_times(sphgpu_server *s, double times[4]);
+
+/* ---- Time integration (replaces runner_do_kick1 / runner_do_kick2 /
+ * runner_do_timestep, runner_time_integration.c:87 / :360 / :639, and the
+ * particle drift of cell_drift_part, cell_drift.c:159, for gas particles
+ * without cosmology, gravity, cooling or entropy floor).  The state lives
+ * in DEVICE memory, in the caller's order; every pointer of
+ * sphgpu_integ_state is a device pointer.  Kernels are enqueued on `stream`
+ * (a cudaStream_t; NULL: the legacy default stream). */
+typedef struct {
+  double time_base;        /* physical time of one integer tick */
+  double dt_min, dt_max;   /* engine dt_min / dt_max */
+  float CFL;               /* hydro_props->CFL_condition */
+  float log_max_h_change;  /* hydro_props->log_max_h_change */
+  float h_min, h_max;
+  float minimal_u;         /* hydro_props->minimal_internal_energy */
+  double dim[3];           /* box, for the periodic wrap of a rebuild */
+  int32_t periodic;
+} sphgpu_integ_params;
+
+typedef struct {
+  double *x;               /* [3n] positions */
+  float *v_full;           /* [3n] xpart.v_full */
+  float *v;                /* [3n] predicted velocities (part.v) */
+  float *a;                /* [3n] a_hydro */
+  float *u_full;           /* [n] xpart.u_full */
+  float *u, *u_dt;         /* [n] predicted internal energy, du/dt */
+  float *h, *h_dt;         /* [n] */
+  float *rho, *P, *c;      /* [n] density, pressure, sound speed */
+  float *v_sig;            /* [n] */
+  int8_t *time_bin;        /* [n] */
+  const int8_t *min_ngb_bin; /* [n] from the force pass (timestep only) */
+} sphgpu_integ_state;
+
+/* which = 1: the first half kick of the particles starting their step at
+ * ti_current (time_bin <= max_active_bin); which = 2: the second half kick
+ * of the particles ending it there, then hydro_reset_predicted_values. */
+int sphgpu_integ_kick(const sphgpu_integ_params *ip, const sphgpu_integ_state *st,
+                      int64_t n, int32_t which, int64_t ti_current,
+                      int32_t max_active_bin, void *stream);
+/* Drift every particle from ti_old to ti_current (drift_part +
+ * hydro_predict_extra + the h clamp); wrap != 0 also applies the periodic
+ * box_wrap of the rebuild that follows (space_cell_index.c:113-123). */
+int sphgpu_integ_drift(const sphgpu_integ_params *ip, const sphgpu_integ_state *st,
+                       int64_t n, int64_t ti_old, int64_t ti_current, int32_t wrap,
+                       void *stream);
+/* New time bins of the active particles; *ti_end_min = the next
+ * synchronisation point over all particles, *n_too_small = particles whose
+ * step fell below dt_min (the reference aborts there).  Synchronises the
+ * stream. */
+int sphgpu_integ_timestep(const sphgpu_integ_params *ip, const sphgpu_integ_state *st,
+                          int64_t n, int64_t ti_current, int32_t max_active_bin,
+                          int64_t *ti_end_min, int64_t *n_too_small, void *stream);
+/* get_max_active_bin (timeline.h:146) */
+int sphgpu_integ_max_active_bin(int64_t ti);
 
 #ifdef __cplusplus
 }

@@ -90,6 +90,8 @@ gcc -std=gnu11 -O2 -c "$HERE/ref_stubs.c" -o "$OUT/ref_stubs.o"
 LINK="-include float.h -include swift.h -include mhd.h"
 gcc $CF $LINK "$HERE/ref_harness.c" "$OUT/libswiftref.a" "$OUT/ref_stubs.o" \
     -lm -lpthread -Wl,--gc-sections -o "$OUT/bin/ref_harness"
+gcc $CF $LINK "$HERE/ref_integrate.c" "$OUT/libswiftref.a" "$OUT/ref_stubs.o" \
+    -lm -lpthread -Wl,--gc-sections -o "$OUT/bin/ref_integrate"
 
 # The reference's own hydro known-answer tests, built from its tests/ tree.
 for t in test27cells test125cells testActivePair testPeriodicBC testSymmetry testKernel; do

@@ -70,7 +70,7 @@ def write_input(path, box, stages=ALL_STAGES, **overrides):
 
 INT_COLS = {"leaf_first": 0, "leaf_count": 1, "leaf_depth": 2, "depth_h": 3,
             "position": 4, "top": 5, "ngb_first": 6, "ngb_final": 7,
-            "ngb_force": 8, "ghost_iters": 9}
+            "ngb_force": 8, "ghost_iters": 9, "min_ngb_bin": 10}
 
 
 def read_output(path):
@@ -92,7 +92,7 @@ def read_output(path):
     for name, col in COLS.items():
         out[name] = res[:, col]
     for name, col in INT_COLS.items():
-        if col < ni:
+        if col < ni and not np.all(ints[:, col] == -1):  # -1: not kept
             out[name] = ints[:, col]
     return out
 

@@ -19,7 +19,7 @@ from .io import COLS, INT_COLS
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libsphoracle.so")
-NFIELDS, NINTS = 24, 10
+NFIELDS, NINTS = 24, 11
 STAGE_DENSITY, STAGE_GHOST, STAGE_FORCE = 1, 2, 4
 ALL = 7
 
@@ -41,14 +41,14 @@ class Result(ctypes.Structure):
 
 
 def build(force=False):
-    src = os.path.join(HERE, "sph_oracle.c")
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(src)):
+    srcs = [os.path.join(HERE, f) for f in ("sph_oracle.c", "sph_integrate.c")]
+    newest = max(os.path.getmtime(f) for f in srcs + [os.path.join(HERE, "sph_oracle.h")])
+    if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
     subprocess.run(["gcc", "-std=gnu11", "-O2", "-fno-fast-math",
-                    "-ffp-contract=off", "-fPIC", "-shared", src, "-o", tmp,
+                    "-ffp-contract=off", "-fPIC", "-shared"] + srcs + ["-o", tmp,
                     "-lm"], check=True)
     os.replace(tmp, LIB)
     return LIB

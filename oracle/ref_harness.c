@@ -341,7 +341,9 @@ int main(int argc, char **argv) {
 
   const size_t nf = 24;
   float *res = xmalloc(n * nf * sizeof(float));
-#define NI 6
+/* the oracle's integer columns 0-5 and 10; 6-9 (neighbour counters the
+ * reference does not keep) are written as -1 */
+#define NI 11
   int32_t *ipart = xmalloc(n * NI * sizeof(int32_t));
 
   const int prime = (hdr.stages & STAGE_PRIME) != 0;
@@ -431,6 +433,8 @@ int main(int argc, char **argv) {
     ip[3] = P[k].depth_h;
     ip[4] = (int32_t)k;
     ip[5] = lr->top;
+    ip[6] = ip[7] = ip[8] = ip[9] = -1;
+    ip[10] = (hdr.stages & STAGE_FORCE) ? P[k].limiter_data.min_ngb_time_bin : -1;
   }
 
   FILE *fo = fopen(argv[2], "wb");

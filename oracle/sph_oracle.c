@@ -57,6 +57,7 @@
 #define MAXRELDX 0.1f
 #define SPLIT_SIZE 400
 #define RECURSE_SIZE 100
+#define NUM_TIME_BINS 56 /* timeline.h:36 */
 
 static const float wendland_c2[12] = {4.f, -15.f, 20.f, -10.f, 0.f, 1.f,
                                       0.f, 0.f,   0.f,  0.f,   0.f, 0.f};
@@ -112,6 +113,7 @@ typedef struct {
   float wcount, wcount_dh, rho_dh, div_v, rot_v[3];
   float f, pressure, soundspeed, v_sig, h_dt, balsara;
   signed char time_bin, depth_h;
+  signed char min_ngb_bin; /* limiter_data.min_ngb_time_bin */
   int ngb_d, ngb_d_first, ngb_f, ghost_iters;
 } opart;
 
@@ -314,6 +316,12 @@ static void iact_force_impl(float r2, const float dx[3], float hi, float hj,
   if (sym) pj->v_sig = fmaxf_ref(pj->v_sig, v_sig);
   pi->ngb_f++;
   if (sym) pj->ngb_f++;
+  /* runner_iact_timebin / runner_iact_nonsym_timebin
+   * (timestep_limiter_iact.h:34-72), called after every force interaction
+   * (runner_doiact_functions_hydro.h:161, :489, ...) */
+  if (pj->time_bin > 0 && pj->time_bin < pi->min_ngb_bin) pi->min_ngb_bin = pj->time_bin;
+  if (sym && pi->time_bin > 0 && pi->time_bin < pj->min_ngb_bin)
+    pj->min_ngb_bin = pi->time_bin;
 }
 
 static inline void iact_force(float r2, const float dx[3], float hi, float hj,
@@ -406,6 +414,8 @@ static void prepare_force(const octx *e, opart *p) {
   p->h_dt = 0.f;
   p->v_sig = 2.f * p->soundspeed;
   p->ngb_f = 0;
+  /* timestep_limiter_prepare_force (timestep_limiter.h:35) */
+  p->min_ngb_bin = NUM_TIME_BINS + 1;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1794,6 +1804,7 @@ int sph_oracle_run(const oracle_params *prm, int n, const double *x,
       ip[7] = p->ngb_d;
       ip[8] = p->ngb_f;
       ip[9] = p->ghost_iters;
+      ip[10] = p->min_ngb_bin;
     }
   }
   res->cdim[0] = s.cdim[0];
@@ -1803,6 +1814,70 @@ int sph_oracle_run(const oracle_params *prm, int n, const double *x,
   res->status = status;
   free_space(&s);
   return status;
+}
+
+/* The force loops alone on a given state: every particle takes h, rho,
+ * grad-h f, P, c and Balsara from state[6 n] (input order); the active
+ * ones (time_bin <= max_active_bin) restart their accelerations the way the
+ * ghost leaves them (hydro_reset_acceleration, hydro.h:749;
+ * timestep_limiter_prepare_force) and run the force loops and end_force.
+ * This is the force task of a step in which inactive particles keep the
+ * predicted state of their last step.  Fields 15-20 and ints 8, 10 are
+ * written. */
+int sph_oracle_run_state(const oracle_params *prm, int n, const double *x,
+                         const float *v, const float *m, const float *u,
+                         const signed char *time_bin, const float *state,
+                         oracle_result *res) {
+  float *h = (float *)ocalloc((size_t)n, sizeof(float));
+  for (int k = 0; k < n; k++) h[k] = state[6 * (size_t)k];
+  ospace s;
+  build_space(&s, prm, n, x, v, m, h, u, time_bin);
+  const int ntop = s.cdim[0] * s.cdim[1] * s.cdim[2];
+  for (int k = 0; k < n; k++) {
+    opart *p = &s.parts[k];
+    const float *st = &state[6 * (size_t)p->id];
+    p->rho = st[1];
+    p->f = st[2];
+    p->pressure = st[3];
+    p->soundspeed = st[4];
+    p->balsara = st[5];
+    if (part_active(&s.e, p)) {
+      p->a[0] = p->a[1] = p->a[2] = 0.f;
+      p->u_dt = 0.f;
+      p->h_dt = 0.f;
+      p->v_sig = 2.f * p->soundspeed;
+      p->min_ngb_bin = NUM_TIME_BINS + 1;
+    }
+    p->ngb_f = 0;
+  }
+  for (int t = 0; t < s.ntasks; t++) {
+    if (!s.tasks[t].is_pair)
+      dosub_self2(&s.e, s.tasks[t].ci, 0);
+    else
+      dosub_pair2(&s.e, s.tasks[t].ci, s.tasks[t].cj, 0);
+  }
+  for (int c = 0; c < ntop; c++) end_force(&s.e, &s.top[c]);
+  for (int k = 0; k < n; k++) {
+    const opart *p = &s.parts[k];
+    float *o = &res->fields[ORACLE_NFIELDS * p->id];
+    o[15] = p->a[0];
+    o[16] = p->a[1];
+    o[17] = p->a[2];
+    o[18] = p->u_dt;
+    o[19] = p->h_dt;
+    o[20] = p->v_sig;
+    int32_t *ip = &res->ints[ORACLE_NINTS * p->id];
+    ip[8] = p->ngb_f;
+    ip[10] = p->min_ngb_bin;
+  }
+  res->cdim[0] = s.cdim[0];
+  res->cdim[1] = s.cdim[1];
+  res->cdim[2] = s.cdim[2];
+  res->ncells = s.pool.ncells;
+  res->status = 0;
+  free_space(&s);
+  free(h);
+  return 0;
 }
 
 /* ------------------------------------------------------------------------ */

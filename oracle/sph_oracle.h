@@ -21,8 +21,10 @@
 /* Per-particle integers: 0 leaf first index, 1 leaf count, 2 leaf depth,
  * 3 depth_h, 4 position in the cell-sorted order, 5 top cell id,
  * 6 density neighbours (first pass), 7 density neighbours (last pass),
- * 8 force neighbours, 9 ghost iterations. */
-#define ORACLE_NINTS 10
+ * 8 force neighbours, 9 ghost iterations, 10 smallest time bin among the
+ * force neighbours (limiter_data.min_ngb_time_bin; num_time_bins + 1 when
+ * there is none). */
+#define ORACLE_NINTS 11
 
 typedef struct {
   double dim[3];
@@ -44,6 +46,13 @@ int sph_oracle_run(const oracle_params *prm, int n, const double *x,
                    const float *u, const signed char *time_bin, int stages,
                    oracle_result *res);
 
+/* The force loops alone on a given state (h, rho, f, P, c, Balsara per
+ * particle, state[6 n]); see sph_oracle.c. */
+int sph_oracle_run_state(const oracle_params *prm, int n, const double *x,
+                         const float *v, const float *m, const float *u,
+                         const signed char *time_bin, const float *state,
+                         oracle_result *res);
+
 /* Sort arrays of every non-empty cell, depth first: rec [ncells][3] =
  * first (cell-sorted order), count, depth; d / idx: per cell 13 arrays of
  * count + 1 entries (keys ascending, FLT_MAX sentinel).  Call with
@@ -58,4 +67,33 @@ void sph_oracle_exact64(const oracle_params *prm, int n, const double *x,
                         const float *v, const float *m, const float *h,
                         const float *rho, const float *f, const float *P,
                         const float *cs, const float *bal, double *out);
+/* Time integration (sph_integrate.c).  State arrays are SoA in the
+ * caller's order: x[3 n] (double), v_full, v (predicted), a (a_hydro) [3 n];
+ * u_full, u (predicted), u_dt, h, h_dt, rho, P, c, v_sig [n]; time_bin [n]. */
+typedef struct {
+  double time_base;     /* physical time of one integer tick */
+  double dt_min, dt_max;
+  float CFL;            /* hydro_props->CFL_condition */
+  float log_max_h_change;
+  float h_min, h_max;
+  float minimal_u;      /* hydro_props->minimal_internal_energy */
+} integ_params;
+
+typedef struct {
+  double *x;
+  float *v_full, *v, *a;
+  float *u_full, *u, *u_dt, *h, *h_dt, *rho, *P, *c, *v_sig;
+  signed char *time_bin;
+} integ_state;
+
+void sph_integ_kick(const integ_params *ip, integ_state *st, int64_t n, int which,
+                    int64_t ti_current, int max_active_bin);
+void sph_integ_drift(const integ_params *ip, integ_state *st, int64_t n, int64_t ti_old,
+                     int64_t ti_current);
+int64_t sph_integ_timestep(const integ_params *ip, integ_state *st, int64_t n,
+                           const signed char *min_ngb_bin, int64_t ti_current,
+                           int max_active_bin);
+int64_t sph_integ_ti_end_min(const integ_state *st, int64_t n, int64_t ti_current);
+int sph_integ_max_active_bin(int64_t ti);
+int64_t sph_integ_time_end(int64_t ti, int bin);
 #endif

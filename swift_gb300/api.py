@@ -54,6 +54,22 @@ class Tuning(ctypes.Structure):
                 ("block_warps", ctypes.c_int32)]
 
 
+class IntegParams(ctypes.Structure):
+    _fields_ = [("time_base", ctypes.c_double), ("dt_min", ctypes.c_double),
+                ("dt_max", ctypes.c_double), ("CFL", ctypes.c_float),
+                ("log_max_h_change", ctypes.c_float), ("h_min", ctypes.c_float),
+                ("h_max", ctypes.c_float), ("minimal_u", ctypes.c_float),
+                ("dim", ctypes.c_double * 3), ("periodic", ctypes.c_int32)]
+
+
+INTEG_FIELDS = ("x", "v_full", "v", "a", "u_full", "u", "u_dt", "h", "h_dt", "rho",
+                "P", "c", "v_sig", "time_bin", "min_ngb_bin")
+
+
+class IntegState(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in INTEG_FIELDS]
+
+
 # Every symbol the header declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -76,6 +92,16 @@ SIGNATURES = {
     "sphgpu_step_plain": (ctypes.c_int, [_P, _P]),
     "sphgpu_download": (ctypes.c_int, [_P, _P, _P]),
     "sphgpu_force_from_state": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "sphgpu_download_min_ngb_bin": (ctypes.c_int, [_P, _P]),
+    "sphgpu_integ_kick": (ctypes.c_int, [ctypes.POINTER(IntegParams), ctypes.POINTER(IntegState),
+                                         ctypes.c_int64, _I32, ctypes.c_int64, _I32, _P]),
+    "sphgpu_integ_drift": (ctypes.c_int, [ctypes.POINTER(IntegParams), ctypes.POINTER(IntegState),
+                                          ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _I32,
+                                          _P]),
+    "sphgpu_integ_timestep": (ctypes.c_int, [ctypes.POINTER(IntegParams),
+                                             ctypes.POINTER(IntegState), ctypes.c_int64,
+                                             ctypes.c_int64, _I32, _P, _P, _P]),
+    "sphgpu_integ_max_active_bin": (ctypes.c_int, [ctypes.c_int64]),
     "sphgpu_begin_loops": (ctypes.c_int, [_P, _P]),
     "sphgpu_dosub_self1_density": (ctypes.c_int, [_P, _I32, _P]),
     "sphgpu_dosub_pair1_density": (ctypes.c_int, [_P, _I32, _I32, _P]),
@@ -328,6 +354,13 @@ class Space:
             out[name] = fields[:, col]
         for name, col in INT_COLS.items():
             out[name] = ints[:, col]
+        return out
+
+    def min_ngb_bin(self):
+        """Smallest time bin > 0 among each particle's force neighbours (last
+        force pass; 57 when it has none)."""
+        out = np.zeros(self.n, np.int8)
+        _check(lib().sphgpu_download_min_ngb_bin(self._h, _ptr(out)))
         return out
 
     def force_from_state(self, h, rho, f, pressure, soundspeed, balsara):

@@ -46,6 +46,7 @@ struct sphgpu_space {
   std::vector<double> x_in;
   std::vector<float> v_in, m_in, h_in, u_in;
   std::vector<int8_t> tb_in;
+  DBuf<int8_t> tbin, ngb_bin;  // store order: time bins, neighbours' smallest bin
   sphgpu_tuning tune{1, SPH_JBLOCK, 1, 8};
 
   // host plans
@@ -205,7 +206,7 @@ void ensure_device(sphgpu_space* s) {
   std::vector<float4> vm(n);
   std::vector<float> hs(n), us(n);
   std::vector<uint8_t> fl(n);
-  std::vector<int8_t> dh(n), dh0(n);
+  std::vector<int8_t> dh(n), dh0(n), tb(n);
   std::vector<int32_t> top(n), lf(n);
   const auto& xw = sp.x();
   const auto& act = sp.active();
@@ -222,6 +223,7 @@ void ensure_device(sphgpu_space* s) {
     hs[g] = s->h_in[k];
     us[g] = s->u_in[k];
     fl[g] = act[srt] ? 1 : 0;
+    tb[g] = s->tb_in[k];
     dh[g] = sp.depth_h()[srt];
     dh0[g] = sp.h_depth_of(s->h_in[k], lvs[leaf_of[srt]]);
     lf[g] = leaf_of[srt];
@@ -267,6 +269,9 @@ void ensure_device(sphgpu_space* s) {
   upload_activity(s, st);
   s->depth_h.upload(dh.data(), n, st);
   s->depth_h0.upload(dh0.data(), n, st);
+  s->tbin.upload(tb.data(), n, st);
+  s->ngb_bin.alloc(n);
+  CK(cudaMemsetAsync(s->ngb_bin.p, SPH_NUM_TIME_BINS + 1, n, st));
   s->leaf_of.upload(lf.data(), n, st);
   s->top_of.upload(top.data(), n, st);
   s->perm.upload(gperm.data(), n, st);
@@ -334,6 +339,8 @@ void ensure_device(sphgpu_space* s) {
   P.ngb_d = s->ngb_d.p;
   P.ngb_d_first = s->ngb_d_first.p;
   P.ngb_f = s->ngb_f.p;
+  P.tbin = s->tbin.p;
+  P.ngb_bin = s->ngb_bin.p;
   CK(launch_prepare_posh(P, s->top_of.p, s->top_loc.p, st));
   s->dplan_d.upload(s->plan_d, st);
   s->dplan_s.upload(s->plan_s, st);
@@ -843,6 +850,20 @@ int sphgpu_download(sphgpu_space* s, float* fields, int32_t* ints) {
       CK(cudaMemcpyAsync(ints, di.p, sizeof(int32_t) * 4 * (size_t)n,
                          cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    return SPHGPU_OK;
+  });
+}
+
+int sphgpu_download_min_ngb_bin(sphgpu_space* s, int8_t* out) {
+  if (!s || !out) return fail(SPHGPU_EINVAL, "null argument");
+  if (!s->dev) return fail(SPHGPU_ESTATE, "no step has run on this space");
+  return guard([&]() {
+    const int n = s->P.n;
+    std::vector<int8_t> st_order(n);
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpy(st_order.data(), s->ngb_bin.p, n, cudaMemcpyDeviceToHost));
+    const auto& gperm = s->space->gperm();
+    for (int g = 0; g < n; g++) out[gperm[g]] = st_order[g];
     return SPHGPU_OK;
   });
 }

@@ -229,6 +229,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           s7 = 0.f;
     if (FORCE) s5 = 2.f * fi.w;
     int ngb = 0;
+    int nbin = SPH_NUM_TIME_BINS + 1;  // smallest time bin > 0 of the force neighbours
     int qh = 0, qt = 0;  // ring head / tail (pending hits: qt - qh)
 
     auto interact = [&](int packed) {
@@ -275,6 +276,10 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         s3 += (Pi * dvdr * r_inv * wi_dr + 0.5f * visc_acc * dvdr) * mj;
         s4 -= __fdividef(mj * dvdr * r_inv, fj.x) * wi_dr * f_ij;
         s5 = fmaxf(s5, vs);
+        if (P.tbin) {  // runner_iact_nonsym_timebin (timestep_limiter_iact.h:64)
+          const int tb = P.tbin[j];
+          if (tb > 0) nbin = min(nbin, tb);
+        }
       }
       ngb++;
     };
@@ -479,6 +484,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
       s6 += __shfl_xor_sync(FULL, s6, o);
       s7 += __shfl_xor_sync(FULL, s7, o);
       ngb += __shfl_xor_sync(FULL, ngb, o);
+      if (FORCE) nbin = min(nbin, __shfl_xor_sync(FULL, nbin, o));
     }
     // lists: each lane of a particle fills its own segment of the row
     // (nl_cap / TPP items); the count word holds both segments' counts
@@ -526,11 +532,13 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         P.acc[i] = ac;
         P.hdt_vsig[i] = hv;
         P.ngb_f[i] += ngb;
+        if (P.ngb_bin) P.ngb_bin[i] = (int8_t)min((int)P.ngb_bin[i], nbin);
       } else {
         // hydro_end_force (hydro.h:878) folded in
         P.acc[i] = make_float4(s0, s1, s2, s3);
         P.hdt_vsig[i] = make_float2(s4 * (hi * SPH_HDIM_INV), s5);
         P.ngb_f[i] = ngb;
+        if (P.ngb_bin) P.ngb_bin[i] = (int8_t)nbin;
       }
     }
   }

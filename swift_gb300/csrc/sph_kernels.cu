@@ -37,6 +37,7 @@ __device__ void prepare_force(const DevParticles& P, int i, float h, float rho,
   P.fin1[i] = make_float2(balsara, pressure);
   P.acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   P.hdt_vsig[i] = make_float2(0.f, 2.f * c);
+  if (P.ngb_bin) P.ngb_bin[i] = SPH_NUM_TIME_BINS + 1;  // timestep_limiter_prepare_force
 }
 
 __global__ void ghost_round(GhostArgs g) {

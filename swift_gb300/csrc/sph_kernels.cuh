@@ -36,6 +36,11 @@ struct DevParticles {
   int32_t* ngb_d;
   int32_t* ngb_d_first;
   int32_t* ngb_f;
+  // optional (null: not kept): time bins, and the smallest time bin > 0
+  // among each particle's force neighbours (limiter_data.min_ngb_time_bin,
+  // num_time_bins + 1 when none), which limits its next time step
+  const int8_t* tbin = nullptr;
+  int8_t* ngb_bin = nullptr;
 };
 
 enum GatherMode { MODE_FIRST = 0, MODE_REDO = 1, MODE_ACCUM = 2 };

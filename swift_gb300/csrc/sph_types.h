@@ -64,6 +64,7 @@ static_assert(sizeof(Entry) == 80, "Entry layout");
 // j-block: up to kJBlock consecutive particles of one leaf (spatially
 // sorted), with their bounding box in the top-cell frame; the gather culls
 // whole blocks against each particle's search sphere.
+#define SPH_NUM_TIME_BINS 56  // timeline.h:36
 #define SPH_JBLOCK 16  // default j-block depth (the autotuner tries 8, 16, 32)
 
 // Per-leaf geometry needed on the device by the ghost (cell_set_part_h_depth,

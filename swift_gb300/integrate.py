@@ -1,0 +1,201 @@
+"""Time integration of a box of gas particles on the GPU: the reference's
+engine sequence (engine_init_particles, engine.c:2245; engine_step) with the
+drift-everything policy (the reference's --drift-all, engine_policy_drift_all)
+and a cell rebuild at every step.
+
+Per step, as the reference's task graph runs it:
+    ti_old = ti_current; ti_current = ti_end_min
+    max_active_bin = get_max_active_bin(ti_current)        (timeline.h:146)
+    drift every particle to ti_current (drift_part + hydro_predict_extra,
+        cell_drift.c:253-332), then the periodic wrap of the rebuild
+    rebuild: a new space (cell tree, sorts, gather lists) from the drifted
+        positions
+    density -> ghost for the active particles (time_bin <= max_active_bin)
+    force for the active particles; inactive ones lend their predicted state
+    kick2, timestep, kick1 for the active particles
+        (runner_time_integration.c:360, :639, :87)
+
+The particle state stays in device memory (torch tensors, the caller's
+order); the kicks, the drift and the time steps are CUDA kernels of the
+library (sphgpu_integ_*).  The density / ghost / force passes run through
+:class:`swift_gb300.api.Space`, whose tree is built on the host from the
+drifted positions (a host round trip per step: the device-resident rebuild
+is a separate piece of work).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import api
+
+NUM_TIME_BINS = 56
+MAX_NR_TIMESTEPS = 1 << (NUM_TIME_BINS + 1)
+
+
+def default_log_max_h_change():
+    """hydro_props_init's log of the largest h change per step from the
+    default volume change of 1.4 (hydro_properties.c): log(1.4^(1/3))."""
+    return float(np.log(np.power(np.float32(1.4), np.float32(1.0) / np.float32(3.0),
+                                 dtype=np.float32), dtype=np.float32))
+
+
+class Integrator:
+    """Integrates ``box`` (positions, velocities, masses, h, u) forward in
+    time on ``cuda:0``.  ``time_end`` fixes the integer time line
+    (time_base = time_end / 2^57); dt_min / dt_max / cfl are the engine's
+    and hydro scheme's parameters.  Space parameters (eta, h_tolerance,
+    max_iter, periodic ...) pass through to every rebuild."""
+
+    def __init__(self, box, *, time_end=1.0, cfl=0.1, dt_min=1e-12, dt_max=1e-2,
+                 log_max_h_change=None, minimal_u=0.0, device="cuda", **space_params):
+        if not torch.cuda.is_available():
+            raise RuntimeError("Integrator needs a CUDA device")
+        self.dev = torch.device(device)
+        self.n = int(box["x"].shape[0])
+        d = box["dim"]
+        self.dim = tuple(float(v) for v in (d if np.ndim(d) else (d, d, d)))
+        self.space_params = dict(space_params)
+        self.box_meta = {k: box[k] for k in ("eta",) if k in box}
+        prm = api.make_params(box, **space_params)
+        self.ip = api.IntegParams()
+        self.ip.time_base = float(time_end) / MAX_NR_TIMESTEPS
+        self.ip.dt_min = float(dt_min)
+        self.ip.dt_max = float(dt_max)
+        self.ip.CFL = float(cfl)
+        self.ip.log_max_h_change = (default_log_max_h_change() if log_max_h_change is None
+                                    else float(log_max_h_change))
+        self.ip.h_min = prm.h_min
+        self.ip.h_max = prm.h_max
+        self.ip.minimal_u = float(minimal_u)
+        self.ip.dim[:] = list(self.dim)
+        self.ip.periodic = prm.periodic
+        n, dev = self.n, self.dev
+        f32 = dict(dtype=torch.float32, device=dev)
+        self.m = np.ascontiguousarray(box["m"], np.float32)
+        v = torch.as_tensor(np.ascontiguousarray(box["v"], np.float32), device=dev)
+        u = torch.as_tensor(np.ascontiguousarray(box["u"], np.float32), device=dev)
+        self.t = {
+            "x": torch.as_tensor(np.ascontiguousarray(box["x"], np.float64), device=dev),
+            "v_full": v.clone(), "v": v.clone(), "a": torch.zeros((n, 3), **f32),
+            "u_full": u.clone(), "u": u.clone(), "u_dt": torch.zeros(n, **f32),
+            "h": torch.as_tensor(np.ascontiguousarray(box["h"], np.float32), device=dev),
+            "h_dt": torch.zeros(n, **f32), "rho": torch.zeros(n, **f32),
+            "P": torch.zeros(n, **f32), "c": torch.zeros(n, **f32),
+            "v_sig": torch.zeros(n, **f32),
+            "time_bin": torch.zeros(n, dtype=torch.int8, device=dev),
+            "min_ngb_bin": torch.full((n,), NUM_TIME_BINS + 1, dtype=torch.int8, device=dev),
+        }
+        # grad-h term and Balsara switch: the force state an inactive
+        # particle keeps from its last ghost
+        self.f = np.zeros(n, np.float32)
+        self.balsara = np.zeros(n, np.float32)
+        self.ti_current = 0
+        self.ti_end_min = 0
+        self.steps = 0
+        self.last_active = 0
+
+    # -- device state ------------------------------------------------------
+    def _state(self):
+        st = api.IntegState()
+        for k in api.INTEG_FIELDS:
+            setattr(st, k, ctypes.c_void_p(self.t[k].data_ptr()))
+        return st
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def state(self):
+        """The particle state as numpy arrays (the caller's order)."""
+        torch.cuda.synchronize(self.dev)
+        out = {k: v.cpu().numpy() for k, v in self.t.items()}
+        out["f"] = self.f.copy()
+        out["balsara"] = self.balsara.copy()
+        return out
+
+    @property
+    def time(self):
+        return self.ti_current * self.ip.time_base
+
+    # -- the operations ----------------------------------------------------
+    def _kick(self, which, mab):
+        L = api.lib()
+        api._check(L.sphgpu_integ_kick(ctypes.byref(self.ip), ctypes.byref(self._state()),
+                                       self.n, which, self.ti_current, mab, self._stream()))
+
+    def _drift(self, ti_old, ti_new):
+        L = api.lib()
+        api._check(L.sphgpu_integ_drift(ctypes.byref(self.ip), ctypes.byref(self._state()),
+                                        self.n, ti_old, ti_new, 1, self._stream()))
+
+    def _timestep(self, mab):
+        L = api.lib()
+        tmin, bad = ctypes.c_int64(), ctypes.c_int64()
+        api._check(L.sphgpu_integ_timestep(ctypes.byref(self.ip), ctypes.byref(self._state()),
+                                           self.n, self.ti_current, mab, ctypes.byref(tmin),
+                                           ctypes.byref(bad), self._stream()))
+        if bad.value:
+            raise api.SphGpuError(api.EINVAL, f"{bad.value} particles want a time step "
+                                  f"below dt_min ({self.ip.dt_min})")
+        self.ti_end_min = tmin.value
+
+    def _hydro(self, mab, stages=api.STAGE_ALL):
+        """Rebuild from the current state and run density -> ghost (-> force)
+        for the particles with time_bin <= mab."""
+        torch.cuda.synchronize(self.dev)
+        host = {k: self.t[k].cpu().numpy() for k in ("x", "v", "h", "u", "rho", "P", "c",
+                                                     "time_bin")}
+        box = dict(x=host["x"], v=host["v"], m=self.m, h=host["h"], u=host["u"],
+                   time_bin=host["time_bin"], dim=self.dim, **self.box_meta)
+        act = host["time_bin"] <= mab
+        self.last_active = int(act.sum())
+        with api.Space(box, max_active_bin=mab, **self.space_params) as sp:
+            sp.step(api.STAGE_DENSITY | api.STAGE_GHOST)
+            g = sp.download()
+            h = np.where(act, g["h"], host["h"]).astype(np.float32)
+            rho = np.where(act, g["rho"], host["rho"]).astype(np.float32)
+            P = np.where(act, g["pressure"], host["P"]).astype(np.float32)
+            c = np.where(act, g["soundspeed"], host["c"]).astype(np.float32)
+            self.f = np.where(act, g["f"], self.f).astype(np.float32)
+            self.balsara = np.where(act, g["balsara"], self.balsara).astype(np.float32)
+            for k, arr in (("h", h), ("rho", rho), ("P", P), ("c", c)):
+                self.t[k].copy_(torch.as_tensor(arr, device=self.dev))
+            if not stages & api.STAGE_FORCE:
+                return
+            sp.force_from_state(h, rho, self.f, P, c, self.balsara)
+            o = sp.download()
+            nb = sp.min_ngb_bin()
+        ia = torch.as_tensor(np.nonzero(act)[0], device=self.dev)
+        a = np.stack([o["ax"], o["ay"], o["az"]], axis=1).astype(np.float32)
+        for k, arr in (("a", a), ("u_dt", o["u_dt"]), ("h_dt", o["h_dt"]),
+                       ("v_sig", o["v_sig"]), ("min_ngb_bin", nb)):
+            src = torch.as_tensor(np.ascontiguousarray(arr), device=self.dev)
+            self.t[k][ia] = src[ia]
+
+    # -- the engine sequence -----------------------------------------------
+    def init(self):
+        """engine_init_particles: a density / ghost pass to settle h, then
+        the initial step at ti = 0 with every particle active (force, kick2
+        over a zero interval, time steps, kick1)."""
+        mab = NUM_TIME_BINS
+        self._hydro(mab, api.STAGE_DENSITY | api.STAGE_GHOST)
+        self._hydro(mab)
+        self._kick(2, mab)
+        self._timestep(mab)
+        self._kick(1, mab)
+        return self
+
+    def step(self):
+        """engine_step: advance to the next synchronisation point."""
+        ti_old = self.ti_current
+        self.ti_current = self.ti_end_min
+        mab = api.lib().sphgpu_integ_max_active_bin(self.ti_current)
+        self._drift(ti_old, self.ti_current)
+        self._hydro(mab)
+        self._kick(2, mab)
+        self._timestep(mab)
+        self._kick(1, mab)
+        self.steps += 1
+        return mab

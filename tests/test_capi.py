@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_defaults():
     L = api.lib()
-    assert L.sphgpu_abi_version() == 1
+    assert L.sphgpu_abi_version() == 2
     p = api.Params()
     L.sphgpu_default_params(ctypes.byref(p))
     assert abs(p.eta - 1.2348) < 1e-6 and p.max_iter == 30

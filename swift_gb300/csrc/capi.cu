@@ -339,7 +339,13 @@ void ensure_device(sphgpu_space* s) {
   P.ngb_d = s->ngb_d.p;
   P.ngb_d_first = s->ngb_d_first.p;
   P.ngb_f = s->ngb_f.p;
-  P.tbin = s->tbin.p;
+  // The neighbours' smallest time bin can only limit a time step when the
+  // bins differ (a step grows at most 2x, i.e. one bin, per step): with one
+  // bin everywhere the force loops skip the extra load and leave it at
+  // num_time_bins + 1.
+  const bool mixed_bins = std::any_of(s->tb_in.begin(), s->tb_in.end(),
+                                      [&](int8_t b) { return b != s->tb_in[0]; });
+  P.tbin = mixed_bins ? s->tbin.p : nullptr;
   P.ngb_bin = s->ngb_bin.p;
   CK(launch_prepare_posh(P, s->top_of.p, s->top_loc.p, st));
   s->dplan_d.upload(s->plan_d, st);

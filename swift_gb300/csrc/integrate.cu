@@ -51,14 +51,17 @@ __device__ __forceinline__ long long integer_timestep(int bin) {
 __device__ __forceinline__ int time_bin_of(long long dti) {
   return 62 - __clzll(dti);
 }
+// The steps are powers of two, so the divisions of the time line are shifts
+// and masks (non-negative operands; (ti - 1) / dti truncates to 0 at ti = 0).
 __device__ __forceinline__ long long time_begin(long long ti, int bin) {
   const long long dti = integer_timestep(bin);
-  return dti == 0 ? 0 : dti * ((ti - 1) / dti);
+  if (dti == 0 || ti <= 0) return 0;
+  return ((ti - 1) >> (bin + 1)) << (bin + 1);
 }
 __device__ __forceinline__ long long time_end(long long ti, int bin) {
   const long long dti = integer_timestep(bin);
   if (dti == 0) return 0;
-  const long long mod = ti % dti;
+  const long long mod = ti & (dti - 1);
   return mod == 0 ? ti : ti - mod + dti;
 }
 
@@ -189,10 +192,12 @@ __global__ void timestep_k(sphgpu_integ_params ip, sphgpu_integ_state st, long l
       const long long current_dti = integer_timestep(bin);
       const long long ti_end = time_end(ti_current, bin);
       if (bin > 0) new_dti = min(new_dti, 2 * current_dti);
-      long long dti_timeline = kMaxNrTimesteps;
-      while (new_dti < dti_timeline) dti_timeline /= 2;
-      new_dti = dti_timeline;
-      if (new_dti > current_dti && (kMaxNrTimesteps - ti_end) % new_dti > 0) new_dti = current_dti;
+      // the largest power of two on the time line not above new_dti (the
+      // reference halves max_nr_timesteps until it is not above new_dti)
+      new_dti = new_dti >= kMaxNrTimesteps ? kMaxNrTimesteps
+              : (new_dti <= 0 ? 0 : (1LL << (63 - __clzll(new_dti))));
+      if (new_dti > current_dti && ((kMaxNrTimesteps - ti_end) & (new_dti - 1)) != 0)
+        new_dti = current_dti;
       bin = time_bin_of(new_dti);
       st.time_bin[k] = (int8_t)bin;
     }

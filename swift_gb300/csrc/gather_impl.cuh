@@ -119,6 +119,7 @@ struct LaneSmem {
   float4 shi[32];
   int q[QCAP][32];     // per-lane hit ring
   int lb[8][32];       // per-lane staging of neighbour-list items (LISTS)
+  float4 ftab[27];     // frame offsets of the 27 partner top cells (offset_of)
 };
 
 // Frame offset of a partner top cell from its index in the 3x3x3
@@ -165,6 +166,16 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
   const unsigned lt_mask = (1u << lane) - 1u;
   const float band = a.band;
   float3 tw = a.top_width;
+  // frame offsets by index, looked up for every hit (the warp's own table:
+  // with per-leaf top widths it changes between groups)
+  auto fill_ftab = [&]() {
+    if (lane < 27) {
+      const float3 o = offset_of(lane, tw);
+      ws.ftab[lane] = make_float4(o.x, o.y, o.z, 0.f);
+    }
+    __syncwarp();
+  };
+  fill_ftab();
   for (;;) {
     int u = 0;
     if (lane == 0) u = atomicAdd(a.queue, 1);
@@ -174,7 +185,11 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     if (U.y == 0) continue;     // no particle of this window takes part
     if (a.leaf_tw) {
       const float4 t = a.leaf_tw[P.leaf_of[U.x]];
-      tw = make_float3(t.x, t.y, t.z);
+      if (t.x != tw.x || t.y != tw.y || t.z != tw.z) {
+        tw = make_float3(t.x, t.y, t.z);
+        __syncwarp();
+        fill_ftab();
+      }
     }
     const bool valid = (U.y >> pl) & 1;
     const int i = U.x + pl;
@@ -234,7 +249,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
 
     auto interact = [&](int packed) {
       const int j = packed & 0x07ffffff;
-      const float3 fd = offset_of((int)((unsigned)packed >> 27), tw);
+      const float4 fd = ws.ftab[(unsigned)packed >> 27];
       const float4 q = P.posh[j];
       const float dx = pi.x - (q.x + fd.x), dy = pi.y - (q.y + fd.y),
                   dz = pi.z - (q.z + fd.z);
@@ -590,6 +605,12 @@ static __global__ void __launch_bounds__(256, 3) redo_from_lists(ListArgs a) {
   constexpr int LPP = 8;  // lanes per particle
   if (a.gate && *a.gate == 0) return;
   const DevParticles& P = a.p;
+  __shared__ float4 ftab[27];  // frame offsets by index (offset_of)
+  if (threadIdx.x < 27) {
+    const float3 o = offset_of(threadIdx.x, a.top_width);
+    ftab[threadIdx.x] = make_float4(o.x, o.y, o.z, 0.f);
+  }
+  __syncthreads();
   const int sub = threadIdx.x % LPP;
   const int stride = gridDim.x * blockDim.x / LPP;
   // the warp's four particles advance together (the shuffles below need
@@ -642,7 +663,7 @@ static __global__ void __launch_bounds__(256, 3) redo_from_lists(ListArgs a) {
 #pragma unroll
         for (int u = 0; u < 4; u++) {
           const int j = pk[u] & 0x07ffffff;
-          const float3 fd = offset_of((int)((unsigned)pk[u] >> 27), a.top_width);
+          const float4 fd = ftab[(unsigned)pk[u] >> 27];
           const float dx = pi.x - (q[u].x + fd.x), dy = pi.y - (q[u].y + fd.y),
                       dz = pi.z - (q[u].z + fd.z);
           const float r2 = dx * dx + dy * dy + dz * dz;

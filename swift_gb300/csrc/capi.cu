@@ -161,7 +161,12 @@ void build_plans(sphgpu_space* s) {
 void upload_activity(sphgpu_space* s, cudaStream_t st);
 
 // Re-run neighbour lists: at most kListCap items per particle.
-constexpr int kListCap = 128;
+constexpr int kListCap = 160;
+// The first density pass records each particle's candidates within
+// sqrt(kListWiden) its search radius (capped by its depth_h cell's width), so
+// that the ghost's re-runs -- Newton's first step moves h by less than 10 %
+// for almost every particle -- run from the lists.
+constexpr float kListWiden = 1.21f;
 
 // j-block boxes and particle ranges of the current j-block depth.
 void upload_blocks(sphgpu_space* s, cudaStream_t st) {
@@ -386,6 +391,8 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   a.nl_cnt = nullptr;
   a.nl_T = nullptr;
   a.nl_cap = 0;
+  a.nl_widen = 1.f;
+  a.leaves = s->leaves.p;
   return a;
 }
 
@@ -423,6 +430,7 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
     a.nl_cnt = s->nl_cnt.p;
     a.nl_T = s->nl_T.p;
     a.nl_cap = kListCap;
+    if (mode == MODE_FIRST) a.nl_widen = kListWiden;
   }
   CK(launch_gather(a, force, s->num_sms, w1 - w0, st, s->tune.block_warps, lists, tpp));
 }
@@ -468,16 +476,16 @@ GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
 // flagged, and re-runs the density of those it sends to another round
 // (subset gather lists); both kernels return at once when the previous
 // round sent none (gates on the redo counts).
+bool lists_on(const sphgpu_space* s) { return s->lists && s->tune.rerun_lists; }
+
 void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st) {
   for (int k = 0; k < s->prm.max_iter; k++) {
     CK(launch_ghost(ghargs(s, k, 0, s->P.n), st));
-    if (!s->lists || !s->tune.rerun_lists) {
+    if (!lists_on(s)) {
       enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k);
-    } else if (k == 0) {
-      // the first re-run records each particle's neighbour list
-      enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k, 0, -1, 0, true);
     } else {
-      // later re-runs: from the lists where they cover h, the gather for the rest
+      // re-runs from the first pass's lists where they cover h, the gather
+      // for the rest
       CK(launch_redo_from_lists(largs(s, s->redo.p + k), st));
       enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k, 0, -1, 8);
     }
@@ -486,7 +494,9 @@ void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st) {
 
 void enqueue_density(sphgpu_space* s, cudaStream_t st, bool density) {
   CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, s->prm.h_max, st));
-  if (density) enqueue_gather(s, st, s->dplan_d, 0, MODE_FIRST, false, 1, nullptr);
+  // the first pass records the re-runs' lists
+  if (density)
+    enqueue_gather(s, st, s->dplan_d, 0, MODE_FIRST, false, 1, nullptr, 0, -1, 0, lists_on(s));
 }
 
 void enqueue_density_ghost(sphgpu_space* s, cudaStream_t st, int stages) {

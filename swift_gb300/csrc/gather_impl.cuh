@@ -212,6 +212,16 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     const float hid_inv = (hi_inv * hi_inv) * (hi_inv * hi_inv);
     const float mi_inv = 1.f / vi.w;
     const float lo2 = hig2 * (1.f - band), hi2 = hig2 * (1.f + band);
+    // recording bound of the lists (r^2, FP32) and the radius the culls use
+    float lw2 = hi2;
+    if (LISTS && valid && a.nl_widen > 1.f) {
+      const LeafInfo& L = a.leaves[P.leaf_of[i]];
+      float cover = 0.f;
+      for (int lev = 0; lev < L.nlevels; lev++)
+        if (L.depth[lev] == dh) cover = SPH_KG * L.hmax[lev] * (1.f - 1.f / 1024.f);
+      lw2 = fmaxf(hi2, fminf(hi2 * a.nl_widen, cover * cover));
+    }
+    const float cr2 = LISTS ? lw2 : hig2;
     const float2 pix2 = make_float2(pi.x, pi.x), piy2 = make_float2(pi.y, pi.y),
                  piz2 = make_float2(pi.z, pi.z);
     const float2 lo22 = make_float2(lo2, lo2), hi22 = make_float2(hi2, hi2);
@@ -226,7 +236,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           gz0 = valid ? pi.z : 3.4e38f;
     float gx1 = valid ? pi.x : -3.4e38f, gy1 = valid ? pi.y : -3.4e38f,
           gz1 = valid ? pi.z : -3.4e38f;
-    float gh2 = hig2;
+    float gh2 = cr2;
     int gd0 = valid ? dh : 1 << 20, gd1 = valid ? dh : -(1 << 20);  // depth range
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -389,7 +399,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           const float dx = fmaxf(fmaxf(slo.x - px, px - shi.x), 0.f);
           const float dy = fmaxf(fmaxf(slo.y - py, py - shi.y), 0.f);
           const float dz = fmaxf(fmaxf(slo.z - pz, pz - shi.z), 0.f);
-          const float R2 = FORCE ? fmaxf(hig2, slo.w) : hig2;
+          const float R2 = FORCE ? fmaxf(hig2, slo.w) : cr2;
           mine = dx * dx + dy * dy + dz * dz < R2 * (1.f + 4.f * band) + 1e-30f;
         }
         if (!__any_sync(FULL, mine)) continue;
@@ -416,7 +426,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         // frame (rare: the warp votes once per chunk).
         auto cidx = [&](int t0, int u) { return t0 + 2 * TPP * (u >> 1) + 2 * sub + (u & 1); };
         for (int t0 = 0; t0 < bcount; t0 += 8 * TPP) {
-          unsigned hm = 0u, cm = 0u;
+          unsigned hm = 0u, cm = 0u, wm = 0u;
 #pragma unroll
           for (int v = 0; v < 4; v++) {
             const int pp = (t0 >> 1) + v * TPP + sub;
@@ -437,6 +447,10 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
             if (r2.y < L2.y) hm |= 2u << (2 * v);
             if (r2.x < U2.x) cm |= 1u << (2 * v);
             if (r2.y < U2.y) cm |= 2u << (2 * v);
+            if (LISTS) {
+              if (r2.x < lw2) wm |= 1u << (2 * v);
+              if (r2.y < lw2) wm |= 2u << (2 * v);
+            }
           }
           unsigned bm = cm & ~hm;
           // this lane's candidates in the block come first in bit order
@@ -451,7 +465,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           bm &= live;
           if (LISTS) {
             // items go to the lane's row of the list 8 at a time (32 bytes)
-            unsigned lm = hm | bm;
+            unsigned lm = wm & live;
             while (lm) {
               const int u = __ffs(lm) - 1;
               lm &= lm - 1u;
@@ -511,7 +525,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     if (!valid || sub != 0) continue;
     if (LISTS) {
       a.nl_cnt[i] = lcnt <= segcap && lc1 <= segcap ? (lcnt | lc1 << 16) : -1;
-      a.nl_T[i] = hi2;
+      a.nl_T[i] = lw2;
     }
     if (OUT == OUT_CALLER) {
       const size_t k = (size_t)co.perm[i];

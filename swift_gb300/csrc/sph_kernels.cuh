@@ -76,6 +76,12 @@ struct G2Args {
                                 // segment overflowed
   float* nl_T;                  // the r^2 bound the items were recorded under
   int nl_cap;
+  // lists recorded by the first density pass cover a wider radius than the
+  // pass's own: r^2 below min(nl_widen (gamma h)^2 (1 + band), the square of
+  // the smallest width of the particle's depth_h cell) -- every particle
+  // closer than that width lies in a cell the recursion pairs at that depth
+  float nl_widen;
+  const LeafInfo* leaves;       // for that width (lists only)
 };
 
 // Later re-runs from the lists: particles whose list covers their new

@@ -107,7 +107,8 @@ struct sphgpu_space {
   DBuf<float> v_stage, m_stage, h_stage, u_stage, out_stage;
   // The batched step is one CUDA graph (density first pass, ghost rounds,
   // force); event-record nodes inside it time each loop of every step.
-  cudaGraphExec_t graph[1] = {nullptr};
+  // graph[0]: density + the first kGraphRounds ghost rounds; graph[1]: force
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double plan_ms = 0;  // host planning inside steps (force re-plans)
   double act_plan_ms = 0, act_upload_ms = 0;  // sphgpu_set_active
@@ -478,8 +479,14 @@ GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
 // round sent none (gates on the redo counts).
 bool lists_on(const sphgpu_space* s) { return s->lists && s->tune.rerun_lists; }
 
-void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st) {
-  for (int k = 0; k < s->prm.max_iter; k++) {
+// The step graph holds the first kGraphRounds ghost rounds (h converges in
+// 2-4 for almost every particle); the rare later ones run outside it, only
+// when particles are left.
+constexpr int kGraphRounds = 8;
+
+void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st, int k0 = 0, int k1 = -1) {
+  if (k1 < 0) k1 = s->prm.max_iter;
+  for (int k = k0; k < k1; k++) {
     CK(launch_ghost(ghargs(s, k, 0, s->P.n), st));
     if (!lists_on(s)) {
       enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k);
@@ -823,17 +830,27 @@ int sphgpu_step(sphgpu_space* s, int32_t stages, void* stream) {
       return SPHGPU_OK;
     }
     s->h_stale = true;
-    if (!s->graph[0])
+    const int rounds = std::min(kGraphRounds, s->prm.max_iter);
+    if (!s->graph[0]) {
       s->graph[0] = capture(st, [&]() {
         // external event-record nodes: the events can be timed from the host
         enqueue_density(s, st, true);
         CK(cudaEventRecordWithFlags(s->ev[1], st, cudaEventRecordExternal));
-        enqueue_ghost_rounds(s, st);
-        CK(cudaEventRecordWithFlags(s->ev[2], st, cudaEventRecordExternal));
-        enqueue_force(s, st);
+        enqueue_ghost_rounds(s, st, 0, rounds);
       });
+      s->graph[1] = capture(st, [&]() { enqueue_force(s, st); });
+    }
     CK(cudaEventRecord(s->ev[0], st));
     CK(cudaGraphLaunch(s->graph[0], st));
+    if (rounds < s->prm.max_iter) {
+      // particles still iterating after the graph's rounds: the rest here
+      int left = 0;
+      CK(cudaMemcpyAsync(&left, s->redo.p + rounds - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      if (left > 0) enqueue_ghost_rounds(s, st, rounds, s->prm.max_iter);
+    }
+    CK(cudaEventRecord(s->ev[2], st));
+    CK(cudaGraphLaunch(s->graph[1], st));
     CK(cudaEventRecord(s->ev[3], st));
     const int rc = check_conv(s, st);  // synchronises the stream
     for (int k = 0; k < 3; k++) {

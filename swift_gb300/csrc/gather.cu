@@ -91,7 +91,7 @@ cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
 }
 
 cudaError_t launch_redo_from_lists(const ListArgs& a, cudaStream_t s) {
-  long long g = ((long long)a.p.n * 8 + 255) / 256;  // eight lanes per particle
+  long long g = ((long long)a.p.n * 4 + 255) / 256;  // four lanes per particle
   g = std::max(1LL, std::min(g, 152LL * 16));
   redo_from_lists<<<(int)g, 256, 0, s>>>(a);
   return cudaGetLastError();

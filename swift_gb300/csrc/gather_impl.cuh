@@ -612,11 +612,11 @@ static __device__ const Entry* rerun_entry(const ListArgs& a, int leaf, int b, i
   return nullptr;
 }
 
-// Eight lanes per particle: lane k of a particle takes items k, k + 8, ...
-// of its list (a particle's row is read 32 bytes at a time), and the lanes
+// Four lanes per particle: lane k of a particle takes items k, k + 4, ...
+// of its list (a particle's row is read 16 bytes at a time), and the lanes
 // add their partial sums at the end (fixed order: deterministic).
-static __global__ void __launch_bounds__(256, 3) redo_from_lists(ListArgs a) {
-  constexpr int LPP = 8;  // lanes per particle
+static __global__ void __launch_bounds__(256, 4) redo_from_lists(ListArgs a) {
+  constexpr int LPP = 4;  // lanes per particle
   if (a.gate && *a.gate == 0) return;
   const DevParticles& P = a.p;
   __shared__ float4 ftab[27];  // frame offsets by index (offset_of)
@@ -658,24 +658,24 @@ static __global__ void __launch_bounds__(256, 3) redo_from_lists(ListArgs a) {
       const float4 vi = P.velm[i];
       const float hi_inv = 1.f / pi.w;
       const int* row = a.nl + (size_t)i * a.nl_cap;
-      // four items per lane at a time, their loads all in flight together; a
+      // three items per lane at a time, their loads all in flight together; a
       // miss is evaluated too, at a distance beyond the kernel's support
       // (zero contributions), so the lanes do not diverge
-      for (int t0 = sub; t0 < cnt; t0 += 4 * LPP) {
-        int pk[4];
-        float4 q[4], vm[4];
+      for (int t0 = sub; t0 < cnt; t0 += 3 * LPP) {
+        int pk[3];
+        float4 q[3], vm[3];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
+        for (int u = 0; u < 3; u++) {
           const int t = t0 + u * LPP;
           pk[u] = t < cnt ? row[t < c0 ? t : t - c0 + a.nl_cap / 2] : i;
         }
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
+        for (int u = 0; u < 3; u++) {
           q[u] = P.posh[pk[u] & 0x07ffffff];
           vm[u] = P.velm[pk[u] & 0x07ffffff];
         }
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
+        for (int u = 0; u < 3; u++) {
           const int j = pk[u] & 0x07ffffff;
           const float4 fd = ftab[(unsigned)pk[u] >> 27];
           const float dx = pi.x - (q[u].x + fd.x), dy = pi.y - (q[u].y + fd.y),

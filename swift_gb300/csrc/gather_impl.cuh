@@ -668,6 +668,9 @@ static __global__ void __launch_bounds__(256, 4) redo_from_lists(ListArgs a) {
         for (int u = 0; u < 3; u++) {
           const int t = t0 + u * LPP;
           pk[u] = t < cnt ? row[t < c0 ? t : t - c0 + a.nl_cap / 2] : i;
+          // an item always names a particle of the store; a corrupt row is
+          // read as a miss rather than followed out of bounds
+          if ((pk[u] & 0x07ffffff) >= P.n || ((unsigned)pk[u] >> 27) > 26) pk[u] = i;
         }
 #pragma unroll
         for (int u = 0; u < 3; u++) {

@@ -206,6 +206,22 @@ int sphgpu_step_host(sphgpu_space *s, const double *x, const float *v,
                      const float *m, const float *h, const float *u,
                      float *fields, void *stream);
 
+/* Pipelined form of sphgpu_step_host for a stream of steps: enqueues the
+ * copies in (on an upload stream), the step and the copies out (on a
+ * download stream) and returns; a step's inputs go up while the previous
+ * step computes, and its results come down while the next one does.  At
+ * most two steps are in flight: a call first waits for the step issued two
+ * calls earlier.  A step's `fields` (required) and input buffers must stay
+ * valid, and its results are complete, once a later call has waited for it
+ * or sphgpu_step_host_wait returns; input differences and non-convergence
+ * are reported there (by the call that waits for that step).  Pinned host
+ * buffers make the copies asynchronous. */
+int sphgpu_step_host_async(sphgpu_space *s, const double *x, const float *v,
+                           const float *m, const float *h, const float *u,
+                           float *fields);
+/* Wait for every step issued by sphgpu_step_host_async. */
+int sphgpu_step_host_wait(sphgpu_space *s);
+
 /* Plain form: the same pass issued task by task as the reference's runner
  * would (one launch per self/pair task and loop, one ghost per top cell). */
 int sphgpu_step_plain(sphgpu_space *s, void *stream);

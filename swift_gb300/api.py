@@ -90,6 +90,8 @@ SIGNATURES = {
     "sphgpu_step": (ctypes.c_int, [_P, _I32, _P]),
     "sphgpu_step_host": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "sphgpu_step_plain": (ctypes.c_int, [_P, _P]),
+    "sphgpu_step_host_async": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "sphgpu_step_host_wait": (ctypes.c_int, [_P]),
     "sphgpu_download": (ctypes.c_int, [_P, _P, _P]),
     "sphgpu_force_from_state": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "sphgpu_download_min_ngb_bin": (ctypes.c_int, [_P, _P]),
@@ -321,6 +323,19 @@ class Space:
                                       _ptr(b["m"]), _ptr(b["h"]), _ptr(b["u"]),
                                       _ptr(fields), stream))
         return fields
+
+    def step_host_async(self, box, fields):
+        """Pipelined step through host buffers (sphgpu_step_host_async):
+        ``box`` arrays and ``fields`` must stay alive until step_host_wait
+        (or two calls later); pinned buffers make the copies overlap."""
+        b = {k: box[k] for k in ("x", "v", "m", "h", "u")}
+        _check(lib().sphgpu_step_host_async(self._h, _ptr(b["x"]), _ptr(b["v"]),
+                                            _ptr(b["m"]), _ptr(b["h"]), _ptr(b["u"]),
+                                            _ptr(fields)))
+        return fields
+
+    def step_host_wait(self):
+        _check(lib().sphgpu_step_host_wait(self._h))
 
     def host_times(self, reset=False):
         """Host planning in ms: activation lists, activation uploads, force

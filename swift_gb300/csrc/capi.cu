@@ -126,11 +126,33 @@ struct sphgpu_space {
   std::vector<int> split_begin, split_n;  // per depth, into sort_split_ids
   int sort_nleaves = 0, sort_max_depth = 0, sorted_mask = 0;
 
+  // Pipelined host steps (sphgpu_step_host_async): two slots of staging
+  // buffers; a slot's inputs go up on `cin`, its results come down on `cout`
+  // while the next step computes.
+  struct AsyncSlot {
+    DBuf<double> x;
+    DBuf<float> v, m, h, u, out;
+    DBuf<int> dflags;                 // [0] inputs differ, [1] unconverged
+    int* hflags = nullptr;            // pinned copy of dflags
+    cudaEvent_t in_done = nullptr, comp_done = nullptr, out_done = nullptr;
+    bool busy = false;
+  } slot[2];
+  cudaStream_t cin = nullptr, cout = nullptr;
+  int64_t async_k = 0;
+
   ~sphgpu_space() {
+    for (auto& sl : slot) {
+      if (sl.out_done) cudaEventSynchronize(sl.out_done);
+      for (cudaEvent_t e : {sl.in_done, sl.comp_done, sl.out_done})
+        if (e) cudaEventDestroy(e);
+      if (sl.hflags) cudaFreeHost(sl.hflags);
+    }
     for (auto& g : graph)
       if (g) cudaGraphExecDestroy(g);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
+    if (cin) cudaStreamDestroy(cin);
+    if (cout) cudaStreamDestroy(cout);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -785,6 +807,38 @@ int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
   });
 }
 
+namespace {
+// A planned step: graph[0] (density + the first rounds), the rare later
+// rounds (a host check of the round counter, only when the graph's rounds
+// did not finish the ghost), graph[1] (force).  Events ev[0..3] bracket the
+// phases; nothing waits for the force.
+void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
+  s->h_stale = true;
+  const int rounds = std::min(kGraphRounds, s->prm.max_iter);
+  if (!s->graph[0]) {
+    s->graph[0] = capture(st, [&]() {
+      // external event-record nodes: the events can be timed from the host
+      enqueue_density(s, st, true);
+      CK(cudaEventRecordWithFlags(s->ev[1], st, cudaEventRecordExternal));
+      enqueue_ghost_rounds(s, st, 0, rounds);
+    });
+    s->graph[1] = capture(st, [&]() { enqueue_force(s, st); });
+  }
+  CK(cudaEventRecord(s->ev[0], st));
+  CK(cudaGraphLaunch(s->graph[0], st));
+  if (rounds < s->prm.max_iter) {
+    // particles still iterating after the graph's rounds: the rest here
+    int left = 0;
+    CK(cudaMemcpyAsync(&left, s->redo.p + rounds - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (left > 0) enqueue_ghost_rounds(s, st, rounds, s->prm.max_iter);
+  }
+  CK(cudaEventRecord(s->ev[2], st));
+  CK(cudaGraphLaunch(s->graph[1], st));
+  CK(cudaEventRecord(s->ev[3], st));
+}
+}  // namespace
+
 int sphgpu_step(sphgpu_space* s, int32_t stages, void* stream) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   if (stages <= 0 || stages > SPHGPU_STAGE_ALL)
@@ -829,29 +883,7 @@ int sphgpu_step(sphgpu_space* s, int32_t stages, void* stream) {
       s->phase_steps++;
       return SPHGPU_OK;
     }
-    s->h_stale = true;
-    const int rounds = std::min(kGraphRounds, s->prm.max_iter);
-    if (!s->graph[0]) {
-      s->graph[0] = capture(st, [&]() {
-        // external event-record nodes: the events can be timed from the host
-        enqueue_density(s, st, true);
-        CK(cudaEventRecordWithFlags(s->ev[1], st, cudaEventRecordExternal));
-        enqueue_ghost_rounds(s, st, 0, rounds);
-      });
-      s->graph[1] = capture(st, [&]() { enqueue_force(s, st); });
-    }
-    CK(cudaEventRecord(s->ev[0], st));
-    CK(cudaGraphLaunch(s->graph[0], st));
-    if (rounds < s->prm.max_iter) {
-      // particles still iterating after the graph's rounds: the rest here
-      int left = 0;
-      CK(cudaMemcpyAsync(&left, s->redo.p + rounds - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      if (left > 0) enqueue_ghost_rounds(s, st, rounds, s->prm.max_iter);
-    }
-    CK(cudaEventRecord(s->ev[2], st));
-    CK(cudaGraphLaunch(s->graph[1], st));
-    CK(cudaEventRecord(s->ev[3], st));
+    run_step_graphs(s, st);
     const int rc = check_conv(s, st);  // synchronises the stream
     for (int k = 0; k < 3; k++) {
       float ms = 0.f;
@@ -947,6 +979,100 @@ int sphgpu_step_host(sphgpu_space* s, const double* x, const float* v,
     }
     if (rc == SPHGPU_ENOCONV) return fail(rc, g_err);
     return SPHGPU_OK;
+  });
+}
+
+namespace {
+// Wait for a slot's step to come back: its results are in the caller's
+// buffer, and its status is read.
+int finish_slot(sphgpu_space* s, int b) {
+  auto& S = s->slot[b];
+  if (!S.busy) return SPHGPU_OK;
+  CK(cudaEventSynchronize(S.out_done));
+  S.busy = false;
+  if (S.hflags[0])
+    return fail(SPHGPU_EINVAL,
+                "sphgpu_step_host_async: positions or smoothing lengths differ from the "
+                "space's; create a new space");
+  if (S.hflags[1] > 0)
+    return fail(SPHGPU_ENOCONV, "smoothing length failed to converge on " +
+                                    std::to_string(S.hflags[1]) + " particles");
+  return SPHGPU_OK;
+}
+}  // namespace
+
+int sphgpu_step_host_async(sphgpu_space* s, const double* x, const float* v, const float* m,
+                           const float* h, const float* u, float* fields) {
+  if (!s || !x || !v || !m || !h || !u || !fields) return fail(SPHGPU_EINVAL, "null argument");
+  return guard([&]() {
+    ensure_device(s);
+    if (!s->force_planned) {
+      // the first step plans the force lists on the host: run it whole
+      int rc = sphgpu_step_host_wait(s);
+      if (rc != SPHGPU_OK) return rc;
+      return sphgpu_step_host(s, x, v, m, h, u, fields, nullptr);
+    }
+    const int n = s->P.n;
+    if (!s->cin) {
+      CK(cudaStreamCreateWithFlags(&s->cin, cudaStreamNonBlocking));
+      CK(cudaStreamCreateWithFlags(&s->cout, cudaStreamNonBlocking));
+      for (auto& S : s->slot) {
+        S.x.alloc(3 * (size_t)n);
+        S.v.alloc(3 * (size_t)n);
+        S.m.alloc(n);
+        S.h.alloc(n);
+        S.u.alloc(n);
+        S.out.alloc(24 * (size_t)n);
+        S.dflags.alloc(2);
+        CK(cudaMallocHost(&S.hflags, 2 * sizeof(int)));
+        for (cudaEvent_t* e : {&S.in_done, &S.comp_done, &S.out_done})
+          CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+      }
+      if (!s->x_ref.p) s->x_ref.upload(s->x_in.data(), s->x_in.size(), s->stream);
+    }
+    const int b = (int)(s->async_k & 1);
+    auto& S = s->slot[b];
+    // the step that used this slot two calls ago must be back first
+    int rc = finish_slot(s, b);
+    if (rc != SPHGPU_OK) return rc;
+    // inputs up (overlaps the previous step's compute)
+    CK(cudaMemcpyAsync(S.x.p, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->cin));
+    CK(cudaMemcpyAsync(S.v.p, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->cin));
+    CK(cudaMemcpyAsync(S.m.p, m, sizeof(float) * n, cudaMemcpyHostToDevice, s->cin));
+    CK(cudaMemcpyAsync(S.h.p, h, sizeof(float) * n, cudaMemcpyHostToDevice, s->cin));
+    CK(cudaMemcpyAsync(S.u.p, u, sizeof(float) * n, cudaMemcpyHostToDevice, s->cin));
+    CK(cudaEventRecord(S.in_done, s->cin));
+    // the step
+    cudaStream_t st = s->stream;
+    CK(cudaStreamWaitEvent(st, S.in_done, 0));
+    CK(cudaMemsetAsync(S.dflags.p, 0, 2 * sizeof(int), st));
+    CK(launch_permute_in(s->P, s->perm.p, S.x.p, s->x_ref.p, S.v.p, S.m.p, S.h.p, S.u.p,
+                         S.dflags.p, st));
+    run_step_graphs(s, st);
+    CK(cudaMemcpyAsync(S.dflags.p + 1, s->redo.p + s->prm.max_iter - 1, sizeof(int),
+                       cudaMemcpyDeviceToDevice, st));
+    CK(launch_collect_out(s->P, s->perm.p, S.out.p, nullptr, st));
+    CK(cudaEventRecord(S.comp_done, st));
+    // results down (overlaps the next step)
+    CK(cudaStreamWaitEvent(s->cout, S.comp_done, 0));
+    CK(cudaMemcpyAsync(fields, S.out.p, sizeof(float) * 24 * (size_t)n, cudaMemcpyDeviceToHost,
+                       s->cout));
+    CK(cudaMemcpyAsync(S.hflags, S.dflags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s->cout));
+    CK(cudaEventRecord(S.out_done, s->cout));
+    S.busy = true;
+    s->async_k++;
+    return SPHGPU_OK;
+  });
+}
+
+int sphgpu_step_host_wait(sphgpu_space* s) {
+  if (!s) return fail(SPHGPU_EINVAL, "null argument");
+  return guard([&]() {
+    // oldest first
+    const int b0 = (int)(s->async_k & 1);
+    int rc = finish_slot(s, b0);
+    const int rc1 = finish_slot(s, 1 - b0);
+    return rc != SPHGPU_OK ? rc : rc1;
   });
 }
 

@@ -184,6 +184,39 @@ def test_step_host_matches_resident_step_and_checks_inputs():
             sp.step_host(grown, fields)
 
 
+def test_step_host_async_pipeline_matches_step_host():
+    """The pipelined host-buffer step: three steps in flight two at a time
+    give, bit for bit, the results of the synchronous call on the same
+    inputs; a position change is reported when its step is waited for."""
+    box = ics.make("clustered:20", seed=3)
+    n = box["x"].shape[0]
+    boxes = []
+    for k in range(3):
+        b = {key: np.ascontiguousarray(box[key]) for key in ("x", "v", "m", "h", "u")}
+        b["v"] = (box["v"] * (1.0 + 0.5 * k)).astype(np.float32)
+        boxes.append(b)
+    with api.Space(box) as sp:
+        sp.step()
+        sync = []
+        for b in boxes:
+            f = np.zeros((n, 24), np.float32)
+            sp.step_host(b, f)
+            sync.append(f)
+        outs = [np.zeros((n, 24), np.float32) for _ in boxes]
+        for b, f in zip(boxes, outs):
+            sp.step_host_async(b, f)
+        sp.step_host_wait()
+        for k in range(3):
+            assert np.array_equal(outs[k].view(np.uint32), sync[k].view(np.uint32)), k
+        moved = dict(boxes[0])
+        moved["x"] = boxes[0]["x"].copy()
+        moved["x"][5, 1] += 1e-3
+        f = np.zeros((n, 24), np.float32)
+        sp.step_host_async(moved, f)
+        with pytest.raises(api.SphGpuError):
+            sp.step_host_wait()
+
+
 # --- open boxes and tiny inputs --------------------------------------------
 
 @pytest.mark.parametrize("cfg,run", [("lattice:16", {"periodic": 0}),

@@ -476,6 +476,9 @@ ListArgs largs(sphgpu_space* s, const int* gate) {
   l.band = kBand;
   l.gate = gate;
   l.hits = s->count_hits ? s->hit_ctr.p + 1 : nullptr;
+  l.bb_lo = s->bb_lo.p;
+  l.bb_hi = s->bb_hi.p;
+  l.bb_fc = s->bb_fc.p;
   return l;
 }
 
@@ -508,6 +511,15 @@ constexpr int kGraphRounds = 8;
 
 void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st, int k0 = 0, int k1 = -1) {
   if (k1 < 0) k1 = s->prm.max_iter;
+  if (lists_on(s)) {
+    // round 0, then every later round particle by particle from the lists
+    if (k0 == 0) {
+      CK(launch_ghost(ghargs(s, 0, 0, s->P.n), st));
+      CK(launch_solve_from_lists(largs(s, s->redo.p), ghargs(s, 1, 0, s->P.n),
+                                 s->prm.max_iter, st));
+    }
+    return;
+  }
   for (int k = k0; k < k1; k++) {
     CK(launch_ghost(ghargs(s, k, 0, s->P.n), st));
     if (!lists_on(s)) {
@@ -814,7 +826,8 @@ namespace {
 // phases; nothing waits for the force.
 void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
   s->h_stale = true;
-  const int rounds = std::min(kGraphRounds, s->prm.max_iter);
+  // with the list solver the graph holds every round
+  const int rounds = lists_on(s) ? s->prm.max_iter : std::min(kGraphRounds, s->prm.max_iter);
   if (!s->graph[0]) {
     s->graph[0] = capture(st, [&]() {
       // external event-record nodes: the events can be timed from the host

@@ -97,6 +97,14 @@ cudaError_t launch_redo_from_lists(const ListArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_solve_from_lists(const ListArgs& a, const GhostArgs& g, int max_iter,
+                                    cudaStream_t s) {
+  long long grid = ((long long)a.p.n * 4 + 255) / 256;  // four lanes per particle
+  grid = grid < 1 ? 1 : (grid > 152LL * 16 ? 152LL * 16 : grid);
+  solve_from_lists<<<(int)grid, 256, 0, s>>>(a, g, max_iter);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_block_hmax(const int2* fc, float4* lo, const float4* posh,
                               int nblocks, cudaStream_t s) {
   int g = (nblocks + 255) / 256;

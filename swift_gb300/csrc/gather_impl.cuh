@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "ghost_impl.cuh"
 #include "sph_kernels.cuh"
 
 namespace sphgpu {
@@ -718,5 +719,157 @@ static __global__ void __launch_bounds__(256, 4) redo_from_lists(ListArgs a) {
     }
   }
 }
+
+// Density sums of particle i at its current h from the j-blocks of its
+// leaf's re-run candidate list (the gather's decisions: FP32 r^2 in the
+// entry's frame, the exact predicate inside the band); lane `sub` of `lpp`
+// takes every lpp-th candidate block.  For the few particles whose h outgrew
+// their list.
+static __device__ void sums_from_blocks(const ListArgs& a, int i, int sub, int lpp, float4 pi,
+                                        float4 vi, float hi_inv, float hig2, float L2, float U2,
+                                        float& s0, float& s1, float& s2, float& s3, float& s4,
+                                        float& s5, float& s6, float& s7, int& ngb) {
+  const DevParticles& P = a.p;
+  const int leaf = P.leaf_of[i];
+  const int dh = P.depth_h[i];
+  const float R2 = hig2 * (1.f + 4.f * a.band) + 1e-30f;
+  for (int p = a.leaf_pair_begin[leaf] + sub; p < a.leaf_pair_begin[leaf + 1]; p += lpp) {
+    const Entry* E = &a.entries[a.pair_entry[p]];
+    if (dh < E->min_depth || dh > E->max_depth) continue;
+    const int b = a.pair_block[p];
+    const float4 lo = a.bb_lo[b], hb = a.bb_hi[b];
+    const float px = pi.x - E->fdx, py = pi.y - E->fdy, pz = pi.z - E->fdz;
+    const float bx = fmaxf(fmaxf(lo.x - px, px - hb.x), 0.f);
+    const float by = fmaxf(fmaxf(lo.y - py, py - hb.y), 0.f);
+    const float bz = fmaxf(fmaxf(lo.z - pz, pz - hb.z), 0.f);
+    if (!(bx * bx + by * by + bz * bz < R2)) continue;
+    const int2 fc = a.bb_fc[b];
+    for (int j = fc.x; j < fc.x + fc.y; j++) {
+      if (j == i) continue;
+      const float4 q = P.posh[j];
+      const float dx = pi.x - (q.x + E->fdx), dy = pi.y - (q.y + E->fdy),
+                  dz = pi.z - (q.z + E->fdz);
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      bool hit = r2 < L2;
+      if (!hit && r2 < U2) hit = exact_r2_2(P.xd, i, j, E) < hig2;
+      if (!hit) continue;
+      density_hit(dx, dy, dz, r2, vi, P.velm[j], hi_inv, s0, s1, s2, s3, s4, s5, s6, s7);
+      ngb++;
+    }
+  }
+}
+
+// The ghost's rounds after the first: each particle iterates on its own
+// (its density at h_k depends on nothing that changes during the ghost):
+// the density from its list (the first pass recorded it; four lanes, three
+// partners in flight each, misses evaluated beyond the kernel's support) or,
+// when h_k is beyond the list, from its leaf's re-run candidate blocks; then
+// the Newton update of round k (ghost_update, the round kernel's own code),
+// until it converges or round max_iter - 1 sends it on (non-convergence is
+// counted in redo_count[max_iter - 1]).  Same sums, same updates, in the
+// same order as the rounds one at a time.
+static __global__ void __launch_bounds__(256, 4)
+    solve_from_lists(ListArgs a, GhostArgs g, int max_iter) {
+  constexpr int LPP = 4;
+  const DevParticles& P = a.p;
+  __shared__ float4 ftab[27];
+  if (threadIdx.x < 27) {
+    const float3 o = offset_of(threadIdx.x, a.top_width);
+    ftab[threadIdx.x] = make_float4(o.x, o.y, o.z, 0.f);
+  }
+  __syncthreads();
+  const int sub = threadIdx.x % LPP;
+  const int gl = (threadIdx.x & 31) & ~(LPP - 1);  // the group's first lane
+  const int stride = gridDim.x * blockDim.x / LPP;
+  for (int base = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / LPP; base < P.n;
+       base += stride) {
+    const int i = base + (threadIdx.x & 31) / LPP;
+    bool going = i < P.n && (P.flags[i] & 3) == 3;  // sent on by round 0
+    int cnt = 0, c0 = 0;
+    float T = 0.f;
+    if (going) {
+      cnt = a.nl_cnt[i];
+      T = a.nl_T[i];
+      if (cnt >= 0) {
+        c0 = a.nl_seg == 2 ? (cnt & 0xffff) : cnt;
+        cnt = c0 + (a.nl_seg == 2 ? cnt >> 16 : 0);
+      }
+    }
+    const int* row = a.nl + (size_t)(i < P.n ? i : 0) * a.nl_cap;
+    for (int it = 1; it < max_iter && __any_sync(FULL, going); it++) {
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f, s5 = 0.f, s6 = 0.f, s7 = 0.f;
+      int ngb = 0;
+      if (going) {
+        const float4 pi = P.posh[i];
+        const float4 vi = P.velm[i];
+        const float hig2 = h2_exact(pi.w);
+        const float L2 = hig2 * (1.f - a.band), U2 = hig2 * (1.f + a.band);
+        const float hi_inv = 1.f / pi.w;
+        if (cnt >= 0 && U2 <= T) {
+          for (int t0 = sub; t0 < cnt; t0 += 3 * LPP) {
+            int pk[3];
+            float4 q[3], vm[3];
+#pragma unroll
+            for (int u = 0; u < 3; u++) {
+              const int t = t0 + u * LPP;
+              pk[u] = t < cnt ? row[t < c0 ? t : t - c0 + a.nl_cap / 2] : i;
+              if ((pk[u] & 0x07ffffff) >= P.n || ((unsigned)pk[u] >> 27) > 26) pk[u] = i;
+            }
+#pragma unroll
+            for (int u = 0; u < 3; u++) {
+              q[u] = P.posh[pk[u] & 0x07ffffff];
+              vm[u] = P.velm[pk[u] & 0x07ffffff];
+            }
+#pragma unroll
+            for (int u = 0; u < 3; u++) {
+              const int j = pk[u] & 0x07ffffff;
+              const float4 fd = ftab[(unsigned)pk[u] >> 27];
+              const float dx = pi.x - (q[u].x + fd.x), dy = pi.y - (q[u].y + fd.y),
+                          dz = pi.z - (q[u].z + fd.z);
+              const float r2 = dx * dx + dy * dy + dz * dz;
+              const bool item = t0 + u * LPP < cnt;
+              bool hit = item && r2 < L2;
+              if (item && !hit && r2 < U2) {
+                const Entry* E = rerun_entry(a, P.leaf_of[i], a.blk_of[j], P.depth_h[i]);
+                hit = E != nullptr && exact_r2_2(P.xd, i, j, E) < hig2;
+              }
+              density_hit(dx, dy, dz, hit ? r2 : 4.f * U2, vi, vm[u], hi_inv, s0, s1, s2, s3, s4,
+                          s5, s6, s7);
+              ngb += hit;
+            }
+          }
+        } else {
+          sums_from_blocks(a, i, sub, LPP, pi, vi, hi_inv, hig2, L2, U2, s0, s1, s2, s3, s4, s5,
+                           s6, s7, ngb);
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < LPP; o <<= 1) {
+        s0 += __shfl_xor_sync(FULL, s0, o);
+        s1 += __shfl_xor_sync(FULL, s1, o);
+        s2 += __shfl_xor_sync(FULL, s2, o);
+        s3 += __shfl_xor_sync(FULL, s3, o);
+        s4 += __shfl_xor_sync(FULL, s4, o);
+        s5 += __shfl_xor_sync(FULL, s5, o);
+        s6 += __shfl_xor_sync(FULL, s6, o);
+        s7 += __shfl_xor_sync(FULL, s7, o);
+        ngb += __shfl_xor_sync(FULL, ngb, o);
+      }
+      int more = 0;
+      if (going && sub == 0) {
+        const float4 d0 = make_float4(s0, s1, s2, s3), d1 = make_float4(s4, s5, s6, s7);
+        P.dens0[i] = d0;
+        P.dens1[i] = d1;
+        P.ngb_d[i] = ngb;
+        if (a.hits) atomicAdd(a.hits, (unsigned long long)ngb);
+        more = ghost_update(g, i, it, d0, d1);
+      }
+      more = __shfl_sync(FULL, more, gl);
+      going = going && more;
+      __syncwarp();  // the new h (posh.w) is read by the group's lanes next round
+    }
+  }
+}
+
 
 }  // namespace sphgpu

@@ -105,6 +105,11 @@ struct ListArgs {
   float band;
   const int* gate;              // do nothing when *gate == 0
   unsigned long long* hits;     // optional: total neighbour hits
+  // j-block boxes and ranges (the solver's gather for a particle whose h
+  // outgrew its list)
+  const float4* bb_lo;
+  const float4* bb_hi;
+  const int2* bb_fc;
 };
 
 struct GhostArgs {
@@ -129,6 +134,12 @@ cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                int need, int veto, const int* leaf_pair_begin,
                                int4* units, const int* gate, cudaStream_t s, int win = 32);
 cudaError_t launch_redo_from_lists(const ListArgs& a, cudaStream_t s);
+// The ghost's rounds 1.. max_iter - 1 for every particle still iterating
+// after round 0, each particle on its own: density from its list (or, where
+// its h outgrew the list, from its leaf's re-run candidate blocks), then the
+// Newton update, until it converges.
+cudaError_t launch_solve_from_lists(const ListArgs& a, const GhostArgs& g, int max_iter,
+                                    cudaStream_t s);
 int noalloc_max_particles();
 int noalloc_max_units();
 cudaError_t launch_density_noalloc(const G2Args& base, const LeafInfo* leaves,

@@ -653,9 +653,10 @@ def run_ours(args):
             # (ghost, units, re-run gather, and the list kernel after the
             # first; gated ones return at once), block h_max, force units +
             # gather
-            # per step: begin-step, density (units + gather), 8 ghost rounds in the
-            # graph (ghost, list re-run, units, gather), force (h_max, units, gather)
-            "gpu_launches": (6 + 8 * (4 if tuning.get("rerun_lists") else 3)) * args.steps,
+            # per step: begin-step, density (units + gather), then with the lists
+            # ghost round 0 + the per-particle solver, else 8 rounds in the graph
+            # (ghost, units, gather); force (h_max, units, gather)
+            "gpu_launches": (6 + (2 if tuning.get("rerun_lists") else 8 * 3)) * args.steps,
             "clocks": clk,
             "cpu_baseline": cb,
         }

@@ -47,6 +47,9 @@ struct sphgpu_space {
   std::vector<float> v_in, m_in, h_in, u_in;
   std::vector<int8_t> tb_in;
   DBuf<int8_t> tbin, ngb_bin;  // store order: time bins, neighbours' smallest bin
+  // list solver: [0] particles handed to the catch-up rounds, [r + 1] those
+  // catch-up round r sends on
+  DBuf<int> catchup;
   sphgpu_tuning tune{1, SPH_JBLOCK, 1, 8};
 
   // host plans
@@ -325,6 +328,7 @@ void ensure_device(sphgpu_space* s) {
   s->ngb_f.alloc(n);
   s->queue.alloc(16);  // [0..7] work counters, [8..15] unit counts
   s->redo.alloc(std::max(1, s->prm.max_iter));
+  s->catchup.alloc(s->prm.max_iter + 1);
   s->hit_ctr.alloc(4);
   {
     size_t fr = 0, tot = 0;
@@ -476,9 +480,7 @@ ListArgs largs(sphgpu_space* s, const int* gate) {
   l.band = kBand;
   l.gate = gate;
   l.hits = s->count_hits ? s->hit_ctr.p + 1 : nullptr;
-  l.bb_lo = s->bb_lo.p;
-  l.bb_hi = s->bb_hi.p;
-  l.bb_fc = s->bb_fc.p;
+  l.handover = s->catchup.p;
   return l;
 }
 
@@ -512,11 +514,19 @@ constexpr int kGraphRounds = 8;
 void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st, int k0 = 0, int k1 = -1) {
   if (k1 < 0) k1 = s->prm.max_iter;
   if (lists_on(s)) {
-    // round 0, then every later round particle by particle from the lists
+    // round 0, then the later rounds particle by particle from the lists;
+    // the particles whose h outgrew their list catch up by gathers, each at
+    // its own round count (catch-up rounds k0 .. k1 - 1)
     if (k0 == 0) {
       CK(launch_ghost(ghargs(s, 0, 0, s->P.n), st));
+      CK(cudaMemsetAsync(s->catchup.p, 0, sizeof(int) * (s->prm.max_iter + 1), st));
       CK(launch_solve_from_lists(largs(s, s->redo.p), ghargs(s, 1, 0, s->P.n),
                                  s->prm.max_iter, st));
+    }
+    for (int r = k0; r < k1 && r < s->prm.max_iter; r++) {
+      enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->catchup.p + r);
+      CK(launch_ghost_catchup(ghargs(s, 0, 0, s->P.n), s->prm.max_iter, s->catchup.p + r,
+                              s->catchup.p + r + 1, st));
     }
     return;
   }
@@ -826,8 +836,7 @@ namespace {
 // phases; nothing waits for the force.
 void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
   s->h_stale = true;
-  // with the list solver the graph holds every round
-  const int rounds = lists_on(s) ? s->prm.max_iter : std::min(kGraphRounds, s->prm.max_iter);
+  const int rounds = std::min(kGraphRounds, s->prm.max_iter);
   if (!s->graph[0]) {
     s->graph[0] = capture(st, [&]() {
       // external event-record nodes: the events can be timed from the host
@@ -842,7 +851,8 @@ void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
   if (rounds < s->prm.max_iter) {
     // particles still iterating after the graph's rounds: the rest here
     int left = 0;
-    CK(cudaMemcpyAsync(&left, s->redo.p + rounds - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    const int* cnt = lists_on(s) ? s->catchup.p + rounds : s->redo.p + rounds - 1;
+    CK(cudaMemcpyAsync(&left, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (left > 0) enqueue_ghost_rounds(s, st, rounds, s->prm.max_iter);
   }

@@ -720,54 +720,16 @@ static __global__ void __launch_bounds__(256, 4) redo_from_lists(ListArgs a) {
   }
 }
 
-// Density sums of particle i at its current h from the j-blocks of its
-// leaf's re-run candidate list (the gather's decisions: FP32 r^2 in the
-// entry's frame, the exact predicate inside the band); lane `sub` of `lpp`
-// takes every lpp-th candidate block.  For the few particles whose h outgrew
-// their list.
-static __device__ void sums_from_blocks(const ListArgs& a, int i, int sub, int lpp, float4 pi,
-                                        float4 vi, float hi_inv, float hig2, float L2, float U2,
-                                        float& s0, float& s1, float& s2, float& s3, float& s4,
-                                        float& s5, float& s6, float& s7, int& ngb) {
-  const DevParticles& P = a.p;
-  const int leaf = P.leaf_of[i];
-  const int dh = P.depth_h[i];
-  const float R2 = hig2 * (1.f + 4.f * a.band) + 1e-30f;
-  for (int p = a.leaf_pair_begin[leaf] + sub; p < a.leaf_pair_begin[leaf + 1]; p += lpp) {
-    const Entry* E = &a.entries[a.pair_entry[p]];
-    if (dh < E->min_depth || dh > E->max_depth) continue;
-    const int b = a.pair_block[p];
-    const float4 lo = a.bb_lo[b], hb = a.bb_hi[b];
-    const float px = pi.x - E->fdx, py = pi.y - E->fdy, pz = pi.z - E->fdz;
-    const float bx = fmaxf(fmaxf(lo.x - px, px - hb.x), 0.f);
-    const float by = fmaxf(fmaxf(lo.y - py, py - hb.y), 0.f);
-    const float bz = fmaxf(fmaxf(lo.z - pz, pz - hb.z), 0.f);
-    if (!(bx * bx + by * by + bz * bz < R2)) continue;
-    const int2 fc = a.bb_fc[b];
-    for (int j = fc.x; j < fc.x + fc.y; j++) {
-      if (j == i) continue;
-      const float4 q = P.posh[j];
-      const float dx = pi.x - (q.x + E->fdx), dy = pi.y - (q.y + E->fdy),
-                  dz = pi.z - (q.z + E->fdz);
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      bool hit = r2 < L2;
-      if (!hit && r2 < U2) hit = exact_r2_2(P.xd, i, j, E) < hig2;
-      if (!hit) continue;
-      density_hit(dx, dy, dz, r2, vi, P.velm[j], hi_inv, s0, s1, s2, s3, s4, s5, s6, s7);
-      ngb++;
-    }
-  }
-}
-
 // The ghost's rounds after the first: each particle iterates on its own
 // (its density at h_k depends on nothing that changes during the ghost):
 // the density from its list (the first pass recorded it; four lanes, three
-// partners in flight each, misses evaluated beyond the kernel's support) or,
-// when h_k is beyond the list, from its leaf's re-run candidate blocks; then
-// the Newton update of round k (ghost_update, the round kernel's own code),
-// until it converges or round max_iter - 1 sends it on (non-convergence is
-// counted in redo_count[max_iter - 1]).  Same sums, same updates, in the
-// same order as the rounds one at a time.
+// partners in flight each, misses evaluated beyond the kernel's support),
+// then the Newton update of round k (ghost_update, the round kernel's own
+// code), until it converges or round max_iter - 1 sends it on
+// (non-convergence is counted in redo_count[max_iter - 1]).  A particle
+// whose h_k is beyond its list stops there and is handed to the catch-up
+// rounds (gathers; *a.handover counts them).  Same sums, same updates, in
+// the same order as the rounds one at a time.
 static __global__ void __launch_bounds__(256, 4)
     solve_from_lists(ListArgs a, GhostArgs g, int max_iter) {
   constexpr int LPP = 4;
@@ -805,7 +767,12 @@ static __global__ void __launch_bounds__(256, 4)
         const float hig2 = h2_exact(pi.w);
         const float L2 = hig2 * (1.f - a.band), U2 = hig2 * (1.f + a.band);
         const float hi_inv = 1.f / pi.w;
-        if (cnt >= 0 && U2 <= T) {
+        if (!(cnt >= 0 && U2 <= T)) {
+          // beyond the list: the catch-up rounds take it from here (it keeps
+          // its iteration count in ghost_iters and its flags)
+          going = false;
+          if (sub == 0) atomicAdd(a.handover, 1);
+        } else {
           for (int t0 = sub; t0 < cnt; t0 += 3 * LPP) {
             int pk[3];
             float4 q[3], vm[3];
@@ -838,9 +805,6 @@ static __global__ void __launch_bounds__(256, 4)
               ngb += hit;
             }
           }
-        } else {
-          sums_from_blocks(a, i, sub, LPP, pi, vi, hi_inv, hig2, L2, U2, s0, s1, s2, s3, s4, s5,
-                           s6, s7, ngb);
         }
       }
 #pragma unroll

@@ -163,6 +163,24 @@ static int grid_for(int n) {
   return g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g);
 }
 
+__global__ void ghost_catchup(GhostArgs g, int max_iter, const int* gate, int* sent) {
+  if (*gate == 0) return;
+  const DevParticles& P = g.p;
+  for (int i = g.lo + blockIdx.x * blockDim.x + threadIdx.x; i < g.hi;
+       i += gridDim.x * blockDim.x) {
+    if ((P.flags[i] & 3) != 3) continue;  // active and still iterating
+    const int it = P.ghost_iters[i];        // rounds taken so far
+    if (it >= max_iter) continue;           // gave up: counted as unconverged
+    if (ghost_update(g, i, it, P.dens0[i], P.dens1[i])) atomicAdd(sent, 1);
+  }
+}
+
+cudaError_t launch_ghost_catchup(const GhostArgs& g, int max_iter, const int* gate, int* sent,
+                                 cudaStream_t s) {
+  ghost_catchup<<<grid_for(g.hi - g.lo), 256, 0, s>>>(g, max_iter, gate, sent);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ghost(const GhostArgs& g, cudaStream_t s) {
   ghost_round<<<grid_for(g.hi - g.lo), 256, 0, s>>>(g);
   return cudaGetLastError();

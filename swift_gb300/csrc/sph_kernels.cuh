@@ -105,11 +105,7 @@ struct ListArgs {
   float band;
   const int* gate;              // do nothing when *gate == 0
   unsigned long long* hits;     // optional: total neighbour hits
-  // j-block boxes and ranges (the solver's gather for a particle whose h
-  // outgrew its list)
-  const float4* bb_lo;
-  const float4* bb_hi;
-  const int2* bb_fc;
+  int* handover;                // solver: particles left to the catch-up rounds
 };
 
 struct GhostArgs {
@@ -151,6 +147,12 @@ cudaError_t launch_density_noalloc(const G2Args& base, const LeafInfo* leaves,
 cudaError_t launch_block_hmax(const int2* fc, float4* lo, const float4* posh,
                               int nblocks, cudaStream_t s);
 cudaError_t launch_ghost(const GhostArgs& g, cudaStream_t s);
+// A catch-up round after the list solver: every particle still iterating
+// takes its own next round (its iteration count, ghost_iters) from the sums
+// a re-run gather just computed; *sent counts those it sends on.  Does
+// nothing when *gate == 0.
+cudaError_t launch_ghost_catchup(const GhostArgs& g, int max_iter, const int* gate, int* sent,
+                                 cudaStream_t s);
 cudaError_t launch_begin_step(const DevParticles& p, int max_iter,
                               int* redo_count, float h_max, cudaStream_t s);
 cudaError_t launch_set_flags(uint8_t* flags, const int* idx, int n, uint8_t v,

@@ -653,10 +653,11 @@ def run_ours(args):
             # (ghost, units, re-run gather, and the list kernel after the
             # first; gated ones return at once), block h_max, force units +
             # gather
-            # per step: begin-step, density (units + gather), then with the lists
-            # ghost round 0 + the per-particle solver, else 8 rounds in the graph
-            # (ghost, units, gather); force (h_max, units, gather)
-            "gpu_launches": (6 + (2 if tuning.get("rerun_lists") else 8 * 3)) * args.steps,
+            # per step: begin-step, density (units + gather), 8 ghost rounds in the
+            # graph (ghost, units, gather; gated) -- with the lists ghost round 0
+            # and the per-particle solver come first and the 8 rounds are
+            # catch-up rounds -- force (h_max, units, gather)
+            "gpu_launches": (6 + 8 * 3 + (2 if tuning.get("rerun_lists") else 0)) * args.steps,
             "clocks": clk,
             "cpu_baseline": cb,
         }

@@ -532,14 +532,7 @@ void enqueue_ghost_rounds(sphgpu_space* s, cudaStream_t st, int k0 = 0, int k1 =
   }
   for (int k = k0; k < k1; k++) {
     CK(launch_ghost(ghargs(s, k, 0, s->P.n), st));
-    if (!lists_on(s)) {
-      enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k);
-    } else {
-      // re-runs from the first pass's lists where they cover h, the gather
-      // for the rest
-      CK(launch_redo_from_lists(largs(s, s->redo.p + k), st));
-      enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k, 0, -1, 8);
-    }
+    enqueue_gather(s, st, s->dplan_s, 1, MODE_REDO, false, 3, s->redo.p + k);
   }
 }
 

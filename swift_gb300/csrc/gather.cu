@@ -90,12 +90,6 @@ cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
   return cudaGetLastError();
 }
 
-cudaError_t launch_redo_from_lists(const ListArgs& a, cudaStream_t s) {
-  long long g = ((long long)a.p.n * 4 + 255) / 256;  // four lanes per particle
-  g = std::max(1LL, std::min(g, 152LL * 16));
-  redo_from_lists<<<(int)g, 256, 0, s>>>(a);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_solve_from_lists(const ListArgs& a, const GhostArgs& g, int max_iter,
                                     cudaStream_t s) {

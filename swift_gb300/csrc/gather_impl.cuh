@@ -613,112 +613,6 @@ static __device__ const Entry* rerun_entry(const ListArgs& a, int leaf, int b, i
   return nullptr;
 }
 
-// Four lanes per particle: lane k of a particle takes items k, k + 4, ...
-// of its list (a particle's row is read 16 bytes at a time), and the lanes
-// add their partial sums at the end (fixed order: deterministic).
-static __global__ void __launch_bounds__(256, 4) redo_from_lists(ListArgs a) {
-  constexpr int LPP = 4;  // lanes per particle
-  if (a.gate && *a.gate == 0) return;
-  const DevParticles& P = a.p;
-  __shared__ float4 ftab[27];  // frame offsets by index (offset_of)
-  if (threadIdx.x < 27) {
-    const float3 o = offset_of(threadIdx.x, a.top_width);
-    ftab[threadIdx.x] = make_float4(o.x, o.y, o.z, 0.f);
-  }
-  __syncthreads();
-  const int sub = threadIdx.x % LPP;
-  const int stride = gridDim.x * blockDim.x / LPP;
-  // the warp's four particles advance together (the shuffles below need
-  // every lane)
-  for (int base = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / LPP; base < P.n;
-       base += stride) {
-    const int i = base + (threadIdx.x & 31) / LPP;
-    bool work = false;
-    float4 pi = make_float4(0.f, 0.f, 0.f, 1.f);
-    float L2 = 0.f, U2 = 0.f, hig2 = 0.f;
-    int cnt = 0, c0 = 0;
-    if (i < P.n) {
-      const uint8_t fl = P.flags[i];
-      if ((fl & 3) == 3) {  // active and re-run this round
-        pi = P.posh[i];
-        hig2 = h2_exact(pi.w);
-        L2 = hig2 * (1.f - a.band);
-        U2 = hig2 * (1.f + a.band);
-        cnt = a.nl_cnt[i];
-        work = cnt >= 0 && U2 <= a.nl_T[i];  // else the list does not cover h: gather
-        if (work) {  // segment 0 holds c0 items, segment 1 (at nl_cap / 2) the rest
-          c0 = a.nl_seg == 2 ? (cnt & 0xffff) : cnt;
-          cnt = c0 + (a.nl_seg == 2 ? cnt >> 16 : 0);
-        }
-        if (sub == 0) P.flags[i] = work ? (fl | 8) : (fl & ~8);
-      }
-    }
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f, s5 = 0.f, s6 = 0.f, s7 = 0.f;
-    int ngb = 0;
-    if (work) {
-      const float4 vi = P.velm[i];
-      const float hi_inv = 1.f / pi.w;
-      const int* row = a.nl + (size_t)i * a.nl_cap;
-      // three items per lane at a time, their loads all in flight together; a
-      // miss is evaluated too, at a distance beyond the kernel's support
-      // (zero contributions), so the lanes do not diverge
-      for (int t0 = sub; t0 < cnt; t0 += 3 * LPP) {
-        int pk[3];
-        float4 q[3], vm[3];
-#pragma unroll
-        for (int u = 0; u < 3; u++) {
-          const int t = t0 + u * LPP;
-          pk[u] = t < cnt ? row[t < c0 ? t : t - c0 + a.nl_cap / 2] : i;
-          // an item always names a particle of the store; a corrupt row is
-          // read as a miss rather than followed out of bounds
-          if ((pk[u] & 0x07ffffff) >= P.n || ((unsigned)pk[u] >> 27) > 26) pk[u] = i;
-        }
-#pragma unroll
-        for (int u = 0; u < 3; u++) {
-          q[u] = P.posh[pk[u] & 0x07ffffff];
-          vm[u] = P.velm[pk[u] & 0x07ffffff];
-        }
-#pragma unroll
-        for (int u = 0; u < 3; u++) {
-          const int j = pk[u] & 0x07ffffff;
-          const float4 fd = ftab[(unsigned)pk[u] >> 27];
-          const float dx = pi.x - (q[u].x + fd.x), dy = pi.y - (q[u].y + fd.y),
-                      dz = pi.z - (q[u].z + fd.z);
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          const bool item = t0 + u * LPP < cnt;
-          bool hit = item && r2 < L2;
-          if (item && !hit && r2 < U2) {  // inside the band: exact decision (rare)
-            const Entry* E = rerun_entry(a, P.leaf_of[i], a.blk_of[j], P.depth_h[i]);
-            hit = E != nullptr && exact_r2_2(P.xd, i, j, E) < hig2;
-          }
-          density_hit(dx, dy, dz, hit ? r2 : 4.f * U2, vi, vm[u], hi_inv, s0, s1, s2, s3, s4,
-                      s5, s6, s7);
-          ngb += hit;
-        }
-      }
-    }
-    // the particle's lanes add their partial sums (lanes of a group share
-    // `work`, so whole groups take part)
-#pragma unroll
-    for (int o = 1; o < LPP; o <<= 1) {
-      s0 += __shfl_xor_sync(FULL, s0, o);
-      s1 += __shfl_xor_sync(FULL, s1, o);
-      s2 += __shfl_xor_sync(FULL, s2, o);
-      s3 += __shfl_xor_sync(FULL, s3, o);
-      s4 += __shfl_xor_sync(FULL, s4, o);
-      s5 += __shfl_xor_sync(FULL, s5, o);
-      s6 += __shfl_xor_sync(FULL, s6, o);
-      s7 += __shfl_xor_sync(FULL, s7, o);
-      ngb += __shfl_xor_sync(FULL, ngb, o);
-    }
-    if (work && sub == 0) {
-      P.dens0[i] = make_float4(s0, s1, s2, s3);
-      P.dens1[i] = make_float4(s4, s5, s6, s7);
-      P.ngb_d[i] = ngb;
-      if (a.hits) atomicAdd(a.hits, (unsigned long long)ngb);
-    }
-  }
-}
 
 // The ghost's rounds after the first: each particle iterates on its own
 // (its density at h_k depends on nothing that changes during the ghost):

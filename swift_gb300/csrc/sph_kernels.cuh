@@ -129,7 +129,6 @@ cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                const int* leaf_window_begin, const uint8_t* flags,
                                int need, int veto, const int* leaf_pair_begin,
                                int4* units, const int* gate, cudaStream_t s, int win = 32);
-cudaError_t launch_redo_from_lists(const ListArgs& a, cudaStream_t s);
 // The ghost's rounds 1.. max_iter - 1 for every particle still iterating
 // after round 0, each particle on its own: density from its list (or, where
 // its h outgrew the list, from its leaf's re-run candidate blocks), then the

@@ -420,6 +420,9 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   a.nl_cap = 0;
   a.nl_widen = 1.f;
   a.leaves = s->leaves.p;
+  a.force_rows = 0;
+  a.nl_seg = 1;
+  a.blk_of = s->blk_of.p;
   return a;
 }
 
@@ -434,7 +437,7 @@ int rec_tpp(const sphgpu_space* s) { return std::min(2, s->tune.threads_per_part
 void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
                     int mode, bool force, int need, const int* gate,
                     int leaf_begin = 0, int leaf_end = -1, int veto = 0,
-                    bool lists = false) {
+                    bool lists = false, bool force_rows = false) {
   const int nl = (int)s->space->leaves().size();
   if (leaf_end < 0) leaf_end = nl;
   // two or four lanes per particle: 16- or 8-particle windows
@@ -458,6 +461,15 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
     a.nl_T = s->nl_T.p;
     a.nl_cap = kListCap;
     if (mode == MODE_FIRST) a.nl_widen = kListWiden;
+  }
+  if (force && force_rows) {
+    // the force reads the rows the first pass recorded this step
+    a.nl = s->nl.p;
+    a.nl_cnt = s->nl_cnt.p;
+    a.nl_T = s->nl_T.p;
+    a.nl_cap = kListCap;
+    a.nl_seg = rec_tpp(s);
+    a.force_rows = 1;
   }
   CK(launch_gather(a, force, s->num_sms, w1 - w0, st, s->tune.block_warps, lists, tpp));
 }
@@ -550,7 +562,8 @@ void enqueue_density_ghost(sphgpu_space* s, cudaStream_t st, int stages) {
 
 void enqueue_force(sphgpu_space* s, cudaStream_t st) {
   CK(launch_block_hmax(s->bb_fc.p, s->bb_lo.p, s->posh.p, s->bb_n, st));
-  enqueue_gather(s, st, s->dplan_f, 2, MODE_FIRST, true, 1, nullptr);
+  enqueue_gather(s, st, s->dplan_f, 2, MODE_FIRST, true, 1, nullptr, 0, -1, 0, false,
+                 lists_on(s));
 }
 
 int check_conv(sphgpu_space* s, cudaStream_t st) {

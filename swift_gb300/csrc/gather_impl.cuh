@@ -338,7 +338,89 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
       if (__any_sync(FULL, qt - qh > QCAP - 8)) drain(false);
     };
 
-    for (int c0 = U.z; c0 < U.w; c0 += 32) {
+    // Force from the first pass's rows: when every lane's row covers its own
+    // radius and the largest radius among the blocks the group reaches (the
+    // cull below), each row holds every force partner of its particle
+    // (r < max(H_i, H_j) < the row's bound), and the candidate search is
+    // skipped: the rows' items are tested instead, with the same criterion.
+    bool use_rows = false;
+    int rcnt = 0, rc0 = 0;
+    if (FORCE && a.force_rows) {
+      bool ok = true;
+      float rT = 3.4e38f;
+      if (valid) {
+        const int c = a.nl_cnt[i];
+        rT = a.nl_T[i];
+        if (c < 0 || !(hi2 <= rT)) {
+          ok = false;
+        } else {
+          rc0 = a.nl_seg == 2 ? (c & 0xffff) : c;
+          rcnt = rc0 + (a.nl_seg == 2 ? c >> 16 : 0);
+        }
+      }
+      if (__all_sync(FULL, ok)) {
+        float maxW = 0.f;
+        for (int c0 = U.z; c0 < U.w; c0 += 32) {
+          const int p = c0 + lane;
+          if (p < U.w) {
+            const int b = a.pair_block[p];
+            const Entry* E = &a.entries[a.pair_entry[p]];
+            const float4 lo = a.bb_lo[b], hb = a.bb_hi[b];
+            const float dx = fmaxf(fmaxf(lo.x + E->fdx - gx1, gx0 - hb.x - E->fdx), 0.f);
+            const float dy = fmaxf(fmaxf(lo.y + E->fdy - gy1, gy0 - hb.y - E->fdy), 0.f);
+            const float dz = fmaxf(fmaxf(lo.z + E->fdz - gz1, gz0 - hb.z - E->fdz), 0.f);
+            if (dx * dx + dy * dy + dz * dz < fmaxf(gh2, lo.w) * (1.f + 4.f * band) + 1e-30f &&
+                gd1 >= E->min_depth && gd0 <= E->max_depth)
+              maxW = fmaxf(maxW, lo.w);
+          }
+        }
+        float minT = rT;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          maxW = fmaxf(maxW, __shfl_xor_sync(FULL, maxW, off));
+          minT = fminf(minT, __shfl_xor_sync(FULL, minT, off));
+        }
+        use_rows = maxW * (1.f + band) <= minT;
+      }
+    }
+    if (FORCE && use_rows) {
+      const int* row = a.nl + (size_t)(valid ? i : 0) * a.nl_cap;
+      const int nmine = valid ? (rcnt - sub + TPP - 1) / TPP : 0;  // items sub, sub + TPP, ...
+      const int kmax = (int)__reduce_max_sync(FULL, (unsigned)max(nmine, 0));
+      for (int k0 = 0; k0 < kmax; k0 += 8) {
+#pragma unroll 4
+        for (int u = 0; u < 8; u++) {
+          const int k = k0 + u;
+          if (k >= nmine) continue;
+          const int t = sub + k * TPP;
+          const int pk = row[t < rc0 ? t : t - rc0 + a.nl_cap / 2];
+          const int j = pk & 0x07ffffff;
+          if (j >= P.n || ((unsigned)pk >> 27) > 26) continue;  // never: rows name store particles
+          const float4 q = P.posh[j];
+          const float4 fd = ws.ftab[(unsigned)pk >> 27];
+          const float dx = pi.x - (q.x + fd.x), dy = pi.y - (q.y + fd.y),
+                      dz = pi.z - (q.z + fd.z);
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          const float H2 = fmaxf(hig2, h2_exact(q.w));
+          if (r2 < H2 * (1.f - band)) {
+            push(pk);
+          } else if (r2 < H2 * (1.f + band)) {
+            // exact, in the frame of the force-list entry pairing the leaf
+            // with the partner's block at this particle's depth
+            const int blk = a.blk_of[j];
+            const Entry* E = nullptr;
+            for (int p = U.z; p < U.w && !E; p++)
+              if (a.pair_block[p] == blk) {
+                const Entry* X = &a.entries[a.pair_entry[p]];
+                if (dh >= X->min_depth && dh <= X->max_depth) E = X;
+              }
+            if (E && exact_r2_2(P.xd, i, j, E) < H2) push(pk);
+          }
+        }
+        room();  // at most 8 pushes per lane since the last check
+      }
+    }
+    for (int c0 = U.z; c0 < (FORCE && use_rows ? U.z : U.w); c0 += 32) {
       const int p = c0 + lane;
       bool ov = false;
       int e = 0;

@@ -559,7 +559,7 @@ struct sphgpu_server {
     a.nl_cnt = nullptr;
     a.nl_T = nullptr;
     a.nl_cap = 0;
-      return a;
+    return a;
   }
 
   void gather(int k, int qslot, int mode, bool force, int need, const int* gate) {

@@ -80,8 +80,13 @@ struct G2Args {
   // pass's own: r^2 below min(nl_widen (gamma h)^2 (1 + band), the square of
   // the smallest width of the particle's depth_h cell) -- every particle
   // closer than that width lies in a cell the recursion pairs at that depth
-  float nl_widen;
-  const LeafInfo* leaves;       // for that width (lists only)
+  float nl_widen = 1.f;
+  const LeafInfo* leaves = nullptr;  // for that width (lists only)
+  // force gathers: take each group's partners from the first pass's rows
+  // where they cover them (rows recorded this step, nl_seg segments each)
+  int force_rows = 0;
+  int nl_seg = 1;
+  const int* blk_of = nullptr;  // j-block of every particle (frame lookups)
 };
 
 // Later re-runs from the lists: particles whose list covers their new

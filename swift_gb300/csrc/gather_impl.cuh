@@ -384,38 +384,66 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
       }
     }
     if (FORCE && use_rows) {
+      // each lane reads the row segment it recorded in the first pass (the
+      // first pass ran with the same lanes per particle), four items per
+      // 16-byte load, the partners' positions all in flight together
       const int* row = a.nl + (size_t)(valid ? i : 0) * a.nl_cap;
-      const int nmine = valid ? (rcnt - sub + TPP - 1) / TPP : 0;  // items sub, sub + TPP, ...
+      const bool own_seg = a.nl_seg == TPP;
+      const int nmine = !valid ? 0
+                        : own_seg ? (TPP == 1 ? rcnt : (sub == 0 ? rc0 : rcnt - rc0))
+                                  : (rcnt - sub + TPP - 1) / TPP;
+      const int* seg = row + (own_seg ? sub * (a.nl_cap / TPP) : 0);
       const int kmax = (int)__reduce_max_sync(FULL, (unsigned)max(nmine, 0));
+      auto test_item = [&](int pk, const float4& q) {
+        const int j = pk & 0x07ffffff;
+        const float4 fd = ws.ftab[(unsigned)pk >> 27];
+        const float dx = pi.x - (q.x + fd.x), dy = pi.y - (q.y + fd.y), dz = pi.z - (q.z + fd.z);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float H2 = fmaxf(hig2, h2_exact(q.w));
+        if (r2 < H2 * (1.f - band)) {
+          push(pk);
+        } else if (r2 < H2 * (1.f + band)) {
+          // exact, in the frame of the force-list entry pairing the leaf
+          // with the partner's block at this particle's depth
+          const int blk = a.blk_of[j];
+          const Entry* E = nullptr;
+          for (int p = U.z; p < U.w && !E; p++)
+            if (a.pair_block[p] == blk) {
+              const Entry* X = &a.entries[a.pair_entry[p]];
+              if (dh >= X->min_depth && dh <= X->max_depth) E = X;
+            }
+          if (E && exact_r2_2(P.xd, i, j, E) < H2) push(pk);
+        }
+      };
       for (int k0 = 0; k0 < kmax; k0 += 8) {
-#pragma unroll 4
-        for (int u = 0; u < 8; u++) {
-          const int k = k0 + u;
-          if (k >= nmine) continue;
-          const int t = sub + k * TPP;
-          const int pk = row[t < rc0 ? t : t - rc0 + a.nl_cap / 2];
-          const int j = pk & 0x07ffffff;
-          if (j >= P.n || ((unsigned)pk >> 27) > 26) continue;  // never: rows name store particles
-          const float4 q = P.posh[j];
-          const float4 fd = ws.ftab[(unsigned)pk >> 27];
-          const float dx = pi.x - (q.x + fd.x), dy = pi.y - (q.y + fd.y),
-                      dz = pi.z - (q.z + fd.z);
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          const float H2 = fmaxf(hig2, h2_exact(q.w));
-          if (r2 < H2 * (1.f - band)) {
-            push(pk);
-          } else if (r2 < H2 * (1.f + band)) {
-            // exact, in the frame of the force-list entry pairing the leaf
-            // with the partner's block at this particle's depth
-            const int blk = a.blk_of[j];
-            const Entry* E = nullptr;
-            for (int p = U.z; p < U.w && !E; p++)
-              if (a.pair_block[p] == blk) {
-                const Entry* X = &a.entries[a.pair_entry[p]];
-                if (dh >= X->min_depth && dh <= X->max_depth) E = X;
-              }
-            if (E && exact_r2_2(P.xd, i, j, E) < H2) push(pk);
+#pragma unroll
+        for (int h4 = 0; h4 < 8; h4 += 4) {
+          int pk[4];
+          if (own_seg) {
+            // k0 + h4 + 4 stays inside the segment's capacity (a multiple of 8)
+            const int4 v4 = k0 + h4 < nmine ? *reinterpret_cast<const int4*>(seg + k0 + h4)
+                                            : make_int4(i, i, i, i);
+            pk[0] = v4.x; pk[1] = v4.y; pk[2] = v4.z; pk[3] = v4.w;
+          } else {
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const int t = sub + (k0 + h4 + u) * TPP;
+              pk[u] = k0 + h4 + u < nmine ? row[t < rc0 ? t : t - rc0 + a.nl_cap / 2] : i;
+            }
           }
+          float4 q[4];
+          unsigned okm = 0u;  // items to test (the packed items use the sign bit)
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            // an item always names a store particle; anything else is skipped
+            const bool ok = k0 + h4 + u < nmine && (pk[u] & 0x07ffffff) < P.n &&
+                            ((unsigned)pk[u] >> 27) <= 26;
+            okm |= ok ? 1u << u : 0u;
+            q[u] = P.posh[ok ? (pk[u] & 0x07ffffff) : (valid ? i : 0)];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            if (okm & (1u << u)) test_item(pk[u], q[u]);
         }
         room();  // at most 8 pushes per lane since the last check
       }

@@ -236,18 +236,17 @@ def run_reference_arm(args):
 
 def traffic_from_profile(workload, tuning):
     """DRAM bytes per force-gather launch from the committed ncu summary of
-    this workload, when it was captured with the same j-block depth."""
+    this workload: the capture made with the same j-block depth and lanes per
+    particle (lines "traffic_bytes_per_launch: N (...) — jtile J,
+    threads_per_particle T")."""
     path = os.path.join(ROOT, "profiles", f"force_gather_{workload}.md")
+    want = (f"jtile {tuning.get('jtile')}",
+            f"threads_per_particle {tuning.get('threads_per_particle', 1)}")
     try:
         with open(path) as f:
-            text = f.read()
-        if f"jtile {tuning.get('jtile')}" not in text:
-            return None
-        if f"threads_per_particle {tuning.get('threads_per_particle', 1)}" not in text:
-            return None
-        for line in text.splitlines():
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1].strip().split()[0])
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:") and all(w in line for w in want):
+                    return float(line.split(":")[1].strip().split()[0])
     except Exception:
         pass
     return None

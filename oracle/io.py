@@ -1,6 +1,6 @@
 """Binary I/O between the oracle's Python side and its C programs.
 
-Test infrastructure only.  ``write_input`` produces the "SPHIN001" file read by
+Test infrastructure only.  ``write_input`` produces the "SPHIN002" file read by
 oracle/ref_harness.c (the driver of the reference's own loops) and by the C
 restatement in oracle/sph_oracle.c; ``read_output`` parses "SPHOUT01".
 """
@@ -36,15 +36,16 @@ HEADER_DTYPE = np.dtype([
     ("h_tolerance", "<f4"), ("h_max", "<f4"), ("h_min", "<f4"),
     ("alpha", "<f4"), ("max_iter", "<i4"), ("max_active_bin", "<i4"),
     ("periodic", "<i4"), ("stages", "<i4"), ("max_top_level_cells", "<i4"),
+    ("subsize_self", "<i4"), ("subsize_pair", "<i4"),
 ])
-assert HEADER_DTYPE.itemsize == 80
+assert HEADER_DTYPE.itemsize == 88
 
 
 def default_params(box):
     return dict(eta=box.get("eta", 1.2348), h_tolerance=1e-4,
                 h_max=np.finfo(np.float32).max, h_min=0.0, alpha=0.8,
                 max_iter=30, max_active_bin=box.get("max_active_bin", 56),
-                periodic=1, max_top_level_cells=12)
+                periodic=1, max_top_level_cells=12, subsize_self=0, subsize_pair=0)
 
 
 def write_input(path, box, stages=ALL_STAGES, **overrides):
@@ -52,11 +53,12 @@ def write_input(path, box, stages=ALL_STAGES, **overrides):
     p.update(overrides)
     n = box["x"].shape[0]
     hdr = np.zeros(1, HEADER_DTYPE)
-    hdr["magic"] = b"SPHIN001"
+    hdr["magic"] = b"SPHIN002"
     hdr["n"] = n
     hdr["dim"] = list(box["dim"]) if np.ndim(box["dim"]) else [box["dim"]] * 3
     for k in ("eta", "h_tolerance", "h_max", "h_min", "alpha", "max_iter",
-              "max_active_bin", "periodic", "max_top_level_cells"):
+              "max_active_bin", "periodic", "max_top_level_cells", "subsize_self",
+              "subsize_pair"):
         hdr[k] = p[k]
     hdr["stages"] = stages
     with open(path, "wb") as f:

@@ -30,14 +30,15 @@ class Params(ctypes.Structure):
                 ("h_max", ctypes.c_float), ("h_min", ctypes.c_float),
                 ("alpha", ctypes.c_float), ("max_iter", ctypes.c_int32),
                 ("max_active_bin", ctypes.c_int32),
-                ("max_top_level_cells", ctypes.c_int32)]
+                ("max_top_level_cells", ctypes.c_int32),
+                ("subsize_self", ctypes.c_int32), ("subsize_pair", ctypes.c_int32)]
 
 
 class Result(ctypes.Structure):
     _fields_ = [("fields", ctypes.POINTER(ctypes.c_float)),
                 ("ints", ctypes.POINTER(ctypes.c_int32)),
                 ("cdim", ctypes.c_int32 * 3), ("ncells", ctypes.c_int32),
-                ("status", ctypes.c_int32)]
+                ("status", ctypes.c_int32), ("ntasks", ctypes.c_int32)]
 
 
 def build(force=False):
@@ -80,6 +81,10 @@ def make_params(box, **kw):
     p.max_iter = kw.get("max_iter", 30)
     p.max_active_bin = kw.get("max_active_bin", box.get("max_active_bin", 56))
     p.max_top_level_cells = kw.get("max_top_level_cells", 12)
+    # 0, 0: one task per top cell / top-cell pair; else the reference's
+    # Scheduler:cell_sub_size_self_hydro / cell_sub_size_pair_hydro split
+    p.subsize_self = kw.get("subsize_self", 0)
+    p.subsize_pair = kw.get("subsize_pair", 0)
     return p
 
 
@@ -109,7 +114,7 @@ def run(box, stages=ALL, **kw):
                      _ptr(tb, ctypes.c_byte), ctypes.c_int(stages),
                      ctypes.byref(res))
     out = {"res": fields, "ints": ints, "cdim": tuple(res.cdim),
-           "ncells": res.ncells, "status": res.status}
+           "ncells": res.ncells, "status": res.status, "ntasks": res.ntasks}
     for name, col in COLS.items():
         out[name] = fields[:, col]
     for name, col in INT_COLS.items():

@@ -14,8 +14,10 @@
  *   runner_do_ghost (runner_ghost.c:1113)
  *   runner_dosub_self2_force / runner_dosub_pair2_force (:3203 / :3102)
  *   runner_do_end_hydro_force (runner_others.c:815)
+ *   scheduler_addtask (scheduler.c:164), scheduler_splittasks_mapper
+ *       (scheduler_splittasks.c:538) when the header asks for task splitting
  *
- * Input  (argv[1]): "SPHIN001" header + SoA arrays (see oracle/io.py).
+ * Input  (argv[1]): "SPHIN002" header + SoA arrays (see oracle/io.py).
  * Output (argv[2]): "SPHOUT01" header + per-particle results in input order,
  *                   followed by the cell tree in depth-first order.
  * Optional (argv[3]): "SPHSRT01" + the 13 sort arrays of every non-empty
@@ -31,6 +33,11 @@
 /* config.h and swift.h come in through -include on the command line. */
 #include "runner.h"
 #include "runner_doiact_hydro.h"
+#include "scheduler.h"
+#include "space_getsid.h"
+
+/* Defined (not static) in scheduler_splittasks.c:538; no header declares it. */
+void scheduler_splittasks_mapper(void *map_data, int num_elements, void *extra_data);
 
 #define STAGE_DENSITY 1
 #define STAGE_GHOST 2
@@ -45,6 +52,7 @@ struct in_header {
   double dim[3];
   float eta, h_tolerance, h_max, h_min, alpha;
   int32_t max_iter, max_active_bin, periodic, stages, max_top_level_cells;
+  int32_t subsize_self, subsize_pair; /* both 0: no task splitting */
 };
 
 static void *xmalloc(size_t n) {
@@ -64,7 +72,7 @@ static void xread(void *dst, size_t sz, size_t n, FILE *f) {
   }
 }
 
-/* Density tasks attached to a top cell, so that the ghost's redo path
+/* Density links of the cells the tasks hold, so that the ghost's redo path
  * (runner_ghost.c:1548-1579) walks real links as in the engine. */
 static struct link *link_pool;
 static int link_used;
@@ -162,7 +170,7 @@ int main(int argc, char **argv) {
   if (!fin) return 2;
   struct in_header hdr;
   xread(&hdr, sizeof(hdr), 1, fin);
-  if (memcmp(hdr.magic, "SPHIN001", 8) != 0) {
+  if (memcmp(hdr.magic, "SPHIN002", 8) != 0) {
     fprintf(stderr, "ref_harness: bad magic\n");
     return 2;
   }
@@ -298,22 +306,27 @@ int main(int argc, char **argv) {
   }
 
   /* Task list: one self task per non-empty top cell, one pair task per
-   * neighbouring non-empty top-cell pair (26-neighbourhood, periodic). */
+   * neighbouring non-empty top-cell pair (26-neighbourhood, periodic),
+   * created through the reference's scheduler_addtask.  With split sizes in
+   * the header the reference's own splitter then splits them
+   * (Scheduler:cell_sub_size_self_hydro / cell_sub_size_pair_hydro), one
+   * task at a time in array order as a single-threaded mapper call does. */
   const int *cdim = s.cdim;
-  struct task *tasks = xmalloc(sizeof(struct task) * (size_t)ncells * 14);
-  link_pool = xmalloc(sizeof(struct link) * (size_t)ncells * 28);
-  int ntasks = 0;
+  static struct scheduler sched;
+  memset(&sched, 0, sizeof(sched));
+  sched.space = &s;
+  sched.nodeID = 0;
+  /* a cell holds at most one self task and 26 pair tasks */
+  sched.size = 27 * (s.tot_cells + ncells) + 64;
+  sched.tasks = xmalloc(sizeof(struct task) * (size_t)sched.size);
+  sched.tasks_ind = xmalloc(sizeof(int) * (size_t)sched.size);
   for (int i = 0; i < cdim[0]; i++)
     for (int j = 0; j < cdim[1]; j++)
       for (int k = 0; k < cdim[2]; k++) {
         const int cid = cell_getid(cdim, i, j, k);
         struct cell *ci = &s.cells_top[cid];
         if (ci->hydro.count == 0) continue;
-        struct task *t = &tasks[ntasks++];
-        t->type = task_type_self;
-        t->subtype = task_subtype_density;
-        t->ci = ci;
-        add_link(&ci->hydro.density, t);
+        scheduler_addtask(&sched, task_type_self, task_subtype_density, 0, 0, ci, NULL);
         for (int di = -1; di <= 1; di++)
           for (int dj = -1; dj <= 1; dj++)
             for (int dk = -1; dk <= 1; dk++) {
@@ -329,15 +342,29 @@ int main(int argc, char **argv) {
               if (cjd <= cid) continue;
               struct cell *cj = &s.cells_top[cjd];
               if (cj->hydro.count == 0) continue;
-              struct task *tp = &tasks[ntasks++];
-              tp->type = task_type_pair;
-              tp->subtype = task_subtype_density;
-              tp->ci = ci;
-              tp->cj = cj;
-              add_link(&ci->hydro.density, tp);
-              add_link(&cj->hydro.density, tp);
+              struct cell *a = ci, *b = cj;
+              double shift[3];
+              const int sid = space_getsid_and_swap_cells(&s, &a, &b, shift);
+              scheduler_addtask(&sched, task_type_pair, task_subtype_density, sid, 0, ci, cj);
             }
       }
+  if (hdr.subsize_self > 0 || hdr.subsize_pair > 0) {
+    space_subsize_self_hydro = hdr.subsize_self;
+    space_subsize_pair_hydro = hdr.subsize_pair;
+    scheduler_splittasks_mapper(sched.tasks, sched.tasks_next, &sched);
+  }
+  /* The tasks the split left (type none dropped, order kept), linked to the
+   * cells they hold in task order (engine_maketasks.c:2311-2333). */
+  struct task *tasks = sched.tasks;
+  int ntasks = 0;
+  for (int t = 0; t < sched.tasks_next; t++)
+    if (tasks[t].type == task_type_self || tasks[t].type == task_type_pair)
+      tasks[ntasks++] = tasks[t];
+  link_pool = xmalloc(sizeof(struct link) * ((size_t)ntasks * 2 + 1));
+  for (int t = 0; t < ntasks; t++) {
+    add_link(&tasks[t].ci->hydro.density, &tasks[t]);
+    if (tasks[t].type == task_type_pair) add_link(&tasks[t].cj->hydro.density, &tasks[t]);
+  }
 
   const size_t nf = 24;
   float *res = xmalloc(n * nf * sizeof(float));

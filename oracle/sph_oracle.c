@@ -1518,7 +1518,7 @@ typedef struct {
   int cdim[3];
   double width[3];
   otask *tasks;
-  int ntasks;
+  int ntasks, tcap;
   olink *links;
   int nlinks;
 } ospace;
@@ -1528,6 +1528,89 @@ static void link_add(ospace *s, ocell *c, otask *t) {
   l->t = t;
   l->next = c->density;
   c->density = l;
+}
+
+static int task_add(ospace *s, int is_pair, ocell *ci, ocell *cj) {
+  if (s->ntasks == s->tcap) {
+    s->tcap *= 2;
+    s->tasks = realloc(s->tasks, sizeof(otask) * (size_t)s->tcap);
+    if (!s->tasks) {
+      fprintf(stderr, "sph_oracle: out of memory\n");
+      abort();
+    }
+  }
+  otask *t = &s->tasks[s->ntasks];
+  t->is_pair = is_pair;
+  t->ci = ci;
+  t->cj = cj;
+  return s->ntasks++;
+}
+
+/* cell_can_split_pair_hydro_task / cell_can_split_self_hydro_task
+ * (cell.h:1152-1186): the cut-off with the space_stretch leeway (1.10f,
+ * space.h:74) fits in half the progeny width.  Tasks are split right after a
+ * rebuild, so h_max is the rebuild's. */
+static inline int can_split_task(const ocell *c) {
+  return c->split && (1.10f * KG * c->h_max < 0.5f * c->dmin);
+}
+
+/* sid_scale (sort_part.h:93-95): relative cost of a pair along each axis. */
+static const float sid_scale[13] = {0.1897f, 0.4025f, 0.1897f, 0.4025f, 0.5788f,
+                                    0.4025f, 0.1897f, 0.4025f, 0.1897f, 0.4025f,
+                                    0.5788f, 0.4025f, 0.5788f};
+
+/* The reference scheduler's hydro task split (scheduler_splittask_hydro,
+ * scheduler_splittasks.c:45-265, with scheduler_dosub = 1 and
+ * scheduler_doforcesplit = 0, scheduler.h:45-51), gas only.  Task ti is
+ * recycled into its first piece and redone; every other piece is appended
+ * and split at once, as scheduler_addtask + the recursive call do, so the
+ * final order is the reference's.  An emptied task keeps ci = NULL.
+ *   self on a cell that can split and holds >= subsize_self particles:
+ *     the self tasks of the non-empty progeny, then a pair task for every
+ *     two non-empty progeny (j < k);
+ *   pair whose cells (after the sid swap) can both split, when the sid is
+ *     a corner (sort_is_corner, sort_part.h:111) or
+ *     count_i * sid_scale[sid] >= subsize_pair / count_j:
+ *     the progeny pairs of the sid's split list, in list order. */
+static void split_task(ospace *s, int ti) {
+  const int sub_self = s->e.prm->subsize_self, sub_pair = s->e.prm->subsize_pair;
+  for (;;) {
+    otask t = s->tasks[ti];
+    const int live = t.ci != NULL && t.ci->count > 0 &&
+                     (!t.is_pair || (t.cj != NULL && t.cj->count > 0));
+    if (!live) {
+      s->tasks[ti].ci = s->tasks[ti].cj = NULL;
+      return;
+    }
+    if (!t.is_pair) {
+      ocell *ci = t.ci;
+      if (!can_split_task(ci) || ci->count < sub_self) return;
+      int first = 0;
+      while (ci->progeny[first] == NULL) first++;
+      s->tasks[ti].ci = ci->progeny[first];
+      for (int k = first + 1; k < 8; k++)
+        if (ci->progeny[k] != NULL && ci->progeny[k]->count)
+          split_task(s, task_add(s, 0, ci->progeny[k], NULL));
+      for (int j = 0; j < 8; j++)
+        if (ci->progeny[j] != NULL && ci->progeny[j]->count)
+          for (int k = j + 1; k < 8; k++)
+            if (ci->progeny[k] != NULL && ci->progeny[k]->count)
+              split_task(s, task_add(s, 1, ci->progeny[j], ci->progeny[k]));
+    } else {
+      ocell *ci = t.ci, *cj = t.cj;
+      double shift[3];
+      const int sid = getsid_and_swap(&s->e, &ci, &cj, shift);
+      if (!(can_split_task(ci) && can_split_task(cj))) return;
+      const int do_sub = (float)ci->count * sid_scale[sid] < (float)(sub_pair / cj->count);
+      const int corner = sid == 0 || sid == 2 || sid == 6 || sid == 8;
+      if (do_sub && !corner) return;
+      s->tasks[ti].ci = ci->progeny[split_pairs[sid][0][0]];
+      s->tasks[ti].cj = cj->progeny[split_pairs[sid][0][1]];
+      for (int k = 1; k < split_pairs_n[sid]; k++)
+        split_task(s, task_add(s, 1, ci->progeny[split_pairs[sid][k][0]],
+                               cj->progeny[split_pairs[sid][k][1]]));
+    }
+  }
 }
 
 static void build_space(ospace *s, const oracle_params *prm, int n,
@@ -1621,9 +1704,11 @@ static void build_space(ospace *s, const oracle_params *prm, int n,
   free(counts);
   for (int cid = 0; cid < ntop; cid++)
     if (s->top[cid].count > 0) do_sort(&s->top[cid]);
-  /* Tasks and density links, in the order oracle/ref_harness.c uses. */
-  s->tasks = ocalloc((size_t)ntop * 14, sizeof(otask));
-  s->links = ocalloc((size_t)ntop * 28, sizeof(olink));
+  /* Tasks, in the order oracle/ref_harness.c creates them: per non-empty
+   * top cell its self task, then its pair tasks with the non-empty
+   * neighbours of higher index (26-neighbourhood, periodic). */
+  s->tcap = ntop * 14 + 16;
+  s->tasks = ocalloc((size_t)s->tcap, sizeof(otask));
   const int *cdim = s->cdim;
   for (int i = 0; i < cdim[0]; i++)
     for (int j = 0; j < cdim[1]; j++)
@@ -1631,10 +1716,7 @@ static void build_space(ospace *s, const oracle_params *prm, int n,
         const int cid = k + cdim[2] * (j + cdim[1] * i);
         ocell *ci = &s->top[cid];
         if (ci->count == 0) continue;
-        otask *t = &s->tasks[s->ntasks++];
-        t->is_pair = 0;
-        t->ci = ci;
-        link_add(s, ci, t);
+        task_add(s, 0, ci, NULL);
         for (int di = -1; di <= 1; di++)
           for (int dj = -1; dj <= 1; dj++)
             for (int dk = -1; dk <= 1; dk++) {
@@ -1650,14 +1732,25 @@ static void build_space(ospace *s, const oracle_params *prm, int n,
               if (cjd <= cid) continue;
               ocell *cj = &s->top[cjd];
               if (cj->count == 0) continue;
-              otask *tp = &s->tasks[s->ntasks++];
-              tp->is_pair = 1;
-              tp->ci = ci;
-              tp->cj = cj;
-              link_add(s, ci, tp);
-              link_add(s, cj, tp);
+              task_add(s, 1, ci, cj);
             }
       }
+  if (prm->subsize_self > 0 || prm->subsize_pair > 0) {
+    const int ntop_tasks = s->ntasks;
+    for (int t = 0; t < ntop_tasks; t++) split_task(s, t);
+    int kept = 0; /* drop the tasks the split left empty, keeping the order */
+    for (int t = 0; t < s->ntasks; t++)
+      if (s->tasks[t].ci != NULL) s->tasks[kept++] = s->tasks[t];
+    s->ntasks = kept;
+  }
+  /* Density links on the cells each task holds (engine_maketasks.c:
+   * 2311-2333), in task order. */
+  s->links = ocalloc((size_t)2 * s->ntasks + 1, sizeof(olink));
+  for (int t = 0; t < s->ntasks; t++) {
+    otask *tk = &s->tasks[t];
+    link_add(s, tk->ci, tk);
+    if (tk->is_pair) link_add(s, tk->cj, tk);
+  }
 }
 
 static void free_space(ospace *s) {
@@ -1812,6 +1905,7 @@ int sph_oracle_run(const oracle_params *prm, int n, const double *x,
   res->cdim[2] = s.cdim[2];
   res->ncells = s.pool.ncells;
   res->status = status;
+  res->ntasks = s.ntasks;
   free_space(&s);
   return status;
 }
@@ -1875,6 +1969,7 @@ int sph_oracle_run_state(const oracle_params *prm, int n, const double *x,
   res->cdim[2] = s.cdim[2];
   res->ncells = s.pool.ncells;
   res->status = 0;
+  res->ntasks = s.ntasks;
   free_space(&s);
   free(h);
   return 0;

@@ -31,6 +31,10 @@ typedef struct {
   int32_t periodic;
   float eta, h_tolerance, h_max, h_min, alpha;
   int32_t max_iter, max_active_bin, max_top_level_cells;
+  /* Task splitting (Scheduler:cell_sub_size_self_hydro / _pair_hydro):
+   * both 0 keeps one task per top cell and top-cell pair; otherwise the
+   * tasks are split as the reference's scheduler splits them. */
+  int32_t subsize_self, subsize_pair;
 } oracle_params;
 
 typedef struct {
@@ -39,6 +43,7 @@ typedef struct {
   int32_t cdim[3];
   int32_t ncells;
   int32_t status; /* 0 ok, 1 ghost did not converge */
+  int32_t ntasks; /* density tasks after splitting */
 } oracle_result;
 
 int sph_oracle_run(const oracle_params *prm, int n, const double *x,

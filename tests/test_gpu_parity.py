@@ -272,6 +272,33 @@ def test_open_box_parity(cfg, run, oracle_lib):
         assert scaled_err(force[k], ref[k]).max() < REL, k
 
 
+def test_parity_with_the_reference_task_split(oracle_lib):
+    """Against the oracle with the reference scheduler's task split
+    (scheduler_splittask_hydro; bit-identical to the reference run with its
+    own splitter): the planner's one task per top cell and top-cell pair
+    reaches the same cell pairs, so counts stay exact and the sums agree at
+    the usual tolerances."""
+    box = ics.make("clustered:24", seed=3)
+    run = {"max_top_level_cells": 3}
+    ref = oracle_lib.run(box, subsize_self=500, subsize_pair=256000000, **run)
+    assert ref["ntasks"] > oracle_lib.run(box, **run)["ntasks"]
+    with api.Space(box, **run) as sp:
+        sp.step(api.STAGE_DENSITY)
+        first = sp.download()
+        sp.step()
+        full = sp.download()
+        sp.force_from_state(ref["h"], ref["rho"], ref["f"], ref["pressure"],
+                            ref["soundspeed"], ref["balsara"])
+        force = sp.download()
+    assert np.array_equal(first["ngb_first"], ref["ngb_first"])
+    assert np.array_equal(force["ngb_force"], ref["ngb_force"])
+    assert rel_err(full["h"], ref["h"]).max() < 2e-4
+    for k in ("rho", "pressure", "soundspeed"):
+        assert rel_err(full[k], ref[k]).max() < 3e-4, k
+    for k in ("ax", "ay", "az", "u_dt", "h_dt"):
+        assert scaled_err(force[k], ref[k]).max() < REL, k
+
+
 @pytest.mark.parametrize("kind", ["rectangular", "faces", "h_min"])
 def test_special_boxes(kind, oracle_lib):
     import sys

@@ -360,6 +360,30 @@ int sphgpu_integ_timestep(const sphgpu_integ_params *ip, const sphgpu_integ_stat
 /* get_max_active_bin (timeline.h:146) */
 int sphgpu_integ_max_active_bin(int64_t ti);
 
+/* ---- Device-resident cell assignment ------------------------------------
+ * Replaces the cell assignment of space_rebuild (space_rebuild.c:49):
+ * space_regrid's top-level grid (space_regrid.c:46-121), the top cell of
+ * every particle (space_parts_get_cell_index, space_cell_index.c:64-150),
+ * the octree split of cells of more than 400 particles (space_split.c:
+ * 196-300, cell_split.c:55-175) and depth_h (cell_set_part_h_depth,
+ * cell.h:1787), computed on the device from positions x [3n] (FP64) and
+ * smoothing lengths h [n] already in device memory (the caller's order;
+ * periodic boxes are wrapped by one period as the rebuild does, x itself is
+ * not changed).  Outputs:
+ *   order [n]   device: the caller's index of each particle in cell order
+ *               (every cell of every level one contiguous range, ranges as
+ *               the reference's; inside a leaf, particles follow their
+ *               octant path, then the caller's order)
+ *   depth_h [n] device, cell order
+ *   cdim [3], *ncells, and cells [ncells][5] (host, may be NULL) in the
+ *               format and numbering of sphgpu_space_tree: first, count,
+ *               depth, parent, top.  With max_cells < *ncells the records
+ *               are not written and SPHGPU_EINVAL is returned.
+ * The call synchronises the stream (it reads back the grid and the tree). */
+int sphgpu_cell_assign(const sphgpu_params *prm, const double *x, const float *h,
+                       int64_t n, int32_t *order, int8_t *depth_h, int32_t cdim[3],
+                       int32_t *ncells, int32_t *cells, int32_t max_cells, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

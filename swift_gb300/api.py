@@ -119,6 +119,8 @@ SIGNATURES = {
     "sphgpu_hydro_sort": (ctypes.c_int, [_P, _I32, _P]),
     "sphgpu_space_tree": (ctypes.c_int, [_P, _P, _P]),
     "sphgpu_cell_sort": (ctypes.c_int, [_P, _I32, _I32, _P, _P]),
+    "sphgpu_cell_assign": (ctypes.c_int, [ctypes.POINTER(Params), _P, _P, ctypes.c_int64, _P,
+                                          _P, _P, _P, _P, _I32, _P]),
     "sphgpu_server_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64, _I32,
                                             ctypes.POINTER(_P)]),
     "sphgpu_server_destroy": (ctypes.c_int, [_P]),
@@ -178,6 +180,45 @@ def make_params(box, **kw):
     p.max_active_bin = kw.get("max_active_bin", box.get("max_active_bin",
                                                         p.max_active_bin))
     return p
+
+
+def cell_assign(x, h, dim, **params):
+    """The rebuild's cell assignment on the device (sphgpu_cell_assign).
+
+    ``x`` [n, 3] float64 and ``h`` [n] float32 are CUDA tensors (the caller's
+    order; numpy arrays are copied to the current CUDA device).  Returns
+    ``(order, depth_h, cells, cdim)``: ``order`` (int32) gives the caller's
+    index of every particle in cell order and ``depth_h`` (int8) its h-depth,
+    both CUDA tensors; ``cells`` is the int32 [ncells, 5] tree (first, count,
+    depth, parent, top; the numbering of :meth:`Space.tree`); ``cdim`` the
+    top-level grid."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    x = torch.as_tensor(x, dtype=torch.float64, device=dev).contiguous()
+    h = torch.as_tensor(h, dtype=torch.float32, device=dev).contiguous()
+    n = int(h.shape[0])
+    if x.shape != (n, 3):
+        raise ValueError("x must be [n, 3] with n = len(h)")
+    prm = make_params({"dim": dim}, **params)
+    order = torch.empty(n, dtype=torch.int32, device=dev)
+    depth_h = torch.empty(n, dtype=torch.int8, device=dev)
+    cdim = np.zeros(3, np.int32)
+    ncells = ctypes.c_int32()
+    # cells <= top cells + 8 children for each split (> 400 particles) per level
+    cap = (prm.max_top_level_cells + 2) ** 3 + n // 2 + 64
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    for _ in range(2):
+        cells = np.zeros((cap, 5), np.int32)
+        rc = lib().sphgpu_cell_assign(ctypes.byref(prm), ctypes.c_void_p(x.data_ptr()),
+                                      ctypes.c_void_p(h.data_ptr()), n,
+                                      ctypes.c_void_p(order.data_ptr()),
+                                      ctypes.c_void_p(depth_h.data_ptr()), _ptr(cdim),
+                                      ctypes.byref(ncells), _ptr(cells), cap, stream)
+        if rc == OK or ncells.value <= cap:
+            break
+        cap = ncells.value
+    _check(rc)
+    return order, depth_h, cells[:ncells.value].copy(), tuple(int(v) for v in cdim)
 
 
 def tuning_key(jtile, tpp, block_warps):

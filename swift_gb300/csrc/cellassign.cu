@@ -1,0 +1,564 @@
+// cellassign.cu -- the rebuild's cell assignment on the device, from
+// positions and smoothing lengths already in device memory:
+//   top-level grid      space_regrid (space_regrid.c:46-121), cell_min from
+//                       space.c:1263-1272 (Space::top_grid, shared with the
+//                       host build)
+//   top cell per part   space_parts_get_cell_index (space_cell_index.c:64-150)
+//   octree split        space_split_recursive (space_split.c:196-300) /
+//                       cell_split (cell_split.c:55-175): a cell of more than
+//                       400 particles splits at its centre into octants
+//   depth_h             cell_set_part_h_depth (cell.h:1787)
+//
+// Every particle gets one 64-bit key: its top cell in the high bits, then
+// the octant it falls in at every level below the top cell, three bits per
+// level, found with the split's own comparisons (x >= loc + width / 2, the
+// child's corner loc + width / 2, all in FP64).  A stable radix sort of the
+// keys puts every cell of every level in one contiguous range, in the
+// reference's cell order (top cells by cell_getid, octants 0..7 below).
+// Cell boundaries are then found level by level by binary searches in the
+// sorted keys; the host keeps only the tree (O(cells)).
+//
+// The result is the reference's tree: the same cells, the same particle
+// ranges and the same depth_h.  Inside a leaf the particles follow their
+// octant path below the leaf and then the caller's order, where the
+// reference's in-place bucket walk (space_sort.c:42-93) leaves another
+// order; nothing in the loops depends on the order inside a leaf except the
+// summation order.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <stdexcept>
+#include <vector>
+
+#include "../../include/swift_gb300.h"
+#include "capi_util.h"
+#include "space.h"
+#include "sph_types.h"
+
+namespace sphgpu {
+namespace {
+
+using capi::DBuf;
+using capi::fail;
+using capi::guard;
+
+constexpr int kThreads = 256;              // 8 warps
+constexpr int kWarpItems = 512;            // items per warp in the radix passes
+constexpr int kTile = 8 * kWarpItems;      // items per block
+constexpr int kScanItems = 8;              // items per thread in the scan
+constexpr int kScanTile = kThreads * kScanItems;
+
+enum CheckFlags : int {
+  kNonFinite = 1,     // a non-finite position
+  kOutside = 2,       // more than one box length outside the periodic box
+  kOutsideOpen = 4,   // outside the non-periodic box
+  kBadH = 8,          // h not positive and finite
+};
+
+struct Box {
+  double dim[3];
+  int periodic;
+};
+
+__global__ void ca_check(const double* __restrict__ x, const float* __restrict__ h, int n,
+                         Box box, unsigned* hmax_bits, int* flags) {
+  int bad = 0;
+  unsigned hb = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int d = 0; d < 3; d++) {
+      double xx = x[3 * (size_t)i + d];
+      if (!isfinite(xx)) {
+        bad |= kNonFinite;
+        continue;
+      }
+      if (box.periodic) {
+        xx = wrap_periodic(xx, box.dim[d]);
+        if (xx < 0.0 || xx > box.dim[d]) bad |= kOutside;
+      } else if (xx < 0.0 || xx >= box.dim[d]) {
+        bad |= kOutsideOpen;
+      }
+    }
+    const float hh = h[i];
+    if (!(hh > 0.f) || !isfinite(hh))
+      bad |= kBadH;
+    else
+      hb = max(hb, __float_as_uint(hh));  // positive floats order as their bits
+  }
+  hb = __reduce_max_sync(0xffffffffu, hb);
+  bad = __reduce_or_sync(0xffffffffu, (unsigned)bad);
+  if ((threadIdx.x & 31) == 0) {
+    if (hb) atomicMax(hmax_bits, hb);
+    if (bad) atomicOr(flags, bad);
+  }
+}
+
+struct Grid {
+  double dim[3], width[3], iw[3];
+  int cdim[3];
+  int periodic, levels, path_bits;
+};
+
+// Key of every particle: top cell << path_bits | octant path (levels x 3
+// bits, the first level highest); the value is the particle's index.
+__global__ void ca_keys(const double* __restrict__ x, int n, Grid g,
+                        unsigned long long* __restrict__ key, int* __restrict__ val) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double pos[3];
+    for (int d = 0; d < 3; d++) {
+      double xx = x[3 * (size_t)i + d];
+      if (g.periodic) xx = wrap_periodic(xx, g.dim[d]);
+      if (xx == g.dim[d]) xx = 0.0;
+      pos[d] = xx;
+    }
+    const int top = top_cell_index(pos, g.iw, g.cdim);
+    const int c2 = top % g.cdim[2], c1 = (top / g.cdim[2]) % g.cdim[1],
+              c0 = top / (g.cdim[2] * g.cdim[1]);
+    double loc[3] = {c0 * g.width[0], c1 * g.width[1], c2 * g.width[2]};
+    double w[3] = {g.width[0], g.width[1], g.width[2]};
+    unsigned long long path = 0;
+    for (int l = 0; l < g.levels; l++) {
+      int digit = 0;
+      for (int d = 0; d < 3; d++) {
+        const double half = w[d] / 2;
+        const double pivot = loc[d] + half;
+        const int b = pos[d] >= pivot;
+        digit = 2 * digit + b;
+        if (b) loc[d] = pivot;
+        w[d] = half;
+      }
+      path = (path << 3) | (unsigned long long)digit;
+    }
+    key[i] = ((unsigned long long)top << g.path_bits) | path;
+    val[i] = i;
+  }
+}
+
+// --- stable LSD radix sort, 8 bits per pass ---------------------------------
+
+__device__ __forceinline__ int digit_of(unsigned long long k, int shift) {
+  return (int)((k >> shift) & 0xffu);
+}
+
+// Per-block digit counts, digit-major: hist[d * nblocks + block].
+__global__ void rs_hist(const unsigned long long* __restrict__ key, int n, int shift,
+                        unsigned* __restrict__ hist) {
+  __shared__ unsigned cnt[256];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kTile;
+  for (int t = threadIdx.x; t < kTile; t += kThreads) {
+    const long long e = base + t;
+    if (e < n) atomicAdd(&cnt[digit_of(key[e], shift)], 1u);
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// Exclusive scan of a[0, n) in tiles of kScanTile; tile totals to sums.
+__global__ void scan_tiles(unsigned* __restrict__ a, long long n, unsigned* __restrict__ sums) {
+  __shared__ unsigned wsum[kThreads / 32];
+  const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+  unsigned v[kScanItems], run = 0;
+  for (int k = 0; k < kScanItems; k++) {
+    v[k] = base + k < n ? a[base + k] : 0u;
+    run += v[k];
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned inc = run;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  unsigned wpre = 0, tot = 0;
+  for (int k = 0; k < kThreads / 32; k++) {
+    if (k < w) wpre += wsum[k];
+    tot += wsum[k];
+  }
+  unsigned ex = wpre + inc - run;
+  for (int k = 0; k < kScanItems; k++) {
+    if (base + k < n) a[base + k] = ex;
+    ex += v[k];
+  }
+  if (threadIdx.x == 0 && sums) sums[blockIdx.x] = tot;
+}
+
+__global__ void add_tile_offsets(unsigned* __restrict__ a, long long n,
+                                 const unsigned* __restrict__ offs) {
+  const long long base = (long long)blockIdx.x * kScanTile;
+  const unsigned o = offs[blockIdx.x];
+  for (int t = threadIdx.x; t < kScanTile; t += kThreads)
+    if (base + t < n) a[base + t] += o;
+}
+
+// Stable scatter: warp w of a block owns items [w * 512, (w + 1) * 512) of
+// the block's tile and places them in index order, 32 at a time; lanes with
+// the same digit in one round are ranked by lane.
+__global__ void rs_scatter(const unsigned long long* __restrict__ kin, const int* __restrict__ vin,
+                           unsigned long long* __restrict__ kout, int* __restrict__ vout, int n,
+                           int shift, const unsigned* __restrict__ offs) {
+  __shared__ unsigned wcnt[8][256];
+  for (int t = threadIdx.x; t < 8 * 256; t += kThreads) (&wcnt[0][0])[t] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long wbase = (long long)blockIdx.x * kTile + (long long)w * kWarpItems;
+  for (int r = 0; r < kWarpItems; r += 32) {
+    const long long e = wbase + r + lane;
+    if (e < n) atomicAdd(&wcnt[w][digit_of(kin[e], shift)], 1u);
+  }
+  __syncthreads();
+  {
+    const int d = threadIdx.x;
+    unsigned run = offs[(size_t)d * gridDim.x + blockIdx.x];
+    for (int k = 0; k < 8; k++) {
+      const unsigned c = wcnt[k][d];
+      wcnt[k][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+  for (int r = 0; r < kWarpItems; r += 32) {
+    const long long e = wbase + r + lane;
+    const bool ok = e < n;
+    unsigned long long k = 0;
+    int v = 0, d = 256 + lane;  // a lane past the end is alone in its group
+    if (ok) {
+      k = kin[e];
+      v = vin[e];
+      d = digit_of(k, shift);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    unsigned b = 0;
+    if (ok && lane == leader) b = wcnt[w][d];
+    b = __shfl_sync(0xffffffffu, b, leader);
+    if (ok) {
+      const unsigned pos = b + __popc(peers & lt);
+      kout[pos] = k;
+      vout[pos] = v;
+      if (lane == leader) wcnt[w][d] = b + __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+// --- tree ------------------------------------------------------------------
+
+__device__ __forceinline__ int lower_bound(const unsigned long long* __restrict__ key, int lo,
+                                           int hi, unsigned long long v) {
+  while (lo < hi) {
+    const int mid = lo + ((hi - lo) >> 1);
+    if (key[mid] < v)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Particle range of every top cell: int2 (first, count).
+__global__ void ca_top_ranges(const unsigned long long* __restrict__ key, int n, int ntop,
+                              int path_bits, int2* __restrict__ range) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntop) return;
+  const int a = lower_bound(key, 0, n, (unsigned long long)t << path_bits);
+  // (t + 1) << path_bits would leave the 64 bits for the last top cell
+  const int b = t + 1 < ntop ? lower_bound(key, a, n, (unsigned long long)(t + 1) << path_bits) : n;
+  range[t] = make_int2(a, b - a);
+}
+
+// Octant counts of every cell that splits: cell f = (first, count, depth);
+// its particles share the key bits above level depth; child k's range
+// starts at the first key with octant >= k at level depth.
+__global__ void ca_children(const unsigned long long* __restrict__ key, const int4* __restrict__ split,
+                            int nsplit, int levels, int* __restrict__ child_count) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nsplit) return;
+  const int4 c = split[f];
+  const int shift = 3 * (levels - c.z - 1);  // the child level's octant
+  const unsigned long long pre = key[c.x] >> (shift + 3) << (shift + 3);
+  int b[9];
+  b[0] = c.x;
+  b[8] = c.x + c.y;
+  for (int k = 1; k < 8; k++)
+    b[k] = lower_bound(key, b[k - 1], b[8], pre | ((unsigned long long)k << shift));
+  for (int k = 0; k < 8; k++) child_count[8 * f + k] = b[k + 1] - b[k];
+}
+
+// depth_h of every particle, one warp per leaf (first, count, depth).
+__global__ void ca_depth_h(const int4* __restrict__ leaf, int nleaf, const int* __restrict__ order,
+                           const float* __restrict__ h, const float* __restrict__ hmin_d,
+                           const float* __restrict__ hmax_d, int8_t* __restrict__ depth_h) {
+  const int lw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (lw >= nleaf) return;
+  const int4 L = leaf[lw];
+  for (int k = L.x + (threadIdx.x & 31); k < L.x + L.y; k += 32) {
+    const float hh = h[order[k]];
+    int dh = 0;  // above the top cell: the reference leaves depth_h as it was
+    if (hh < hmin_d[L.z]) {
+      dh = L.z;
+    } else {
+      for (int d = L.z; d >= 0; d--)
+        if (hh >= hmin_d[d] && hh < hmax_d[d]) {
+          dh = d;
+          break;
+        }
+    }
+    depth_h[k] = (int8_t)dh;
+  }
+}
+
+int blocks_for(long long n, int per_block, int cap = 152 * 32) {
+  const long long b = (n + per_block - 1) / per_block;
+  return (int)std::max(1LL, std::min<long long>(b, cap));
+}
+
+// Exclusive scan of a device array of n unsigned (n < 2^31).
+// tmp is a deque: its elements never move, so the buffers stay owned once.
+void exclusive_scan(unsigned* a, long long n, cudaStream_t st, std::deque<DBuf<unsigned>>& tmp) {
+  const long long tiles = (n + kScanTile - 1) / kScanTile;
+  if (tiles <= 1) {
+    scan_tiles<<<1, kThreads, 0, st>>>(a, n, nullptr);
+    CK(cudaGetLastError());
+    return;
+  }
+  tmp.emplace_back();
+  DBuf<unsigned>& sums = tmp.back();
+  sums.alloc((size_t)tiles);
+  unsigned* sp = sums.p;
+  scan_tiles<<<(unsigned)tiles, kThreads, 0, st>>>(a, n, sp);
+  CK(cudaGetLastError());
+  exclusive_scan(sp, tiles, st, tmp);
+  add_tile_offsets<<<(unsigned)tiles, kThreads, 0, st>>>(a, n, sp);
+  CK(cudaGetLastError());
+}
+
+struct HCell {
+  int first, count, depth, parent, top;
+  int child[8];
+};
+
+}  // namespace
+}  // namespace sphgpu
+
+using namespace sphgpu;
+
+int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h, int64_t n,
+                       int32_t* order, int8_t* depth_h, int32_t cdim_out[3], int32_t* ncells,
+                       int32_t* cells, int32_t max_cells, void* stream) {
+  if (!prm || !x || !h || !order || !depth_h || !cdim_out || !ncells || n <= 0)
+    return fail(SPHGPU_EINVAL, "sphgpu_cell_assign: null argument or n <= 0");
+  if (n > SPHGPU_MAX_PARTICLES)
+    return fail(SPHGPU_EINVAL, "sphgpu_cell_assign: more than SPHGPU_MAX_PARTICLES particles");
+  if (prm->max_top_level_cells < 3 || !(prm->dim[0] > 0) || !(prm->dim[1] > 0) ||
+      !(prm->dim[2] > 0))
+    return fail(SPHGPU_EINVAL, "sphgpu_cell_assign: invalid parameters");
+  return guard([&]() {
+    cudaStream_t st = (cudaStream_t)stream;
+    const int N = (int)n;
+    Params P;
+    for (int d = 0; d < 3; d++) P.dim[d] = prm->dim[d];
+    P.periodic = prm->periodic;
+    P.max_top_level_cells = prm->max_top_level_cells;
+
+    // 1. validation and the largest h
+    DBuf<unsigned> scal;
+    scal.alloc(2);
+    CK(cudaMemsetAsync(scal.p, 0, 2 * sizeof(unsigned), st));
+    Box box{{P.dim[0], P.dim[1], P.dim[2]}, P.periodic};
+    ca_check<<<blocks_for(N, kThreads), kThreads, 0, st>>>(x, h, N, box, scal.p,
+                                                            (int*)(scal.p + 1));
+    CK(cudaGetLastError());
+    unsigned hs[2];
+    CK(cudaMemcpyAsync(hs, scal.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (hs[1] & kNonFinite) throw std::runtime_error("non-finite position");
+    if (hs[1] & kOutside)
+      throw std::runtime_error("particle more than one box length outside the periodic box");
+    if (hs[1] & kOutsideOpen) throw std::runtime_error("particle outside the non-periodic box");
+    if (hs[1] & kBadH) throw std::runtime_error("smoothing lengths must be positive and finite");
+    float max_h;
+    std::memcpy(&max_h, &hs[0], sizeof(float));
+
+    // 2. grid and key layout
+    Grid g{};
+    Space::top_grid(P, max_h, g.cdim, g.width);
+    for (int d = 0; d < 3; d++) {
+      g.dim[d] = P.dim[d];
+      g.iw[d] = 1.0 / g.width[d];
+      cdim_out[d] = g.cdim[d];
+    }
+    g.periodic = P.periodic;
+    const long long ntop_l = (long long)g.cdim[0] * g.cdim[1] * g.cdim[2];
+    if (ntop_l > (1LL << 30)) throw std::runtime_error("too many top-level cells");
+    const int ntop = (int)ntop_l;
+    int top_bits = 1;
+    while ((1LL << top_bits) < ntop_l) top_bits++;
+    g.levels = std::min(SPH_MAX_DEPTH - 1, (64 - top_bits) / 3);
+    g.path_bits = 3 * g.levels;
+    const int key_bits = top_bits + g.path_bits;
+
+    // 3. keys, sorted
+    DBuf<unsigned long long> k0, k1;
+    DBuf<int> v1;
+    k0.alloc(N);
+    k1.alloc(N);
+    v1.alloc(N);
+    int* v0 = order;  // the sort ends in the caller's buffer after an even pass count
+    ca_keys<<<blocks_for(N, kThreads), kThreads, 0, st>>>(x, N, g, k0.p, v0);
+    CK(cudaGetLastError());
+    const int nblk = (int)((n + kTile - 1) / kTile);
+    DBuf<unsigned> hist;
+    hist.alloc((size_t)256 * nblk);
+    const int npass = (key_bits + 7) / 8;
+    unsigned long long *ka = k0.p, *kb = k1.p;
+    int *va = v0, *vb = v1.p;
+    std::deque<DBuf<unsigned>> scan_tmp;
+    for (int p = 0; p < npass; p++) {
+      const int shift = 8 * p;
+      rs_hist<<<nblk, kThreads, 0, st>>>(ka, N, shift, hist.p);
+      CK(cudaGetLastError());
+      exclusive_scan(hist.p, (long long)256 * nblk, st, scan_tmp);
+      rs_scatter<<<nblk, kThreads, 0, st>>>(ka, va, kb, vb, N, shift, hist.p);
+      CK(cudaGetLastError());
+      std::swap(ka, kb);
+      std::swap(va, vb);
+    }
+    if (va != order)
+      CK(cudaMemcpyAsync(order, va, sizeof(int) * (size_t)N, cudaMemcpyDeviceToDevice, st));
+    const unsigned long long* key = ka;
+
+    // 4. the tree, level by level
+    DBuf<int2> rng;
+    rng.alloc(ntop);
+    ca_top_ranges<<<(ntop + kThreads - 1) / kThreads, kThreads, 0, st>>>(key, N, ntop,
+                                                                          g.path_bits, rng.p);
+    CK(cudaGetLastError());
+    std::vector<int2> top(ntop);
+    CK(cudaMemcpyAsync(top.data(), rng.p, sizeof(int2) * ntop, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<HCell> hc(ntop);
+    long long total = 0;
+    for (int t = 0; t < ntop; t++) {
+      hc[t] = HCell{top[t].x, top[t].y, 0, -1, t, {-1, -1, -1, -1, -1, -1, -1, -1}};
+      total += top[t].y;
+    }
+    if (total != n) throw std::runtime_error("cell assignment lost particles");
+    std::vector<int> frontier;
+    for (int t = 0; t < ntop; t++)
+      if (hc[t].count > Space::kSplitSize) frontier.push_back(t);
+    DBuf<int4> fbuf;
+    DBuf<int> cbuf;
+    std::vector<int4> fh;
+    std::vector<int> ch;
+    while (!frontier.empty()) {
+      fh.resize(frontier.size());
+      for (size_t f = 0; f < frontier.size(); f++) {
+        const HCell& c = hc[frontier[f]];
+        if (c.depth >= SPH_MAX_DEPTH - 1)
+          throw std::runtime_error(
+              "cell tree deeper than supported (particles at identical positions?)");
+        if (c.depth >= g.levels)
+          throw std::runtime_error("cell tree deeper than the device keys resolve");
+        fh[f] = make_int4(c.first, c.count, c.depth, 0);
+      }
+      const int nf = (int)fh.size();
+      fbuf.upload(fh.data(), nf, st);
+      if (cbuf.n < (size_t)8 * nf) cbuf.alloc((size_t)8 * nf);
+      ca_children<<<(nf + kThreads - 1) / kThreads, kThreads, 0, st>>>(key, fbuf.p, nf,
+                                                                        g.levels, cbuf.p);
+      CK(cudaGetLastError());
+      ch.resize((size_t)8 * nf);
+      CK(cudaMemcpyAsync(ch.data(), cbuf.p, sizeof(int) * 8 * nf, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      std::vector<int> next;
+      for (int f = 0; f < nf; f++) {
+        const int pc = frontier[f];
+        int off = hc[pc].first;
+        for (int k = 0; k < 8; k++) {
+          const int cnt = ch[8 * f + k];
+          if (cnt == 0) continue;
+          HCell c{off, cnt, hc[pc].depth + 1, pc, hc[pc].top, {-1, -1, -1, -1, -1, -1, -1, -1}};
+          off += cnt;
+          hc[pc].child[k] = (int)hc.size();
+          if (cnt > Space::kSplitSize) next.push_back((int)hc.size());
+          hc.push_back(c);
+        }
+        if (off != hc[pc].first + hc[pc].count)
+          throw std::runtime_error("cell assignment lost particles in a split");
+      }
+      frontier.swap(next);
+    }
+
+    // 5. the host build's numbering: top cells in cell_getid order, then
+    // every top cell's subtree depth first, octants in order
+    const int nc = (int)hc.size();
+    *ncells = nc;
+    std::vector<int> id(nc, -1);
+    for (int t = 0; t < ntop; t++) id[t] = t;
+    int next_id = ntop;
+    std::vector<int> stack;
+    for (int t = 0; t < ntop; t++) {
+      // preorder: a child is numbered before its own children and after the
+      // whole subtree of the previous sibling
+      stack.assign(1, t);
+      while (!stack.empty()) {
+        const int c = stack.back();
+        stack.pop_back();
+        if (id[c] < 0) id[c] = next_id++;
+        for (int k = 7; k >= 0; k--)
+          if (hc[c].child[k] >= 0) stack.push_back(hc[c].child[k]);
+      }
+    }
+    if (cells && max_cells >= nc) {
+      for (int c = 0; c < nc; c++) {
+        int32_t* r = cells + 5 * (size_t)id[c];
+        r[0] = hc[c].first;
+        r[1] = hc[c].count;
+        r[2] = hc[c].depth;
+        r[3] = hc[c].parent >= 0 ? id[hc[c].parent] : -1;
+        r[4] = hc[c].top;
+      }
+    }
+
+    // 6. depth_h
+    float hmin_d[SPH_MAX_DEPTH], hmax_d[SPH_MAX_DEPTH];
+    {
+      float dmin = std::min(std::min((float)g.width[0], (float)g.width[1]), (float)g.width[2]);
+      for (int d = 0; d < SPH_MAX_DEPTH; d++) {
+        Cell c;
+        c.dmin = dmin;
+        c.h_min_allowed = c.dmin * 0.5 * (1. / SPH_KG);
+        c.h_max_allowed = c.dmin * (1. / SPH_KG);
+        hmin_d[d] = c.h_min_allowed;
+        hmax_d[d] = c.h_max_allowed;
+        dmin = c.dmin / 2;
+      }
+    }
+    std::vector<int4> leaves;
+    for (int c = 0; c < nc; c++)
+      if (hc[c].count > 0 && hc[c].count <= Space::kSplitSize)
+        leaves.push_back(make_int4(hc[c].first, hc[c].count, hc[c].depth, 0));
+    DBuf<int4> lbuf;
+    lbuf.upload(leaves.data(), leaves.size(), st);
+    DBuf<float> tab;
+    std::vector<float> tabh(hmin_d, hmin_d + SPH_MAX_DEPTH);
+    tabh.insert(tabh.end(), hmax_d, hmax_d + SPH_MAX_DEPTH);
+    tab.upload(tabh.data(), tabh.size(), st);
+    const int nl = (int)leaves.size();
+    ca_depth_h<<<(nl * 32 + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+        lbuf.p, nl, order, h, tab.p, tab.p + SPH_MAX_DEPTH, depth_h);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    if (cells && max_cells < nc)
+      return fail(SPHGPU_EINVAL, "sphgpu_cell_assign: cells buffer too small (see *ncells)");
+    return SPHGPU_OK;
+  });
+}

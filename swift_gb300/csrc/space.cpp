@@ -218,6 +218,25 @@ void Space::set_h_depth(int sorted_idx, int leaf) {
   }
 }
 
+void Space::top_grid(const Params& prm, float max_h, int cdim[3], double width[3]) {
+  // space_regrid (space_regrid.c:46-121) with cell_min from space_init
+  // (space.c:1263-1272): cells at least 1.10 * gamma * h_max wide, at most
+  // max_top_level_cells per side of the largest dimension.
+  const int maxt = prm.max_top_level_cells;
+  const double dmax = std::max(std::max(prm.dim[0], prm.dim[1]), prm.dim[2]);
+  const float tol = fmaxr((float)(1.0 - 1.0 / (maxt * maxt)), (float)0.99);
+  const double cell_min = tol * dmax / maxt;
+  float hmax = cell_min / SPH_KG / 1.10f;
+  if (max_h > hmax) hmax = max_h;
+  for (int d = 0; d < 3; d++) {
+    cdim[d] = (int)std::floor(prm.dim[d] / std::fmax(hmax * SPH_KG * 1.10f, cell_min));
+    if (cdim[d] < 1) throw std::runtime_error("top-level cell dimension of 0");
+    if (prm.periodic && cdim[d] < 3)
+      throw std::runtime_error("periodic box needs at least 3 top cells per axis");
+    width[d] = prm.dim[d] / cdim[d];
+  }
+}
+
 void Space::build(int64_t n, const double* x, const float* h,
                   const int8_t* time_bin) {
   if (n <= 0 || n > (int64_t)0x7fffffff - 16)
@@ -229,31 +248,21 @@ void Space::build(int64_t n, const double* x, const float* h,
       double& xx = x_[3 * (size_t)k + d];
       if (!std::isfinite(xx)) throw std::runtime_error("non-finite position");
       if (prm_.periodic) {
-        while (xx < 0) xx += prm_.dim[d];
-        while (xx >= prm_.dim[d]) xx -= prm_.dim[d];
+        xx = wrap_periodic(xx, prm_.dim[d]);
+        if (xx < 0 || xx > prm_.dim[d])
+          throw std::runtime_error("particle more than one box length outside the periodic box");
       } else if (xx < 0 || xx >= prm_.dim[d]) {
         throw std::runtime_error("particle outside the non-periodic box");
       }
     }
   // Top-level grid.
-  const int maxt = prm_.max_top_level_cells;
-  const double dmax = std::max(std::max(prm_.dim[0], prm_.dim[1]), prm_.dim[2]);
-  const float tol = fmaxr((float)(1.0 - 1.0 / (maxt * maxt)), (float)0.99);
-  const double cell_min = tol * dmax / maxt;
-  float hmax = cell_min / SPH_KG / 1.10f;
+  float max_h = 0.f;
   for (int k = 0; k < n_; k++) {
     if (!(h[k] > 0.f) || !std::isfinite(h[k]))
       throw std::runtime_error("smoothing lengths must be positive and finite");
-    if (h[k] > hmax) hmax = h[k];
+    if (h[k] > max_h) max_h = h[k];
   }
-  for (int d = 0; d < 3; d++) {
-    cdim_[d] = (int)std::floor(prm_.dim[d] /
-                               std::fmax(hmax * SPH_KG * 1.10f, cell_min));
-    if (cdim_[d] < 1) throw std::runtime_error("top-level cell dimension of 0");
-    if (prm_.periodic && cdim_[d] < 3)
-      throw std::runtime_error("periodic box needs at least 3 top cells per axis");
-    width_[d] = prm_.dim[d] / cdim_[d];
-  }
+  top_grid(prm_, max_h, cdim_, width_);
   const double iw[3] = {1.0 / width_[0], 1.0 / width_[1], 1.0 / width_[2]};
   const float dmin = fminr(fminr((float)width_[0], (float)width_[1]), (float)width_[2]);
   const int ntop = cdim_[0] * cdim_[1] * cdim_[2];
@@ -266,8 +275,7 @@ void Space::build(int64_t n, const double* x, const float* h,
       pos[d] = xx;
       x_[3 * (size_t)k + d] = xx;
     }
-    bin[k] = (int)(pos[2] * iw[2]) +
-             cdim_[2] * ((int)(pos[1] * iw[1]) + cdim_[1] * (int)(pos[0] * iw[0]));
+    bin[k] = top_cell_index(pos, iw, cdim_);
   }
   perm_.resize(n_);
   for (int k = 0; k < n_; k++) perm_[k] = k;

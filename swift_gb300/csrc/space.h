@@ -63,6 +63,9 @@ class Space {
   static constexpr int kRecurseSize = 100;   // space.h:64-65
 
   explicit Space(const Params& prm);
+  // Top-level grid for particles whose largest h is max_h: cells per side
+  // and cell widths (throws where the reference would refuse the box).
+  static void top_grid(const Params& prm, float max_h, int cdim[3], double width[3]);
   void build(int64_t n, const double* x, const float* h, const int8_t* time_bin);
   // Start of a step at max_active_bin, with the reference's drift at zero
   // displacement (cell_drift.c:330-371): active particles restart from the

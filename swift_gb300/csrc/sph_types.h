@@ -33,6 +33,25 @@ namespace sphgpu {
 #define SPH_GAMMA_M1 0.66666666666666667f
 #define SPH_VISC_BETA 3.0f
 
+// box_wrap(x, 0, dim) of the rebuild (periodic.h:34-40,
+// space_cell_index.c:113-116): one period back into the box.
+SPH_HD inline double wrap_periodic(double x, double dim) {
+  return x < 0.0 ? x + dim : (x >= dim ? x - dim : x);
+}
+
+// Top-level cell of a wrapped position (space_cell_index.c:126-128,
+// cell_getid cell.h:532): (int)(pos * (1 / width)) per axis.  A position
+// within rounding of the upper face can give cdim, which the reference
+// would index past its grid with; it is kept in the last cell here.
+SPH_HD inline int top_cell_index(const double pos[3], const double iw[3], const int cdim[3]) {
+  int c[3];
+  for (int d = 0; d < 3; d++) {
+    c[d] = (int)(pos[d] * iw[d]);
+    if (c[d] >= cdim[d]) c[d] = cdim[d] - 1;
+  }
+  return c[2] + cdim[2] * (c[1] + cdim[1] * c[0]);
+}
+
 // Kinds of reference evaluation frame.  The neighbour predicate r^2 < H^2
 // must be evaluated in the same frame, with the same roundings, as the
 // reference loop that owns the pair, or borderline pairs flip.

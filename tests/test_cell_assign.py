@@ -1,0 +1,120 @@
+"""Device-resident cell assignment (sphgpu_cell_assign): the rebuild's grid,
+top cells, octree split and depth_h computed on the GPU from positions in
+device memory, against the host build (sphgpu_space_create, bit-exact
+against the reference's space_rebuild) -- the same cell records in the same
+numbering, and for every particle the same leaf, depth_h and top cell."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from swift_gb300 import api, ics
+
+CASES = [("lattice:16", {}),
+         ("clustered:24", {"max_top_level_cells": 3}),
+         ("sedov:20", {}),
+         ("clustered:20", {"max_top_level_cells": 3, "periodic": 0})]
+
+
+def per_particle(order, depth_h, cells, n):
+    """Leaf first / count / depth and depth_h per particle (caller's order)
+    from the device outputs."""
+    parent = cells[:, 3]
+    split = np.zeros(len(cells), bool)
+    split[parent[parent >= 0]] = True
+    out = {k: np.full(n, -1, np.int64) for k in ("leaf_first", "leaf_count", "leaf_depth", "top")}
+    for c in np.nonzero(~split & (cells[:, 1] > 0))[0]:
+        first, count, depth, _, top = cells[c]
+        idx = order[first:first + count]
+        out["leaf_first"][idx] = first
+        out["leaf_count"][idx] = count
+        out["leaf_depth"][idx] = depth
+        out["top"][idx] = top
+    out["depth_h"] = np.empty(n, np.int64)
+    out["depth_h"][order] = depth_h
+    return out
+
+
+def check_against_host(box, run):
+    with api.Space(box, **run) as sp:
+        tree = sp.tree()
+        host = sp.cells()
+        info = sp.info()
+    order, dh, cells, cdim = api.cell_assign(box["x"], box["h"], box["dim"], **run)
+    order = order.cpu().numpy()
+    n = box["x"].shape[0]
+    assert cdim == (info["cdim0"], info["cdim1"], info["cdim2"])
+    assert np.array_equal(np.sort(order), np.arange(n))
+    assert np.array_equal(cells, tree)
+    dev = per_particle(order, dh.cpu().numpy(), cells, n)
+    for k in ("leaf_first", "leaf_count", "leaf_depth", "depth_h", "top"):
+        assert np.array_equal(dev[k], host[k]), k
+    return cells
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg,run", CASES)
+def test_device_tree_equals_host_tree(cfg, run):
+    box = ics.make(cfg, seed=7)
+    cells = check_against_host(box, run)
+    if "clustered:24" in cfg:
+        assert cells[:, 2].max() >= 1  # the split ran
+
+
+@pytest.mark.gpu
+def test_device_tree_deep_and_large():
+    """A deeper tree (three top cells per side, clustered) and a 2.1M
+    particle box."""
+    box = ics.clustered(40, seed=9, rms=0.8)
+    cells = check_against_host(box, {"max_top_level_cells": 3})
+    assert cells[:, 2].max() >= 2
+    check_against_host(ics.clustered(128, seed=1), {})
+
+
+@pytest.mark.gpu
+def test_device_tree_wraps_one_period():
+    """Positions one box length outside a periodic box are wrapped back as
+    the rebuild does; x itself is left alone."""
+    import torch
+    box = ics.clustered(24, seed=11)
+    shifted = dict(box)
+    x = box["x"].copy()
+    x[::3, 0] += 1.0
+    x[1::3, 1] -= 1.0
+    shifted["x"] = x
+    xd = torch.as_tensor(x, device="cuda")
+    a = api.cell_assign(xd, box["h"], box["dim"])
+    b = api.cell_assign(box["x"], box["h"], box["dim"])
+    assert np.array_equal(a[2], b[2])
+    assert np.array_equal(a[0].cpu().numpy(), b[0].cpu().numpy())
+    assert np.array_equal(xd.cpu().numpy(), x)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["nan", "outside_open", "h_zero", "two_periods"])
+def test_device_tree_rejects_bad_input(kind):
+    box = ics.lattice(12, seed=3)
+    x, h, run = box["x"].copy(), box["h"].copy(), {}
+    if kind == "nan":
+        x[5, 1] = np.nan
+    elif kind == "outside_open":
+        x[7, 2] = 1.25
+        run = {"periodic": 0}
+    elif kind == "h_zero":
+        h[9] = 0.0
+    else:
+        x[2, 0] = 2.5
+    with pytest.raises(api.SphGpuError) as e:
+        api.cell_assign(x, h, box["dim"], **run)
+    assert e.value.code == api.EINVAL
+
+
+def test_cell_assign_rejects_null_arguments():
+    L = api.lib()
+    p = api.Params()
+    L.sphgpu_default_params(ctypes.byref(p))
+    n = ctypes.c_int32()
+    cdim = (ctypes.c_int32 * 3)()
+    rc = L.sphgpu_cell_assign(ctypes.byref(p), None, None, 10, None, None, cdim,
+                              ctypes.byref(n), None, 0, None)
+    assert rc == api.EINVAL

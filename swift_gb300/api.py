@@ -204,8 +204,9 @@ def cell_assign(x, h, dim, **params):
     depth_h = torch.empty(n, dtype=torch.int8, device=dev)
     cdim = np.zeros(3, np.int32)
     ncells = ctypes.c_int32()
-    # cells <= top cells + 8 children for each split (> 400 particles) per level
-    cap = (prm.max_top_level_cells + 2) ** 3 + n // 2 + 64
+    # top cells + 8 children for each split cell (> 400 particles), with
+    # room for four levels of splits; a deeper tree is fetched again
+    cap = (prm.max_top_level_cells + 2) ** 3 + 32 * (n // 401) + 64
     stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
     for _ in range(2):
         cells = np.zeros((cap, 5), np.int32)

@@ -60,29 +60,11 @@ enum CheckFlags : int {
   kBadH = 8,          // h not positive and finite
 };
 
-struct Box {
-  double dim[3];
-  int periodic;
-};
-
-__global__ void ca_check(const double* __restrict__ x, const float* __restrict__ h, int n,
-                         Box box, unsigned* hmax_bits, int* flags) {
+// The largest h (and whether every h is positive and finite).
+__global__ void ca_check_h(const float* __restrict__ h, int n, unsigned* hmax_bits, int* flags) {
   int bad = 0;
   unsigned hb = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    for (int d = 0; d < 3; d++) {
-      double xx = x[3 * (size_t)i + d];
-      if (!isfinite(xx)) {
-        bad |= kNonFinite;
-        continue;
-      }
-      if (box.periodic) {
-        xx = wrap_periodic(xx, box.dim[d]);
-        if (xx < 0.0 || xx > box.dim[d]) bad |= kOutside;
-      } else if (xx < 0.0 || xx >= box.dim[d]) {
-        bad |= kOutsideOpen;
-      }
-    }
     const float hh = h[i];
     if (!(hh > 0.f) || !isfinite(hh))
       bad |= kBadH;
@@ -99,43 +81,92 @@ __global__ void ca_check(const double* __restrict__ x, const float* __restrict__
 
 struct Grid {
   double dim[3], width[3], iw[3];
+  long long dim_bits[3];  // the bits of dim: non-negative doubles order as their bits
+  double scale[3];        // 2^(levels + frac_bits) / width: x in fixed-point octant units
+  long long eps;          // fixed-point units within which x may fall on either side
+  int frac_bits;
   int cdim[3];
   int periodic, levels, path_bits;
 };
 
 // Key of every particle: top cell << path_bits | octant path (levels x 3
-// bits, the first level highest); the value is the particle's index.
+// bits, the first level highest); the value is the particle's index.  Bad
+// positions are flagged (the keys are then not used).
+//
+// The split compares x with the pivots loc + width / 2 that the FP64 chain
+// of child corners produces.  Those pivots lie within a few ulps of the
+// dyadic points i width + k width / 2^l, which are whole numbers in units
+// of the finest octant, T = x 2^levels / width.  T is taken in fixed point
+// (frac_bits fractional bits, one FP64 multiply); where it is farther than
+// eps from every whole number, its integer bits are the top cell and the
+// octants of all levels at once.  Otherwise (a position on or next to a
+// cell boundary) the rebuild's own FP64 chain decides.
 __global__ void ca_keys(const double* __restrict__ x, int n, Grid g,
-                        unsigned long long* __restrict__ key, int* __restrict__ val) {
+                        unsigned long long* __restrict__ key, int* __restrict__ val,
+                        int* __restrict__ flags) {
+  int bad = 0;
+  const long long one = 1LL << g.frac_bits, fmask = one - 1;
+  const long long qmask = (1LL << g.levels) - 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double pos[3];
+    bool chain = false;
+    long long c[3], q[3];
     for (int d = 0; d < 3; d++) {
       double xx = x[3 * (size_t)i + d];
-      if (g.periodic) xx = wrap_periodic(xx, g.dim[d]);
-      if (xx == g.dim[d]) xx = 0.0;
-      pos[d] = xx;
-    }
-    const int top = top_cell_index(pos, g.iw, g.cdim);
-    const int c2 = top % g.cdim[2], c1 = (top / g.cdim[2]) % g.cdim[1],
-              c0 = top / (g.cdim[2] * g.cdim[1]);
-    double loc[3] = {c0 * g.width[0], c1 * g.width[1], c2 * g.width[2]};
-    double w[3] = {g.width[0], g.width[1], g.width[2]};
-    unsigned long long path = 0;
-    for (int l = 0; l < g.levels; l++) {
-      int digit = 0;
-      for (int d = 0; d < 3; d++) {
-        const double half = w[d] / 2;
-        const double pivot = loc[d] + half;
-        const int b = pos[d] >= pivot;
-        digit = 2 * digit + b;
-        if (b) loc[d] = pivot;
-        w[d] = half;
+      long long b = __double_as_longlong(xx);
+      if (((b >> 52) & 0x7ff) == 0x7ff) {
+        bad |= kNonFinite;
+        xx = 0.0;
+        b = 0;
       }
-      path = (path << 3) | (unsigned long long)digit;
+      // outside [0, dim) (-0.0 counts as 0): the rebuild's wrap
+      if ((b < 0 && b != (long long)0x8000000000000000ULL) || b >= g.dim_bits[d]) {
+        if (g.periodic) {
+          xx = wrap_periodic(xx, g.dim[d]);
+          if (xx < 0.0 || xx > g.dim[d]) bad |= kOutside;
+        } else {
+          bad |= kOutsideOpen;
+        }
+        if (xx == g.dim[d]) xx = 0.0;
+      }
+      pos[d] = xx;
+      const long long t = (long long)(xx * g.scale[d]);
+      const long long fr = t & fmask;
+      c[d] = t >> (g.levels + g.frac_bits);
+      q[d] = (t >> g.frac_bits) & qmask;
+      if (t < 0 || fr < g.eps || fr > one - g.eps || c[d] >= g.cdim[d]) chain = true;
+    }
+    int top;
+    unsigned long long path = 0;
+    if (!chain) {
+      top = (int)(c[2] + g.cdim[2] * (c[1] + g.cdim[1] * c[0]));
+      for (int l = g.levels - 1; l >= 0; l--)
+        path = (path << 3) | (unsigned long long)((((q[0] >> l) & 1) << 2) |
+                                                  (((q[1] >> l) & 1) << 1) | ((q[2] >> l) & 1));
+    } else {
+      top = top_cell_index(pos, g.iw, g.cdim);
+      const int c2 = top % g.cdim[2], c1 = (top / g.cdim[2]) % g.cdim[1],
+                c0 = top / (g.cdim[2] * g.cdim[1]);
+      double loc[3] = {c0 * g.width[0], c1 * g.width[1], c2 * g.width[2]};
+      double w[3] = {g.width[0], g.width[1], g.width[2]};
+      for (int l = 0; l < g.levels; l++) {
+        int digit = 0;
+        for (int d = 0; d < 3; d++) {
+          const double half = w[d] / 2;
+          const double pivot = loc[d] + half;
+          const int bb = pos[d] >= pivot;
+          digit = 2 * digit + bb;
+          if (bb) loc[d] = pivot;
+          w[d] = half;
+        }
+        path = (path << 3) | (unsigned long long)digit;
+      }
     }
     key[i] = ((unsigned long long)top << g.path_bits) | path;
     val[i] = i;
   }
+  bad = __reduce_or_sync(0xffffffffu, (unsigned)bad);
+  if ((threadIdx.x & 31) == 0 && bad) atomicOr(flags, bad);
 }
 
 // --- stable LSD radix sort, 8 bits per pass ---------------------------------
@@ -345,6 +376,30 @@ struct HCell {
   int child[8];
 };
 
+// Device scratch kept between the calls of a host thread (a rebuild runs
+// every step); it grows to the largest box seen and moves with the device.
+struct Scratch {
+  int device = -1;
+  DBuf<unsigned long long> k0, k1;
+  DBuf<int> v1, cbuf, flags;
+  DBuf<unsigned> hist, scal;
+  DBuf<int2> rng;
+  DBuf<int4> fbuf, lbuf;
+  DBuf<float> tab;
+  template <class T>
+  static void ensure(DBuf<T>& b, size_t count) {
+    if (b.n < count || !b.p) b.alloc(count);
+  }
+  void on_device(int dev) {
+    if (dev == device) return;
+    k0.release(); k1.release(); v1.release(); cbuf.release(); flags.release();
+    hist.release(); scal.release(); rng.release(); fbuf.release(); lbuf.release();
+    tab.release();
+    device = dev;
+  }
+};
+thread_local Scratch g_scratch;
+
 }  // namespace
 }  // namespace sphgpu
 
@@ -368,21 +423,20 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
     P.periodic = prm->periodic;
     P.max_top_level_cells = prm->max_top_level_cells;
 
-    // 1. validation and the largest h
-    DBuf<unsigned> scal;
-    scal.alloc(2);
-    CK(cudaMemsetAsync(scal.p, 0, 2 * sizeof(unsigned), st));
-    Box box{{P.dim[0], P.dim[1], P.dim[2]}, P.periodic};
-    ca_check<<<blocks_for(N, kThreads), kThreads, 0, st>>>(x, h, N, box, scal.p,
-                                                            (int*)(scal.p + 1));
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    Scratch& S = g_scratch;
+    S.on_device(dev);
+
+    // 1. the largest h (positions are checked with the keys)
+    Scratch::ensure(S.scal, 2);
+    CK(cudaMemsetAsync(S.scal.p, 0, 2 * sizeof(unsigned), st));
+    ca_check_h<<<blocks_for(N, kThreads), kThreads, 0, st>>>(h, N, S.scal.p,
+                                                              (int*)(S.scal.p + 1));
     CK(cudaGetLastError());
     unsigned hs[2];
-    CK(cudaMemcpyAsync(hs, scal.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hs, S.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (hs[1] & kNonFinite) throw std::runtime_error("non-finite position");
-    if (hs[1] & kOutside)
-      throw std::runtime_error("particle more than one box length outside the periodic box");
-    if (hs[1] & kOutsideOpen) throw std::runtime_error("particle outside the non-periodic box");
     if (hs[1] & kBadH) throw std::runtime_error("smoothing lengths must be positive and finite");
     float max_h;
     std::memcpy(&max_h, &hs[0], sizeof(float));
@@ -401,100 +455,148 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
     const int ntop = (int)ntop_l;
     int top_bits = 1;
     while ((1LL << top_bits) < ntop_l) top_bits++;
-    g.levels = std::min(SPH_MAX_DEPTH - 1, (64 - top_bits) / 3);
-    g.path_bits = 3 * g.levels;
-    const int key_bits = top_bits + g.path_bits;
+    // Keys of at most 32 bits first (four radix passes); where the tree
+    // reaches below their levels, once more with as many levels as 64 bits
+    // hold.
+    const int levels_full = std::min(SPH_MAX_DEPTH - 1, (64 - top_bits) / 3);
+    const int levels_short = std::max(1, std::min(levels_full, (32 - top_bits) / 3));
 
-    // 3. keys, sorted
-    DBuf<unsigned long long> k0, k1;
-    DBuf<int> v1;
-    k0.alloc(N);
-    k1.alloc(N);
-    v1.alloc(N);
-    int* v0 = order;  // the sort ends in the caller's buffer after an even pass count
-    ca_keys<<<blocks_for(N, kThreads), kThreads, 0, st>>>(x, N, g, k0.p, v0);
-    CK(cudaGetLastError());
+    Scratch::ensure(S.k0, N);
+    Scratch::ensure(S.k1, N);
+    Scratch::ensure(S.v1, N);
     const int nblk = (int)((n + kTile - 1) / kTile);
-    DBuf<unsigned> hist;
-    hist.alloc((size_t)256 * nblk);
-    const int npass = (key_bits + 7) / 8;
-    unsigned long long *ka = k0.p, *kb = k1.p;
-    int *va = v0, *vb = v1.p;
-    std::deque<DBuf<unsigned>> scan_tmp;
-    for (int p = 0; p < npass; p++) {
-      const int shift = 8 * p;
-      rs_hist<<<nblk, kThreads, 0, st>>>(ka, N, shift, hist.p);
-      CK(cudaGetLastError());
-      exclusive_scan(hist.p, (long long)256 * nblk, st, scan_tmp);
-      rs_scatter<<<nblk, kThreads, 0, st>>>(ka, va, kb, vb, N, shift, hist.p);
-      CK(cudaGetLastError());
-      std::swap(ka, kb);
-      std::swap(va, vb);
+    Scratch::ensure(S.hist, (size_t)256 * nblk);
+    Scratch::ensure(S.rng, ntop);
+    Scratch::ensure(S.flags, 1);
+    DBuf<unsigned long long>&k0 = S.k0, &k1 = S.k1;
+    DBuf<int>&v1 = S.v1, &cbuf = S.cbuf;
+    DBuf<unsigned>& hist = S.hist;
+    DBuf<int2>& rng = S.rng;
+    DBuf<int4>& fbuf = S.fbuf;
+    std::vector<HCell> hc;
+    hc.reserve((size_t)ntop + 16 * ((size_t)n / (Space::kSplitSize + 1)) + 64);
+    const unsigned long long* key = nullptr;
+    double wmin = g.width[0], dmax = g.dim[0];
+    for (int d = 1; d < 3; d++) {
+      wmin = std::min(wmin, g.width[d]);
+      dmax = std::max(dmax, g.dim[d]);
     }
-    if (va != order)
-      CK(cudaMemcpyAsync(order, va, sizeof(int) * (size_t)N, cudaMemcpyDeviceToDevice, st));
-    const unsigned long long* key = ka;
+    for (int attempt = 0; attempt < 2; attempt++) {
+      g.levels = attempt == 0 ? levels_short : levels_full;
+      g.path_bits = 3 * g.levels;
+      const int key_bits = top_bits + g.path_bits;
+      // Fixed point: T = x 2^levels / width < cdim 2^levels, held with
+      // frac_bits more bits while T 2^frac_bits stays exact in FP64 to 2^-1.
+      int axis_bits = 1;
+      for (int d = 0; d < 3; d++)
+        while ((1LL << axis_bits) < g.cdim[d]) axis_bits++;
+      g.frac_bits = std::max(0, std::min(20, 51 - g.levels - axis_bits));
+      for (int d = 0; d < 3; d++) {
+        g.scale[d] = std::ldexp(std::ldexp(1.0, g.levels) * g.iw[d], g.frac_bits);
+        std::memcpy(&g.dim_bits[d], &g.dim[d], sizeof(double));
+      }
+      // Distance (octant units) between a chain pivot and its dyadic point
+      // (a rounding per level of the corner chain and of loc_top), plus the
+      // rounding of T itself and the fixed-point truncation, generously.
+      const double tmax = std::ldexp(1.0, g.levels);
+      const double eps_t = 1024.0 * DBL_EPSILON * dmax * tmax / wmin +
+                           8.0 * std::ldexp(1.0, g.levels + axis_bits - 52);
+      g.eps = (long long)std::ceil(eps_t * std::ldexp(1.0, g.frac_bits)) + 2;
 
-    // 4. the tree, level by level
-    DBuf<int2> rng;
-    rng.alloc(ntop);
-    ca_top_ranges<<<(ntop + kThreads - 1) / kThreads, kThreads, 0, st>>>(key, N, ntop,
-                                                                          g.path_bits, rng.p);
-    CK(cudaGetLastError());
-    std::vector<int2> top(ntop);
-    CK(cudaMemcpyAsync(top.data(), rng.p, sizeof(int2) * ntop, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    std::vector<HCell> hc(ntop);
-    long long total = 0;
-    for (int t = 0; t < ntop; t++) {
-      hc[t] = HCell{top[t].x, top[t].y, 0, -1, t, {-1, -1, -1, -1, -1, -1, -1, -1}};
-      total += top[t].y;
-    }
-    if (total != n) throw std::runtime_error("cell assignment lost particles");
-    std::vector<int> frontier;
-    for (int t = 0; t < ntop; t++)
-      if (hc[t].count > Space::kSplitSize) frontier.push_back(t);
-    DBuf<int4> fbuf;
-    DBuf<int> cbuf;
-    std::vector<int4> fh;
-    std::vector<int> ch;
-    while (!frontier.empty()) {
-      fh.resize(frontier.size());
-      for (size_t f = 0; f < frontier.size(); f++) {
-        const HCell& c = hc[frontier[f]];
-        if (c.depth >= SPH_MAX_DEPTH - 1)
-          throw std::runtime_error(
-              "cell tree deeper than supported (particles at identical positions?)");
-        if (c.depth >= g.levels)
-          throw std::runtime_error("cell tree deeper than the device keys resolve");
-        fh[f] = make_int4(c.first, c.count, c.depth, 0);
-      }
-      const int nf = (int)fh.size();
-      fbuf.upload(fh.data(), nf, st);
-      if (cbuf.n < (size_t)8 * nf) cbuf.alloc((size_t)8 * nf);
-      ca_children<<<(nf + kThreads - 1) / kThreads, kThreads, 0, st>>>(key, fbuf.p, nf,
-                                                                        g.levels, cbuf.p);
+      // 3. keys, sorted
+      int* v0 = order;  // the sort ends in the caller's buffer after an even pass count
+      CK(cudaMemsetAsync(S.flags.p, 0, sizeof(int), st));
+      ca_keys<<<blocks_for(N, kThreads), kThreads, 0, st>>>(x, N, g, k0.p, v0, S.flags.p);
       CK(cudaGetLastError());
-      ch.resize((size_t)8 * nf);
-      CK(cudaMemcpyAsync(ch.data(), cbuf.p, sizeof(int) * 8 * nf, cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      std::vector<int> next;
-      for (int f = 0; f < nf; f++) {
-        const int pc = frontier[f];
-        int off = hc[pc].first;
-        for (int k = 0; k < 8; k++) {
-          const int cnt = ch[8 * f + k];
-          if (cnt == 0) continue;
-          HCell c{off, cnt, hc[pc].depth + 1, pc, hc[pc].top, {-1, -1, -1, -1, -1, -1, -1, -1}};
-          off += cnt;
-          hc[pc].child[k] = (int)hc.size();
-          if (cnt > Space::kSplitSize) next.push_back((int)hc.size());
-          hc.push_back(c);
-        }
-        if (off != hc[pc].first + hc[pc].count)
-          throw std::runtime_error("cell assignment lost particles in a split");
+      const int npass = (key_bits + 7) / 8;
+      unsigned long long *ka = k0.p, *kb = k1.p;
+      int *va = v0, *vb = v1.p;
+      std::deque<DBuf<unsigned>> scan_tmp;
+      for (int p = 0; p < npass; p++) {
+        const int shift = 8 * p;
+        rs_hist<<<nblk, kThreads, 0, st>>>(ka, N, shift, hist.p);
+        CK(cudaGetLastError());
+        exclusive_scan(hist.p, (long long)256 * nblk, st, scan_tmp);
+        rs_scatter<<<nblk, kThreads, 0, st>>>(ka, va, kb, vb, N, shift, hist.p);
+        CK(cudaGetLastError());
+        std::swap(ka, kb);
+        std::swap(va, vb);
       }
-      frontier.swap(next);
+      if (va != order)
+        CK(cudaMemcpyAsync(order, va, sizeof(int) * (size_t)N, cudaMemcpyDeviceToDevice, st));
+      key = ka;
+
+      // 4. the tree, level by level
+      ca_top_ranges<<<(ntop + kThreads - 1) / kThreads, kThreads, 0, st>>>(key, N, ntop,
+                                                                            g.path_bits, rng.p);
+      CK(cudaGetLastError());
+      std::vector<int2> top(ntop);
+      CK(cudaMemcpyAsync(top.data(), rng.p, sizeof(int2) * ntop, cudaMemcpyDeviceToHost, st));
+      int bad = 0;
+      CK(cudaMemcpyAsync(&bad, S.flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      if (bad & kNonFinite) throw std::runtime_error("non-finite position");
+      if (bad & kOutside)
+        throw std::runtime_error("particle more than one box length outside the periodic box");
+      if (bad & kOutsideOpen) throw std::runtime_error("particle outside the non-periodic box");
+      hc.assign(ntop, HCell{});
+      long long total = 0;
+      for (int t = 0; t < ntop; t++) {
+        hc[t] = HCell{top[t].x, top[t].y, 0, -1, t, {-1, -1, -1, -1, -1, -1, -1, -1}};
+        total += top[t].y;
+      }
+      if (total != n) throw std::runtime_error("cell assignment lost particles");
+      std::vector<int> frontier;
+      for (int t = 0; t < ntop; t++)
+        if (hc[t].count > Space::kSplitSize) frontier.push_back(t);
+      std::vector<int4> fh;
+      std::vector<int> ch;
+      bool deeper = false;
+      while (!frontier.empty() && !deeper) {
+        fh.resize(frontier.size());
+        for (size_t f = 0; f < frontier.size(); f++) {
+          const HCell& c = hc[frontier[f]];
+          if (c.depth >= SPH_MAX_DEPTH - 1)
+            throw std::runtime_error(
+                "cell tree deeper than supported (particles at identical positions?)");
+          if (c.depth >= g.levels) {
+            if (g.levels == levels_full)
+              throw std::runtime_error("cell tree deeper than the device keys resolve");
+            deeper = true;
+          }
+          fh[f] = make_int4(c.first, c.count, c.depth, 0);
+        }
+        if (deeper) break;
+        const int nf = (int)fh.size();
+        fbuf.upload(fh.data(), nf, st);
+        if (cbuf.n < (size_t)8 * nf) cbuf.alloc((size_t)8 * nf);
+        ca_children<<<(nf + kThreads - 1) / kThreads, kThreads, 0, st>>>(key, fbuf.p, nf,
+                                                                          g.levels, cbuf.p);
+        CK(cudaGetLastError());
+        ch.resize((size_t)8 * nf);
+        CK(cudaMemcpyAsync(ch.data(), cbuf.p, sizeof(int) * 8 * nf, cudaMemcpyDeviceToHost,
+                           st));
+        CK(cudaStreamSynchronize(st));
+        std::vector<int> next;
+        for (int f = 0; f < nf; f++) {
+          const int pc = frontier[f];
+          int off = hc[pc].first;
+          for (int k = 0; k < 8; k++) {
+            const int cnt = ch[8 * f + k];
+            if (cnt == 0) continue;
+            HCell c{off, cnt, hc[pc].depth + 1, pc, hc[pc].top,
+                    {-1, -1, -1, -1, -1, -1, -1, -1}};
+            off += cnt;
+            hc[pc].child[k] = (int)hc.size();
+            if (cnt > Space::kSplitSize) next.push_back((int)hc.size());
+            hc.push_back(c);
+          }
+          if (off != hc[pc].first + hc[pc].count)
+            throw std::runtime_error("cell assignment lost particles in a split");
+        }
+        frontier.swap(next);
+      }
+      if (!deeper) break;
     }
 
     // 5. the host build's numbering: top cells in cell_getid order, then
@@ -546,9 +648,9 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
     for (int c = 0; c < nc; c++)
       if (hc[c].count > 0 && hc[c].count <= Space::kSplitSize)
         leaves.push_back(make_int4(hc[c].first, hc[c].count, hc[c].depth, 0));
-    DBuf<int4> lbuf;
+    DBuf<int4>& lbuf = S.lbuf;
     lbuf.upload(leaves.data(), leaves.size(), st);
-    DBuf<float> tab;
+    DBuf<float>& tab = S.tab;
     std::vector<float> tabh(hmin_d, hmin_d + SPH_MAX_DEPTH);
     tabh.insert(tabh.end(), hmax_d, hmax_d + SPH_MAX_DEPTH);
     tab.upload(tabh.data(), tabh.size(), st);

@@ -72,6 +72,23 @@ def test_device_tree_deep_and_large():
 
 
 @pytest.mark.gpu
+def test_device_tree_deeper_than_the_short_keys():
+    """600 particles packed in a cube of side 1e-5 split down to depth ~15,
+    below the levels the first (32-bit) keys hold: the call sorts again
+    with 64-bit keys and still gives the host build's tree."""
+    box = ics.lattice(12, seed=5)
+    rng = np.random.default_rng(5)
+    extra = 0.5 + 1e-5 * rng.random((600, 3))
+    for k, v in (("x", extra), ("v", np.zeros((600, 3), np.float32)),
+                 ("m", np.full(600, box["m"][0], np.float32)),
+                 ("h", np.full(600, box["h"][0], np.float32)),
+                 ("u", np.ones(600, np.float32)), ("time_bin", np.zeros(600, np.int8))):
+        box[k] = np.concatenate([box[k], v.astype(box[k].dtype)])
+    cells = check_against_host(box, {"max_top_level_cells": 3})
+    assert cells[:, 2].max() >= 12
+
+
+@pytest.mark.gpu
 def test_device_tree_wraps_one_period():
     """Positions one box length outside a periodic box are wrapped back as
     the rebuild does; x itself is left alone."""

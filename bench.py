@@ -476,11 +476,13 @@ def run_rebuild(args):
     torch.cuda.synchronize()
     clocks = ClockSampler(local_rank)
     t_dev, t_e2e = [], []
+    phases = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         order, dh, cells, cdim = api.cell_assign(xd, hd, box["dim"])
         torch.cuda.synchronize()
         t_dev.append(time.perf_counter() - t0)
+        phases.append(api.cell_assign_times())
     for _ in range(args.steps):
         t0 = time.perf_counter()
         xd.copy_(xh, non_blocking=True)
@@ -507,6 +509,7 @@ def run_rebuild(args):
                    "l2": "inputs larger than L2 (x 24 B + h 4 B per particle)"},
         "e2e": {"value": n / de, "unit": "particles/s", "h2d_bytes_per_step": n * 28,
                 "d2h_bytes_per_step": n * 5},
+        "phases_ms": {k: statistics.median(p[k] for p in phases) for k in phases[0]},
         "host_space_create_s": t_host,
         "tree_equals_host_build": same,
         "gpu_launches": None,

@@ -121,6 +121,7 @@ SIGNATURES = {
     "sphgpu_cell_sort": (ctypes.c_int, [_P, _I32, _I32, _P, _P]),
     "sphgpu_cell_assign": (ctypes.c_int, [ctypes.POINTER(Params), _P, _P, ctypes.c_int64, _P,
                                           _P, _P, _P, _P, _I32, _P]),
+    "sphgpu_cell_assign_times": (ctypes.c_int, [_P]),
     "sphgpu_server_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64, _I32,
                                             ctypes.POINTER(_P)]),
     "sphgpu_server_destroy": (ctypes.c_int, [_P]),
@@ -220,6 +221,15 @@ def cell_assign(x, h, dim, **params):
         cap = ncells.value
     _check(rc)
     return order, depth_h, cells[:ncells.value].copy(), tuple(int(v) for v in cdim)
+
+
+def cell_assign_times():
+    """Host-clock phases (ms) of this thread's last :func:`cell_assign`: h scan
+    and grid, keys and sort, tree levels, numbering and records, depth_h."""
+    ms = np.zeros(5, np.float64)
+    _check(lib().sphgpu_cell_assign_times(_ptr(ms)))
+    return dict(zip(("grid", "keys_sort", "tree_levels", "numbering", "depth_h"),
+                    (float(v) for v in ms)))
 
 
 def tuning_key(jtile, tpp, block_warps):

@@ -29,6 +29,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <deque>
@@ -48,7 +49,7 @@ using capi::fail;
 using capi::guard;
 
 constexpr int kThreads = 256;              // 8 warps
-constexpr int kWarpItems = 512;            // items per warp in the radix passes
+constexpr int kWarpItems = 256;            // items per warp in the radix passes
 constexpr int kTile = 8 * kWarpItems;      // items per block
 constexpr int kScanItems = 8;              // items per thread in the scan
 constexpr int kScanTile = kThreads * kScanItems;
@@ -228,25 +229,46 @@ __global__ void add_tile_offsets(unsigned* __restrict__ a, long long n,
     if (base + t < n) a[base + t] += o;
 }
 
-// Stable scatter: warp w of a block owns items [w * 512, (w + 1) * 512) of
-// the block's tile and places them in index order, 32 at a time; lanes with
-// the same digit in one round are ranked by lane.
+// Stable scatter: warp w of a block owns items [w * 256, (w + 1) * 256) of
+// the block's tile and ranks them in index order, 32 at a time (lanes with
+// the same digit in one round are ranked by lane); the tile is first
+// ordered by digit in shared memory, then written out in runs of equal
+// digits, so that consecutive threads store to consecutive addresses.
 __global__ void rs_scatter(const unsigned long long* __restrict__ kin, const int* __restrict__ vin,
                            unsigned long long* __restrict__ kout, int* __restrict__ vout, int n,
                            int shift, const unsigned* __restrict__ offs) {
   __shared__ unsigned wcnt[8][256];
+  __shared__ unsigned dstart[256], goff[256], wtot[8];
+  __shared__ unsigned long long sk[kTile];
+  __shared__ int sv[kTile];
   for (int t = threadIdx.x; t < 8 * 256; t += kThreads) (&wcnt[0][0])[t] = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const long long wbase = (long long)blockIdx.x * kTile + (long long)w * kWarpItems;
+  const long long tbase = (long long)blockIdx.x * kTile;
+  const long long wbase = tbase + (long long)w * kWarpItems;
   for (int r = 0; r < kWarpItems; r += 32) {
     const long long e = wbase + r + lane;
     if (e < n) atomicAdd(&wcnt[w][digit_of(kin[e], shift)], 1u);
   }
   __syncthreads();
   {
+    // digit d = thread: its count in the tile, the tile's exclusive prefix
+    // over digits (block scan), then per-warp starts inside the digit's run
     const int d = threadIdx.x;
-    unsigned run = offs[(size_t)d * gridDim.x + blockIdx.x];
+    unsigned tot = 0;
+    for (int k = 0; k < 8; k++) tot += wcnt[k][d];
+    unsigned inc = tot;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) wtot[w] = inc;
+    __syncthreads();
+    unsigned pre = 0;
+    for (int k = 0; k < w; k++) pre += wtot[k];
+    unsigned run = pre + inc - tot;
+    dstart[d] = run;
+    goff[d] = offs[(size_t)d * gridDim.x + blockIdx.x];
     for (int k = 0; k < 8; k++) {
       const unsigned c = wcnt[k][d];
       wcnt[k][d] = run;
@@ -272,11 +294,20 @@ __global__ void rs_scatter(const unsigned long long* __restrict__ kin, const int
     b = __shfl_sync(0xffffffffu, b, leader);
     if (ok) {
       const unsigned pos = b + __popc(peers & lt);
-      kout[pos] = k;
-      vout[pos] = v;
+      sk[pos] = k;
+      sv[pos] = v;
       if (lane == leader) wcnt[w][d] = b + __popc(peers);
     }
     __syncwarp();
+  }
+  __syncthreads();
+  const int tcount = (int)min((long long)kTile, (long long)n - tbase);
+  for (int t = threadIdx.x; t < tcount; t += kThreads) {
+    const unsigned long long k = sk[t];
+    const int d = digit_of(k, shift);
+    const unsigned dst = goff[d] + (unsigned)t - dstart[d];
+    kout[dst] = k;
+    vout[dst] = sv[t];
   }
 }
 
@@ -324,12 +355,13 @@ __global__ void ca_children(const unsigned long long* __restrict__ key, const in
 }
 
 // depth_h of every particle, one warp per leaf (first, count, depth).
-__global__ void ca_depth_h(const int4* __restrict__ leaf, int nleaf, const int* __restrict__ order,
+__global__ void ca_depth_h(const int2* __restrict__ leaf, int nleaf, const int* __restrict__ order,
                            const float* __restrict__ h, const float* __restrict__ hmin_d,
                            const float* __restrict__ hmax_d, int8_t* __restrict__ depth_h) {
   const int lw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (lw >= nleaf) return;
-  const int4 L = leaf[lw];
+  const int2 l2 = leaf[lw];  // first, count | depth << 16
+  const int4 L = make_int4(l2.x, l2.y & 0xffff, l2.y >> 16, 0);
   for (int k = L.x + (threadIdx.x & 31); k < L.x + L.y; k += 32) {
     const float hh = h[order[k]];
     int dh = 0;  // above the top cell: the reference leaves depth_h as it was
@@ -371,9 +403,47 @@ void exclusive_scan(unsigned* a, long long n, cudaStream_t st, std::deque<DBuf<u
   CK(cudaGetLastError());
 }
 
-struct HCell {
-  int first, count, depth, parent, top;
-  int child[8];
+// The tree on the host, one entry per cell in creation order (top cells,
+// then every level's children, a parent's children consecutive).
+struct Tree {
+  std::vector<int> first, count, depth, parent, top, kid0, nkid;
+  void clear() {
+    for (auto* v : {&first, &count, &depth, &parent, &top, &kid0, &nkid}) v->clear();
+  }
+  void reserve(size_t m) {
+    for (auto* v : {&first, &count, &depth, &parent, &top, &kid0, &nkid}) v->reserve(m);
+  }
+  int add(int f, int c, int d, int p, int t) {
+    first.push_back(f);
+    count.push_back(c);
+    depth.push_back(d);
+    parent.push_back(p);
+    top.push_back(t);
+    kid0.push_back(-1);
+    nkid.push_back(0);
+    return (int)first.size() - 1;
+  }
+  int size() const { return (int)first.size(); }
+};
+
+// Page-locked host staging that grows as needed.
+template <class T>
+struct Pinned {
+  T* p = nullptr;
+  size_t n = 0;
+  T* get(size_t count) {
+    if (count > n) {
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+      n = 0;
+      CK(cudaMallocHost(&p, std::max<size_t>(count, 1) * sizeof(T)));
+      n = count;
+    }
+    return p;
+  }
+  ~Pinned() {
+    if (p) cudaFreeHost(p);
+  }
 };
 
 // Device scratch kept between the calls of a host thread (a rebuild runs
@@ -384,8 +454,11 @@ struct Scratch {
   DBuf<int> v1, cbuf, flags;
   DBuf<unsigned> hist, scal;
   DBuf<int2> rng;
-  DBuf<int4> fbuf, lbuf;
+  DBuf<int4> fbuf;
+  DBuf<int2> lbuf;
   DBuf<float> tab;
+  Pinned<int> ch;
+  Pinned<int2> leaves;
   template <class T>
   static void ensure(DBuf<T>& b, size_t count) {
     if (b.n < count || !b.p) b.alloc(count);
@@ -399,6 +472,18 @@ struct Scratch {
   }
 };
 thread_local Scratch g_scratch;
+
+// Host-clock phases of the calling thread's last call (ms): [0] h scan and
+// grid, [1] keys and sort, [2] tree levels, [3] numbering and records, [4]
+// depth_h (each up to its own synchronisation).
+thread_local double g_phase_ms[5];
+using Clock = std::chrono::steady_clock;
+double ms_since(Clock::time_point& t) {
+  const auto now = Clock::now();
+  const double ms = std::chrono::duration<double, std::milli>(now - t).count();
+  t = now;
+  return ms;
+}
 
 }  // namespace
 }  // namespace sphgpu
@@ -423,6 +508,8 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
     P.periodic = prm->periodic;
     P.max_top_level_cells = prm->max_top_level_cells;
 
+    auto tmark = Clock::now();
+    for (double& v : g_phase_ms) v = 0.0;
     int dev = 0;
     CK(cudaGetDevice(&dev));
     Scratch& S = g_scratch;
@@ -440,6 +527,7 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
     if (hs[1] & kBadH) throw std::runtime_error("smoothing lengths must be positive and finite");
     float max_h;
     std::memcpy(&max_h, &hs[0], sizeof(float));
+    g_phase_ms[0] += ms_since(tmark);
 
     // 2. grid and key layout
     Grid g{};
@@ -473,8 +561,8 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
     DBuf<unsigned>& hist = S.hist;
     DBuf<int2>& rng = S.rng;
     DBuf<int4>& fbuf = S.fbuf;
-    std::vector<HCell> hc;
-    hc.reserve((size_t)ntop + 16 * ((size_t)n / (Space::kSplitSize + 1)) + 64);
+    Tree T;
+    T.reserve((size_t)ntop + 16 * ((size_t)n / (Space::kSplitSize + 1)) + 64);
     const unsigned long long* key = nullptr;
     double wmin = g.width[0], dmax = g.dim[0];
     for (int d = 1; d < 3; d++) {
@@ -539,32 +627,32 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
       if (bad & kOutside)
         throw std::runtime_error("particle more than one box length outside the periodic box");
       if (bad & kOutsideOpen) throw std::runtime_error("particle outside the non-periodic box");
-      hc.assign(ntop, HCell{});
+      g_phase_ms[1] += ms_since(tmark);
+      T.clear();
       long long total = 0;
       for (int t = 0; t < ntop; t++) {
-        hc[t] = HCell{top[t].x, top[t].y, 0, -1, t, {-1, -1, -1, -1, -1, -1, -1, -1}};
+        T.add(top[t].x, top[t].y, 0, -1, t);
         total += top[t].y;
       }
       if (total != n) throw std::runtime_error("cell assignment lost particles");
       std::vector<int> frontier;
       for (int t = 0; t < ntop; t++)
-        if (hc[t].count > Space::kSplitSize) frontier.push_back(t);
+        if (T.count[t] > Space::kSplitSize) frontier.push_back(t);
       std::vector<int4> fh;
-      std::vector<int> ch;
       bool deeper = false;
       while (!frontier.empty() && !deeper) {
         fh.resize(frontier.size());
         for (size_t f = 0; f < frontier.size(); f++) {
-          const HCell& c = hc[frontier[f]];
-          if (c.depth >= SPH_MAX_DEPTH - 1)
+          const int c = frontier[f];
+          if (T.depth[c] >= SPH_MAX_DEPTH - 1)
             throw std::runtime_error(
                 "cell tree deeper than supported (particles at identical positions?)");
-          if (c.depth >= g.levels) {
+          if (T.depth[c] >= g.levels) {
             if (g.levels == levels_full)
               throw std::runtime_error("cell tree deeper than the device keys resolve");
             deeper = true;
           }
-          fh[f] = make_int4(c.first, c.count, c.depth, 0);
+          fh[f] = make_int4(T.first[c], T.count[c], T.depth[c], 0);
         }
         if (deeper) break;
         const int nf = (int)fh.size();
@@ -573,62 +661,67 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
         ca_children<<<(nf + kThreads - 1) / kThreads, kThreads, 0, st>>>(key, fbuf.p, nf,
                                                                           g.levels, cbuf.p);
         CK(cudaGetLastError());
-        ch.resize((size_t)8 * nf);
-        CK(cudaMemcpyAsync(ch.data(), cbuf.p, sizeof(int) * 8 * nf, cudaMemcpyDeviceToHost,
-                           st));
+        int* ch = S.ch.get((size_t)8 * nf);
+        CK(cudaMemcpyAsync(ch, cbuf.p, sizeof(int) * 8 * nf, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         std::vector<int> next;
         for (int f = 0; f < nf; f++) {
           const int pc = frontier[f];
-          int off = hc[pc].first;
+          int off = T.first[pc];
+          const int dep = T.depth[pc] + 1, tp = T.top[pc];
+          T.kid0[pc] = T.size();
           for (int k = 0; k < 8; k++) {
             const int cnt = ch[8 * f + k];
             if (cnt == 0) continue;
-            HCell c{off, cnt, hc[pc].depth + 1, pc, hc[pc].top,
-                    {-1, -1, -1, -1, -1, -1, -1, -1}};
+            const int c = T.add(off, cnt, dep, pc, tp);
+            T.nkid[pc]++;
             off += cnt;
-            hc[pc].child[k] = (int)hc.size();
-            if (cnt > Space::kSplitSize) next.push_back((int)hc.size());
-            hc.push_back(c);
+            if (cnt > Space::kSplitSize) next.push_back(c);
           }
-          if (off != hc[pc].first + hc[pc].count)
+          if (off != T.first[pc] + T.count[pc])
             throw std::runtime_error("cell assignment lost particles in a split");
         }
         frontier.swap(next);
       }
+      g_phase_ms[2] += ms_since(tmark);
       if (!deeper) break;
     }
 
     // 5. the host build's numbering: top cells in cell_getid order, then
-    // every top cell's subtree depth first, octants in order
-    const int nc = (int)hc.size();
+    // every top cell's subtree in preorder (a cell before its children, a
+    // child's whole subtree before the next child), from subtree sizes;
+    // creation order has parents before children
+    const int nc = T.size();
     *ncells = nc;
-    std::vector<int> id(nc, -1);
-    for (int t = 0; t < ntop; t++) id[t] = t;
-    int next_id = ntop;
-    std::vector<int> stack;
-    for (int t = 0; t < ntop; t++) {
-      // preorder: a child is numbered before its own children and after the
-      // whole subtree of the previous sibling
-      stack.assign(1, t);
-      while (!stack.empty()) {
-        const int c = stack.back();
-        stack.pop_back();
-        if (id[c] < 0) id[c] = next_id++;
-        for (int k = 7; k >= 0; k--)
-          if (hc[c].child[k] >= 0) stack.push_back(hc[c].child[k]);
+    std::vector<int> size(nc, 1), id(nc, -1);
+    for (int c = nc - 1; c >= ntop; c--) size[T.parent[c]] += size[c];
+    int base = ntop;
+    for (int c = 0; c < nc; c++) {
+      int pos;
+      if (c < ntop) {
+        id[c] = c;
+        pos = base;
+        base += size[c] - 1;
+      } else {
+        pos = id[c] + 1;
+      }
+      for (int k = 0; k < T.nkid[c]; k++) {
+        const int kid = T.kid0[c] + k;
+        id[kid] = pos;
+        pos += size[kid];
       }
     }
     if (cells && max_cells >= nc) {
       for (int c = 0; c < nc; c++) {
         int32_t* r = cells + 5 * (size_t)id[c];
-        r[0] = hc[c].first;
-        r[1] = hc[c].count;
-        r[2] = hc[c].depth;
-        r[3] = hc[c].parent >= 0 ? id[hc[c].parent] : -1;
-        r[4] = hc[c].top;
+        r[0] = T.first[c];
+        r[1] = T.count[c];
+        r[2] = T.depth[c];
+        r[3] = T.parent[c] >= 0 ? id[T.parent[c]] : -1;
+        r[4] = T.top[c];
       }
     }
+    g_phase_ms[3] += ms_since(tmark);
 
     // 6. depth_h
     float hmin_d[SPH_MAX_DEPTH], hmax_d[SPH_MAX_DEPTH];
@@ -644,23 +737,33 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
         dmin = c.dmin / 2;
       }
     }
-    std::vector<int4> leaves;
+    int nl = 0;
     for (int c = 0; c < nc; c++)
-      if (hc[c].count > 0 && hc[c].count <= Space::kSplitSize)
-        leaves.push_back(make_int4(hc[c].first, hc[c].count, hc[c].depth, 0));
-    DBuf<int4>& lbuf = S.lbuf;
-    lbuf.upload(leaves.data(), leaves.size(), st);
+      if (T.count[c] > 0 && T.nkid[c] == 0) nl++;
+    int2* leaves = S.leaves.get(nl);
+    nl = 0;
+    for (int c = 0; c < nc; c++)
+      if (T.count[c] > 0 && T.nkid[c] == 0)
+        leaves[nl++] = make_int2(T.first[c], T.count[c] | T.depth[c] << 16);
+    DBuf<int2>& lbuf = S.lbuf;
+    lbuf.upload(leaves, nl, st);
     DBuf<float>& tab = S.tab;
     std::vector<float> tabh(hmin_d, hmin_d + SPH_MAX_DEPTH);
     tabh.insert(tabh.end(), hmax_d, hmax_d + SPH_MAX_DEPTH);
     tab.upload(tabh.data(), tabh.size(), st);
-    const int nl = (int)leaves.size();
     ca_depth_h<<<(nl * 32 + kThreads - 1) / kThreads, kThreads, 0, st>>>(
         lbuf.p, nl, order, h, tab.p, tab.p + SPH_MAX_DEPTH, depth_h);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
+    g_phase_ms[4] += ms_since(tmark);
     if (cells && max_cells < nc)
       return fail(SPHGPU_EINVAL, "sphgpu_cell_assign: cells buffer too small (see *ncells)");
     return SPHGPU_OK;
   });
+}
+
+int sphgpu_cell_assign_times(double ms[5]) {
+  if (!ms) return fail(SPHGPU_EINVAL, "sphgpu_cell_assign_times: null argument");
+  for (int k = 0; k < 5; k++) ms[k] = g_phase_ms[k];
+  return SPHGPU_OK;
 }

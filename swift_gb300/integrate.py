@@ -29,7 +29,7 @@ import ctypes
 import numpy as np
 import torch
 
-from . import api
+from . import api, snapshot
 
 NUM_TIME_BINS = 56
 MAX_NR_TIMESTEPS = 1 << (NUM_TIME_BINS + 1)
@@ -51,6 +51,8 @@ class Integrator:
 
     def __init__(self, box, *, time_end=1.0, cfl=0.1, dt_min=1e-12, dt_max=1e-2,
                  log_max_h_change=None, minimal_u=0.0, device="cuda", **space_params):
+        self._settings = dict(time_end=float(time_end), cfl=float(cfl), dt_min=float(dt_min),
+                              dt_max=float(dt_max), minimal_u=float(minimal_u))
         if not torch.cuda.is_available():
             raise RuntimeError("Integrator needs a CUDA device")
         self.dev = torch.device(device)
@@ -118,6 +120,50 @@ class Integrator:
     @property
     def time(self):
         return self.ti_current * self.ip.time_base
+
+    # -- snapshots and restarts ---------------------------------------------
+    def save(self, path):
+        """Write a snapshot (swift_gb300.snapshot: the PartType0 output
+        fields) with the state a restart needs."""
+        st = self.state()
+        fields = {k: st[k] for k in ("x", "v", "h", "u", "rho", "P")}
+        fields["m"] = self.m
+        restart = {k: st[k] for k in snapshot.RESTART_FIELDS}
+        restart.update(ti_current=np.int64(self.ti_current),
+                       ti_end_min=np.int64(self.ti_end_min), steps=np.int64(self.steps),
+                       log_max_h_change=np.float32(self.ip.log_max_h_change),
+                       settings=np.array([self._settings[k] for k in
+                                          ("time_end", "cfl", "dt_min", "dt_max", "minimal_u")]))
+        if "eta" in self.box_meta:
+            restart["eta"] = np.float64(self.box_meta["eta"])
+        snapshot.write(path, fields, self.dim, self.time, restart)
+
+    @classmethod
+    def restart(cls, path, device="cuda", **space_params):
+        """An integrator that continues from a snapshot written by
+        :meth:`save`, bit for bit where the original would have gone on."""
+        box = snapshot.read(path)
+        r = box.pop("restart")
+        if "ti_current" not in r:
+            raise ValueError(f"{path} is a plain snapshot without restart data")
+        if "eta" in r:
+            box["eta"] = float(r["eta"])
+        time_end, cfl, dt_min, dt_max, minimal_u = (float(v) for v in r["settings"])
+        it = cls(box, time_end=time_end, cfl=cfl, dt_min=dt_min, dt_max=dt_max,
+                 log_max_h_change=float(r["log_max_h_change"]), minimal_u=minimal_u,
+                 device=device, **space_params)
+        for k in ("rho", "P"):
+            it.t[k].copy_(torch.as_tensor(np.ascontiguousarray(box[k]), device=it.dev))
+        for k in snapshot.RESTART_FIELDS:
+            if k in ("f", "balsara"):
+                continue
+            it.t[k].copy_(torch.as_tensor(np.ascontiguousarray(r[k]), device=it.dev))
+        it.f = np.array(r["f"], np.float32)
+        it.balsara = np.array(r["balsara"], np.float32)
+        it.ti_current = int(r["ti_current"])
+        it.ti_end_min = int(r["ti_end_min"])
+        it.steps = int(r["steps"])
+        return it
 
     # -- the operations ----------------------------------------------------
     def _kick(self, which, mab):

@@ -385,8 +385,9 @@ int sphgpu_cell_assign(const sphgpu_params *prm, const double *x, const float *h
                        int32_t *ncells, int32_t *cells, int32_t max_cells, void *stream);
 /* Host-clock phases (ms) of the calling thread's last sphgpu_cell_assign:
  * [0] h scan and grid, [1] keys and radix sort, [2] tree levels, [3] cell
- * numbering and records, [4] depth_h. */
-int sphgpu_cell_assign_times(double ms[5]);
+ * numbering and records, [4] depth_h; [5] the number of kernels it
+ * launched. */
+int sphgpu_cell_assign_times(double ms[6]);
 
 #ifdef __cplusplus
 }

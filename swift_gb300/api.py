@@ -225,10 +225,11 @@ def cell_assign(x, h, dim, **params):
 
 def cell_assign_times():
     """Host-clock phases (ms) of this thread's last :func:`cell_assign`: h scan
-    and grid, keys and sort, tree levels, numbering and records, depth_h."""
-    ms = np.zeros(5, np.float64)
+    and grid, keys and sort, tree levels, numbering and records, depth_h; and
+    the number of kernels it launched."""
+    ms = np.zeros(6, np.float64)
     _check(lib().sphgpu_cell_assign_times(_ptr(ms)))
-    return dict(zip(("grid", "keys_sort", "tree_levels", "numbering", "depth_h"),
+    return dict(zip(("grid", "keys_sort", "tree_levels", "numbering", "depth_h", "launches"),
                     (float(v) for v in ms)))
 
 

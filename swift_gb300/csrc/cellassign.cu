@@ -54,6 +54,8 @@ constexpr int kTile = 8 * kWarpItems;      // items per block
 constexpr int kScanItems = 8;              // items per thread in the scan
 constexpr int kScanTile = kThreads * kScanItems;
 
+thread_local int g_launches;  // kernels launched by the calling thread's last call
+
 enum CheckFlags : int {
   kNonFinite = 1,     // a non-finite position
   kOutside = 2,       // more than one box length outside the periodic box
@@ -390,6 +392,7 @@ void exclusive_scan(unsigned* a, long long n, cudaStream_t st, std::deque<DBuf<u
   if (tiles <= 1) {
     scan_tiles<<<1, kThreads, 0, st>>>(a, n, nullptr);
     CK(cudaGetLastError());
+    ++g_launches;
     return;
   }
   tmp.emplace_back();
@@ -398,9 +401,11 @@ void exclusive_scan(unsigned* a, long long n, cudaStream_t st, std::deque<DBuf<u
   unsigned* sp = sums.p;
   scan_tiles<<<(unsigned)tiles, kThreads, 0, st>>>(a, n, sp);
   CK(cudaGetLastError());
+  ++g_launches;
   exclusive_scan(sp, tiles, st, tmp);
   add_tile_offsets<<<(unsigned)tiles, kThreads, 0, st>>>(a, n, sp);
   CK(cudaGetLastError());
+  ++g_launches;
 }
 
 // The tree on the host, one entry per cell in creation order (top cells,
@@ -510,6 +515,7 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
 
     auto tmark = Clock::now();
     for (double& v : g_phase_ms) v = 0.0;
+    g_launches = 0;
     int dev = 0;
     CK(cudaGetDevice(&dev));
     Scratch& S = g_scratch;
@@ -521,6 +527,7 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
     ca_check_h<<<blocks_for(N, kThreads), kThreads, 0, st>>>(h, N, S.scal.p,
                                                               (int*)(S.scal.p + 1));
     CK(cudaGetLastError());
+    ++g_launches;
     unsigned hs[2];
     CK(cudaMemcpyAsync(hs, S.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -596,6 +603,7 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
       CK(cudaMemsetAsync(S.flags.p, 0, sizeof(int), st));
       ca_keys<<<blocks_for(N, kThreads), kThreads, 0, st>>>(x, N, g, k0.p, v0, S.flags.p);
       CK(cudaGetLastError());
+      ++g_launches;
       const int npass = (key_bits + 7) / 8;
       unsigned long long *ka = k0.p, *kb = k1.p;
       int *va = v0, *vb = v1.p;
@@ -604,9 +612,11 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
         const int shift = 8 * p;
         rs_hist<<<nblk, kThreads, 0, st>>>(ka, N, shift, hist.p);
         CK(cudaGetLastError());
+        ++g_launches;
         exclusive_scan(hist.p, (long long)256 * nblk, st, scan_tmp);
         rs_scatter<<<nblk, kThreads, 0, st>>>(ka, va, kb, vb, N, shift, hist.p);
         CK(cudaGetLastError());
+        ++g_launches;
         std::swap(ka, kb);
         std::swap(va, vb);
       }
@@ -618,6 +628,7 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
       ca_top_ranges<<<(ntop + kThreads - 1) / kThreads, kThreads, 0, st>>>(key, N, ntop,
                                                                             g.path_bits, rng.p);
       CK(cudaGetLastError());
+      ++g_launches;
       std::vector<int2> top(ntop);
       CK(cudaMemcpyAsync(top.data(), rng.p, sizeof(int2) * ntop, cudaMemcpyDeviceToHost, st));
       int bad = 0;
@@ -661,6 +672,7 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
         ca_children<<<(nf + kThreads - 1) / kThreads, kThreads, 0, st>>>(key, fbuf.p, nf,
                                                                           g.levels, cbuf.p);
         CK(cudaGetLastError());
+        ++g_launches;
         int* ch = S.ch.get((size_t)8 * nf);
         CK(cudaMemcpyAsync(ch, cbuf.p, sizeof(int) * 8 * nf, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -754,6 +766,7 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
     ca_depth_h<<<(nl * 32 + kThreads - 1) / kThreads, kThreads, 0, st>>>(
         lbuf.p, nl, order, h, tab.p, tab.p + SPH_MAX_DEPTH, depth_h);
     CK(cudaGetLastError());
+    ++g_launches;
     CK(cudaStreamSynchronize(st));
     g_phase_ms[4] += ms_since(tmark);
     if (cells && max_cells < nc)
@@ -762,8 +775,9 @@ int sphgpu_cell_assign(const sphgpu_params* prm, const double* x, const float* h
   });
 }
 
-int sphgpu_cell_assign_times(double ms[5]) {
+int sphgpu_cell_assign_times(double ms[6]) {
   if (!ms) return fail(SPHGPU_EINVAL, "sphgpu_cell_assign_times: null argument");
   for (int k = 0; k < 5; k++) ms[k] = g_phase_ms[k];
+  ms[5] = g_launches;
   return SPHGPU_OK;
 }

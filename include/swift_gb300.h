@@ -389,6 +389,18 @@ int sphgpu_cell_assign(const sphgpu_params *prm, const double *x, const float *h
  * launched. */
 int sphgpu_cell_assign_times(double ms[6]);
 
+/* sphgpu_space_create with the cell assignment already made by
+ * sphgpu_cell_assign (its order, copied to the host, and its cell records):
+ * the space adopts that tree instead of building one with the host's bucket
+ * and octant permutations (space_rebuild without its cell assignment).  The
+ * tree is checked for consistency (a permutation, children inside their
+ * parents, every cell of more than 400 particles split). */
+int sphgpu_space_create_assigned(const sphgpu_params *prm, int64_t n, const double *x,
+                                 const float *v, const float *m, const float *h,
+                                 const float *u, const int8_t *time_bin,
+                                 const int32_t *order, const int32_t *cells, int32_t ncells,
+                                 sphgpu_space **out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,6 +122,9 @@ SIGNATURES = {
     "sphgpu_cell_assign": (ctypes.c_int, [ctypes.POINTER(Params), _P, _P, ctypes.c_int64, _P,
                                           _P, _P, _P, _P, _I32, _P]),
     "sphgpu_cell_assign_times": (ctypes.c_int, [_P]),
+    "sphgpu_space_create_assigned": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64,
+                                                    _P, _P, _P, _P, _P, _P, _P, _P, _I32,
+                                                    ctypes.POINTER(_P)]),
     "sphgpu_server_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64, _I32,
                                             ctypes.POINTER(_P)]),
     "sphgpu_server_destroy": (ctypes.c_int, [_P]),
@@ -242,7 +245,10 @@ class Space:
     """A box of SPH particles with its cell tree, resident on the GPU once a
     GPU call is made.  Mirrors the reference's space + runner entry points."""
 
-    def __init__(self, box, **params):
+    def __init__(self, box, assigned=None, **params):
+        """``assigned``: optionally ``(order, cells)`` from :func:`cell_assign`
+        (order as a host or CUDA int32 array), adopted instead of the host's
+        own cell assignment."""
         L = lib()
         self.n = int(box["x"].shape[0])
         self._keep = {
@@ -256,10 +262,21 @@ class Space:
         k = self._keep
         self.params = make_params(box, **params)
         h = ctypes.c_void_p()
-        _check(L.sphgpu_space_create(ctypes.byref(self.params), self.n,
-                                     _ptr(k["x"]), _ptr(k["v"]), _ptr(k["m"]),
-                                     _ptr(k["h"]), _ptr(k["u"]), _ptr(k["tb"]),
-                                     ctypes.byref(h)))
+        if assigned is None:
+            _check(L.sphgpu_space_create(ctypes.byref(self.params), self.n,
+                                         _ptr(k["x"]), _ptr(k["v"]), _ptr(k["m"]),
+                                         _ptr(k["h"]), _ptr(k["u"]), _ptr(k["tb"]),
+                                         ctypes.byref(h)))
+        else:
+            order, cells = assigned
+            if hasattr(order, "cpu"):
+                order = order.cpu().numpy()
+            order = np.ascontiguousarray(order, np.int32)
+            cells = np.ascontiguousarray(cells, np.int32)
+            _check(L.sphgpu_space_create_assigned(
+                ctypes.byref(self.params), self.n, _ptr(k["x"]), _ptr(k["v"]), _ptr(k["m"]),
+                _ptr(k["h"]), _ptr(k["u"]), _ptr(k["tb"]), _ptr(order), _ptr(cells),
+                int(cells.shape[0]), ctypes.byref(h)))
         self._h = h
 
     # -- lifecycle ---------------------------------------------------------

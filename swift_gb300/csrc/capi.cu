@@ -674,10 +674,32 @@ void sphgpu_default_params(sphgpu_params* p) {
   p->max_top_level_cells = d.max_top_level_cells;
 }
 
+static int space_create(const sphgpu_params* prm, int64_t n, const double* x,
+                        const float* v, const float* m, const float* h,
+                        const float* u, const int8_t* time_bin, const int32_t* order,
+                        const int32_t* tree, int32_t ncells, sphgpu_space** out);
+
 int sphgpu_space_create(const sphgpu_params* prm, int64_t n, const double* x,
                         const float* v, const float* m, const float* h,
                         const float* u, const int8_t* time_bin,
                         sphgpu_space** out) {
+  return space_create(prm, n, x, v, m, h, u, time_bin, nullptr, nullptr, 0, out);
+}
+
+int sphgpu_space_create_assigned(const sphgpu_params* prm, int64_t n, const double* x,
+                                 const float* v, const float* m, const float* h,
+                                 const float* u, const int8_t* time_bin,
+                                 const int32_t* order, const int32_t* cells, int32_t ncells,
+                                 sphgpu_space** out) {
+  if (!order || !cells || ncells <= 0)
+    return fail(SPHGPU_EINVAL, "sphgpu_space_create_assigned: no order or tree");
+  return space_create(prm, n, x, v, m, h, u, time_bin, order, cells, ncells, out);
+}
+
+static int space_create(const sphgpu_params* prm, int64_t n, const double* x,
+                        const float* v, const float* m, const float* h,
+                        const float* u, const int8_t* time_bin, const int32_t* order,
+                        const int32_t* tree, int32_t ncells, sphgpu_space** out) {
   if (!prm || !x || !v || !m || !h || !u || !time_bin || !out || n <= 0)
     return fail(SPHGPU_EINVAL, "sphgpu_space_create: null argument or n <= 0");
   if (n > SPHGPU_MAX_PARTICLES)
@@ -707,7 +729,7 @@ int sphgpu_space_create(const sphgpu_params* prm, int64_t n, const double* x,
     s->u_in.assign(u, u + n);
     s->tb_in.assign(time_bin, time_bin + n);
     s->space = std::make_unique<Space>(P);
-    s->space->build(n, x, h, time_bin);
+    s->space->build(n, x, h, time_bin, order, tree, ncells);
     build_plans(s.get());
     *out = s.release();
     return SPHGPU_OK;

@@ -238,7 +238,8 @@ void Space::top_grid(const Params& prm, float max_h, int cdim[3], double width[3
 }
 
 void Space::build(int64_t n, const double* x, const float* h,
-                  const int8_t* time_bin) {
+                  const int8_t* time_bin, const int32_t* order, const int32_t* tree,
+                  int ncells) {
   if (n <= 0 || n > (int64_t)0x7fffffff - 16)
     throw std::runtime_error("particle count out of range");
   n_ = (int)n;
@@ -278,9 +279,23 @@ void Space::build(int64_t n, const double* x, const float* h,
     bin[k] = top_cell_index(pos, iw, cdim_);
   }
   perm_.resize(n_);
-  for (int k = 0; k < n_; k++) perm_[k] = k;
   std::vector<int> counts;
-  bucket_permute(bin, ntop, 0, n_, counts);
+  if (order) {
+    // the tree came from the device assignment: its order and top counts
+    if (ncells < ntop) throw std::runtime_error("assigned tree has fewer cells than the grid");
+    std::vector<uint8_t> seen(n_, 0);
+    for (int k = 0; k < n_; k++) {
+      const int i = order[k];
+      if (i < 0 || i >= n_ || seen[i]) throw std::runtime_error("assigned order is not a permutation");
+      seen[i] = 1;
+      perm_[k] = i;
+    }
+    counts.resize(ntop);
+    for (int c = 0; c < ntop; c++) counts[c] = tree[5 * (size_t)c + 1];
+  } else {
+    for (int k = 0; k < n_; k++) perm_[k] = k;
+    bucket_permute(bin, ntop, 0, n_, counts);
+  }
   cells_.clear();
   cells_.resize(ntop);
   for (int i = 0; i < cdim_[0]; i++)
@@ -315,11 +330,17 @@ void Space::build(int64_t n, const double* x, const float* h,
   // The split permutes perm_ inside each top cell; h_/active_ are refreshed
   // from perm_ before each leaf is finalised, so refresh them per top cell
   // after the split of that cell has reordered it.
-  for (int cid = 0; cid < ntop; cid++) {
-    if (cells_[cid].count == 0) continue;
-    // Octant permutations only reorder within [first, first+count); h and
-    // activity are gathered for the final order once the subtree is built.
-    split_tree_then_gather(cid);
+  if (order) {
+    adopt_tree(tree, ncells);
+    for (int cid = 0; cid < ntop; cid++)
+      if (cells_[cid].count > 0) finalize_h(cid);
+  } else {
+    for (int cid = 0; cid < ntop; cid++) {
+      if (cells_[cid].count == 0) continue;
+      // Octant permutations only reorder within [first, first+count); h and
+      // activity are gathered for the final order once the subtree is built.
+      split_tree_then_gather(cid);
+    }
   }
   // Inverse permutation.
   inv_perm_.resize(n_);
@@ -464,6 +485,51 @@ void Space::split_geometry(int c) {
   } else {
     cells_[c].split = 0;
   }
+}
+
+// The cells below the top level from tree records (first, count, depth,
+// parent, top) numbered as split_geometry numbers them (parents first, each
+// top cell's subtree in preorder): every child's octant is that of its
+// first particle about the parent's centre, and its geometry follows from
+// the parent's exactly as split_geometry derives it.
+void Space::adopt_tree(const int32_t* tree, int ncells) {
+  const int ntop = (int)cells_.size();
+  for (int c = ntop; c < ncells; c++) {
+    const int32_t* r = tree + 5 * (size_t)c;
+    const int pc = r[3];
+    if (pc < 0 || pc >= c) throw std::runtime_error("assigned tree: parent after child");
+    const Cell& par = cells_[pc];
+    if (r[1] <= 0 || r[0] < par.first || r[0] + r[1] > par.first + par.count ||
+        r[2] != par.depth + 1 || par.count <= kSplitSize)
+      throw std::runtime_error("assigned tree: child outside its parent");
+    const double* x = &x_[3 * (size_t)perm_[r[0]]];
+    const double pivot[3] = {par.loc[0] + par.width[0] / 2, par.loc[1] + par.width[1] / 2,
+                             par.loc[2] + par.width[2] / 2};
+    const int k = (x[0] >= pivot[0]) * 4 + (x[1] >= pivot[1]) * 2 + (x[2] >= pivot[2]);
+    Cell p;
+    for (int d = 0; d < 3; d++) {
+      p.loc[d] = par.loc[d];
+      p.width[d] = par.width[d] / 2;
+    }
+    p.dmin = par.dmin / 2;
+    p.h_min_allowed = p.dmin * 0.5 * (1. / SPH_KG);
+    p.h_max_allowed = p.dmin * (1. / SPH_KG);
+    if (k & 4) p.loc[0] += p.width[0];
+    if (k & 2) p.loc[1] += p.width[1];
+    if (k & 1) p.loc[2] += p.width[2];
+    p.depth = par.depth + 1;
+    p.parent = pc;
+    p.top = par.top;
+    p.count = r[1];
+    p.first = r[0];
+    if (cells_[pc].progeny[k] >= 0) throw std::runtime_error("assigned tree: octant taken twice");
+    cells_.push_back(p);
+    cells_[pc].progeny[k] = c;
+    cells_[pc].split = 1;
+  }
+  for (const Cell& c : cells_)
+    if (c.count > kSplitSize && !c.split)
+      throw std::runtime_error("assigned tree: a cell of more than 400 particles is not split");
 }
 
 void Space::finalize_h(int c) {

@@ -66,7 +66,11 @@ class Space {
   // Top-level grid for particles whose largest h is max_h: cells per side
   // and cell widths (throws where the reference would refuse the box).
   static void top_grid(const Params& prm, float max_h, int cdim[3], double width[3]);
-  void build(int64_t n, const double* x, const float* h, const int8_t* time_bin);
+  // order / tree / ncells (optional): the cell assignment made elsewhere
+  // (the device's sphgpu_cell_assign: particle order and tree records), used
+  // instead of the host's bucket and octant permutations.
+  void build(int64_t n, const double* x, const float* h, const int8_t* time_bin,
+             const int32_t* order = nullptr, const int32_t* tree = nullptr, int ncells = 0);
   // Start of a step at max_active_bin, with the reference's drift at zero
   // displacement (cell_drift.c:330-371): active particles restart from the
   // caller's h (the input h), every particle takes the depth_h of its h,
@@ -137,6 +141,7 @@ class Space {
   void split_tree_then_gather(int top);
   void split_geometry(int c);
   void finalize_h(int c);
+  void adopt_tree(const int32_t* tree, int ncells);
   void build_top_pairs();
   void redrift(int c);
   void redrift_leaf(int c);

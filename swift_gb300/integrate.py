@@ -9,7 +9,8 @@ Per step, as the reference's task graph runs it:
     drift every particle to ti_current (drift_part + hydro_predict_extra,
         cell_drift.c:253-332), then the periodic wrap of the rebuild
     rebuild: a new space (cell tree, sorts, gather lists) from the drifted
-        positions
+        positions; its cell assignment is made on the device
+        (sphgpu_cell_assign) and adopted by the host planner
     density -> ghost for the active particles (time_bin <= max_active_bin)
     force for the active particles; inactive ones lend their predicted state
     kick2, timestep, kick1 for the active particles
@@ -18,9 +19,9 @@ Per step, as the reference's task graph runs it:
 The particle state stays in device memory (torch tensors, the caller's
 order); the kicks, the drift and the time steps are CUDA kernels of the
 library (sphgpu_integ_*).  The density / ghost / force passes run through
-:class:`swift_gb300.api.Space`, whose tree is built on the host from the
-drifted positions (a host round trip per step: the device-resident rebuild
-is a separate piece of work).
+:class:`swift_gb300.api.Space`: the tree comes from the device's cell
+assignment of the drifted positions, the gather lists from the host planner
+(so the particle state still makes a host round trip per step).
 """
 from __future__ import annotations
 
@@ -50,7 +51,9 @@ class Integrator:
     max_iter, periodic ...) pass through to every rebuild."""
 
     def __init__(self, box, *, time_end=1.0, cfl=0.1, dt_min=1e-12, dt_max=1e-2,
-                 log_max_h_change=None, minimal_u=0.0, device="cuda", **space_params):
+                 log_max_h_change=None, minimal_u=0.0, device="cuda", device_rebuild=True,
+                 **space_params):
+        self.device_rebuild = bool(device_rebuild)
         self._settings = dict(time_end=float(time_end), cfl=float(cfl), dt_min=float(dt_min),
                               dt_max=float(dt_max), minimal_u=float(minimal_u))
         if not torch.cuda.is_available():
@@ -197,7 +200,14 @@ class Integrator:
                    time_bin=host["time_bin"], dim=self.dim, **self.box_meta)
         act = host["time_bin"] <= mab
         self.last_active = int(act.sum())
-        with api.Space(box, max_active_bin=mab, **self.space_params) as sp:
+        assigned = None
+        if self.device_rebuild:
+            # the rebuild's cell assignment on the device, from the drifted
+            # state in HBM; the space adopts it
+            order, _, cells, _ = api.cell_assign(self.t["x"], self.t["h"], self.dim,
+                                                 **self.space_params)
+            assigned = (order, cells)
+        with api.Space(box, assigned=assigned, max_active_bin=mab, **self.space_params) as sp:
             sp.step(api.STAGE_DENSITY | api.STAGE_GHOST)
             g = sp.download()
             h = np.where(act, g["h"], host["h"]).astype(np.float32)

@@ -135,3 +135,69 @@ def test_cell_assign_rejects_null_arguments():
     rc = L.sphgpu_cell_assign(ctypes.byref(p), None, None, 10, None, None, cdim,
                               ctypes.byref(n), None, 0, None)
     assert rc == api.EINVAL
+
+
+def host_assignment(box, run):
+    with api.Space(box, **run) as sp:
+        cells = sp.cells()
+        tree = sp.tree()
+        info = sp.info()
+    order = np.argsort(cells["position"]).astype(np.int32)
+    return order, tree, cells, info
+
+
+@pytest.mark.parametrize("cfg,run", CASES)
+def test_space_adopts_an_assigned_tree(cfg, run):
+    """sphgpu_space_create_assigned with the host build's own order and tree,
+    and with the particles of every leaf reordered (as the device's
+    assignment orders them): the same tree, leaves and plans."""
+    box = ics.make(cfg, seed=7)
+    order, tree, cells, info = host_assignment(box, run)
+    rng = np.random.default_rng(1)
+    shuffled = order.copy()
+    parent = tree[:, 3]
+    split = np.zeros(len(tree), bool)
+    split[parent[parent >= 0]] = True
+    for first, count in tree[~split & (tree[:, 1] > 0), :2]:
+        shuffled[first:first + count] = rng.permutation(shuffled[first:first + count])
+    for o in (order, shuffled):
+        with api.Space(box, assigned=(o, tree), **run) as sp:
+            assert np.array_equal(sp.tree(), tree)
+            got = sp.cells()
+            inf = sp.info()
+        for k in ("leaf_first", "leaf_count", "leaf_depth", "depth_h", "top"):
+            assert np.array_equal(got[k], cells[k]), k
+        for k in ("cells", "leaves", "tasks", "entries"):
+            assert inf[k] == info[k], k
+
+
+def test_space_rejects_an_inconsistent_tree():
+    box = ics.clustered(24, seed=7)
+    run = {"max_top_level_cells": 3}
+    order, tree, _, _ = host_assignment(box, run)
+    bad = order.copy()
+    bad[0] = bad[1]
+    with pytest.raises(api.SphGpuError):
+        api.Space(box, assigned=(bad, tree), **run)
+    t2 = tree.copy()
+    t2[-1, 0] = -5  # a child outside its parent
+    with pytest.raises(api.SphGpuError):
+        api.Space(box, assigned=(order, t2), **run)
+
+
+@pytest.mark.gpu
+def test_space_from_device_assignment_matches_host_space():
+    """The whole pass on a space built from the device's cell assignment:
+    the same neighbour counts as the host-built space, sums within rounding
+    (only the order inside leaves differs)."""
+    box = ics.clustered(32, seed=3)
+    order, dh, cells, cdim = api.cell_assign(box["x"], box["h"], box["dim"])
+    with api.Space(box) as sp:
+        sp.step(api.STAGE_DENSITY)
+        a = sp.download()
+    with api.Space(box, assigned=(order, cells)) as sp:
+        sp.step(api.STAGE_DENSITY)
+        b = sp.download()
+    assert np.array_equal(a["ngb_first"], b["ngb_first"])
+    for k in ("d_rho", "d_wcount"):
+        assert np.max(np.abs(a[k] - b[k]) / np.abs(a[k])) < 1e-5, k

@@ -497,6 +497,10 @@ def run_rebuild(args):
     with api.Space(box) as sp:
         t_host = time.perf_counter() - t0
         same = bool(np.array_equal(sp.tree(), cells))
+    # the same host build adopting the device's tree (order copied down)
+    t0 = time.perf_counter()
+    with api.Space(box, assigned=(oh.numpy(), cells)) as sp:
+        t_adopt = time.perf_counter() - t0
     dt, de = statistics.median(t_dev), statistics.median(t_e2e)
     out = {
         "metric": "particles assigned to cells per second (device-resident rebuild)",
@@ -512,6 +516,7 @@ def run_rebuild(args):
         "phases_ms": {k: statistics.median(p[k] for p in phases) for k in phases[0]
                       if k != "launches"},
         "host_space_create_s": t_host,
+        "host_space_create_assigned_s": t_adopt,
         "tree_equals_host_build": same,
         "gpu_launches": int(sum(p["launches"] for p in phases)),
         "clocks": clk,

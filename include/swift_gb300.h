@@ -379,7 +379,10 @@ int sphgpu_integ_max_active_bin(int64_t ti);
  *               format and numbering of sphgpu_space_tree: first, count,
  *               depth, parent, top.  With max_cells < *ncells the records
  *               are not written and SPHGPU_EINVAL is returned.
- * The call synchronises the stream (it reads back the grid and the tree). */
+ * The call synchronises the stream (it reads back the grid and the tree).
+ * Its device scratch (about 21 bytes per particle) and page-locked staging
+ * stay allocated for the calling host thread's next call, until the thread
+ * ends. */
 int sphgpu_cell_assign(const sphgpu_params *prm, const double *x, const float *h,
                        int64_t n, int32_t *order, int8_t *depth_h, int32_t cdim[3],
                        int32_t *ncells, int32_t *cells, int32_t max_cells, void *stream);

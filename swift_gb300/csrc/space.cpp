@@ -280,6 +280,7 @@ void Space::build(int64_t n, const double* x, const float* h,
   }
   perm_.resize(n_);
   std::vector<int> counts;
+  adopted_ = order != nullptr;
   if (order) {
     // the tree came from the device assignment: its order and top counts
     if (ncells < ntop) throw std::runtime_error("assigned tree has fewer cells than the grid");
@@ -375,6 +376,14 @@ void Space::build_gpu_order() {
   std::vector<int> leaf_block_begin(leaves_.size() + 1, 0);
   for (size_t l = 0; l < leaves_.size(); l++) {
     const Cell& c = cells_[leaves_[l]];
+    if (adopted_) {
+      // an adopted order already follows each particle's octant path inside
+      // its leaf (a Morton order at the split's own pivots): keep it
+      for (int k = c.first; k < c.first + c.count; k++) {
+        gperm_[k] = perm_[k];
+        g_of_s_[k] = k;
+      }
+    } else {
     key.clear();
     for (int k = c.first; k < c.first + c.count; k++) {
       const double* x = &x_[3 * (size_t)perm_[k]];
@@ -390,6 +399,7 @@ void Space::build_gpu_order() {
     for (size_t r = 0; r < key.size(); r++) {
       gperm_[c.first + (int)r] = perm_[key[r].second];
       g_of_s_[key[r].second] = c.first + (int)r;
+    }
     }
     leaf_block_begin[l] = (int)jb_.first.size();
     const Cell& top = cells_[c.top];

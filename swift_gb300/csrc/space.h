@@ -184,6 +184,7 @@ class Space {
   int cdim_[3] = {0, 0, 0};
   double width_[3] = {0, 0, 0};
   int jblock_ = SPH_JBLOCK;
+  bool adopted_ = false;  // the cell assignment (and leaf order) came from outside
   int threads_ = 0;
   std::vector<double> x_;
   std::vector<float> h_in_, h_;

@@ -14,7 +14,9 @@
 #   MODE=stock           : the reference's own optimisation flags (timed baseline)
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-${SWIFT_REFERENCE_ROOT:-/root/reference}}"
+# The reference tree: the argument, else $SWIFT_REFERENCE_ROOT, else a
+# `reference` directory beside this repository.
+REF="${1:-${SWIFT_REFERENCE_ROOT:-$HERE/../../reference}}"
 MODE="${MODE:-parity}"
 OUT="$HERE/_ref/$MODE"
 if [ ! -d "$REF/src" ]; then

@@ -38,6 +38,7 @@
 
 #include "../../include/swift_gb300.h"
 #include "capi_util.h"
+#include "device_sms.h"
 #include "space.h"
 #include "sph_types.h"
 
@@ -380,7 +381,8 @@ __global__ void ca_depth_h(const int2* __restrict__ leaf, int nleaf, const int* 
   }
 }
 
-int blocks_for(long long n, int per_block, int cap = 152 * 32) {
+int blocks_for(long long n, int per_block, int cap = 0) {
+  if (cap <= 0) cap = 32 * sm_count();
   const long long b = (n + per_block - 1) / per_block;
   return (int)std::max(1LL, std::min<long long>(b, cap));
 }

@@ -21,6 +21,7 @@
 
 #include <algorithm>
 
+#include "device_sms.h"
 #include "gather_impl.cuh"
 
 namespace sphgpu {
@@ -84,7 +85,7 @@ cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                int need, int veto, const int* leaf_pair_begin,
                                int4* units, const int* gate, cudaStream_t s, int win) {
   int g = (nleaves * 32 + 255) / 256;
-  g = std::max(1, std::min(g, 152 * 16));
+  g = std::max(1, std::min(g, sm_count() * 16));
   build_units<<<g, 256, 0, s>>>(leaves, nleaves, leaf_window_begin, flags, need, veto,
                                 leaf_pair_begin, units, gate, win);
   return cudaGetLastError();
@@ -94,7 +95,8 @@ cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
 cudaError_t launch_solve_from_lists(const ListArgs& a, const GhostArgs& g, int max_iter,
                                     cudaStream_t s) {
   long long grid = ((long long)a.p.n * 4 + 255) / 256;  // four lanes per particle
-  grid = grid < 1 ? 1 : (grid > 152LL * 16 ? 152LL * 16 : grid);
+  const long long cap = 16LL * sm_count();
+  grid = grid < 1 ? 1 : (grid > cap ? cap : grid);
   solve_from_lists<<<(int)grid, 256, 0, s>>>(a, g, max_iter);
   return cudaGetLastError();
 }
@@ -102,7 +104,7 @@ cudaError_t launch_solve_from_lists(const ListArgs& a, const GhostArgs& g, int m
 cudaError_t launch_block_hmax(const int2* fc, float4* lo, const float4* posh,
                               int nblocks, cudaStream_t s) {
   int g = (nblocks + 255) / 256;
-  g = std::max(1, std::min(g, 152 * 8));
+  g = std::max(1, std::min(g, sm_count() * 8));
   block_hmax<<<g, 256, 0, s>>>(fc, lo, posh, nblocks);
   return cudaGetLastError();
 }

@@ -27,6 +27,7 @@
 
 #include "../../include/swift_gb300.h"
 #include "capi_util.h"
+#include "device_sms.h"
 #include "sph_types.h"
 
 namespace sphgpu {
@@ -213,7 +214,7 @@ __global__ void timestep_k(sphgpu_integ_params ip, sphgpu_integ_state st, long l
   }
 }
 
-int grid_for(long long n) { return (int)std::max(1LL, std::min((n + 255) / 256, 152LL * 8)); }
+int grid_for(long long n) { return (int)std::max(1LL, std::min((n + 255) / 256, 8LL * sm_count())); }
 
 int check_args(const sphgpu_integ_params* ip, const sphgpu_integ_state* st, long long n) {
   if (!ip || !st || n < 0) return fail(SPHGPU_EINVAL, "integrator: null argument or n < 0");

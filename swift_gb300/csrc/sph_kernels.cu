@@ -7,6 +7,7 @@
 
 #include <algorithm>
 
+#include "device_sms.h"
 #include "ghost_impl.cuh"
 #include "sph_kernels.cuh"
 
@@ -124,6 +125,19 @@ __global__ void permute_in(DevParticles P, const int32_t* __restrict__ perm,
   }
 }
 
+// New velocities, masses and internal energies (input order) into the
+// store; positions and h stay the space's.
+__global__ void permute_vmu_in(DevParticles P, const int32_t* __restrict__ perm,
+                               const float* __restrict__ v, const float* __restrict__ m,
+                               const float* __restrict__ u) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n;
+       i += gridDim.x * blockDim.x) {
+    const size_t k = (size_t)perm[i];
+    P.velm[i] = make_float4(v[3 * k], v[3 * k + 1], v[3 * k + 2], m[k]);
+    P.u[i] = u[k];
+  }
+}
+
 // Cell-sorted results -> input order, float [n][24] and int32 [n][4].
 __global__ void collect_out(DevParticles P, const int32_t* __restrict__ perm,
                             float* __restrict__ fields, int32_t* __restrict__ ints) {
@@ -160,7 +174,8 @@ __global__ void collect_out(DevParticles P, const int32_t* __restrict__ perm,
 
 static int grid_for(int n) {
   int g = (n + 255) / 256;
-  return g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g);
+  const int cap = 16 * sm_count();
+  return g < 1 ? 1 : (g > cap ? cap : g);
 }
 
 __global__ void ghost_catchup(GhostArgs g, int max_iter, const int* gate, int* sent) {
@@ -225,6 +240,12 @@ cudaError_t launch_permute_in(DevParticles p, const int32_t* perm,
                               cudaStream_t s) {
   permute_in<<<grid_for(p.n), 256, 0, s>>>(p, perm, x_in, x_ref, v_in, m_in, h_in, u_in,
                                            differ);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_permute_vmu_in(DevParticles p, const int32_t* perm, const float* v,
+                                  const float* m, const float* u, cudaStream_t s) {
+  permute_vmu_in<<<grid_for(p.n), 256, 0, s>>>(p, perm, v, m, u);
   return cudaGetLastError();
 }
 

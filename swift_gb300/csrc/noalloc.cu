@@ -1,11 +1,10 @@
 // noalloc.cu -- a density first pass that allocates no device memory.
 //
 // Some callers cannot allocate device memory at the moment they need a
-// density pass: code running inside CUDA stream capture (a cudaMalloc there
-// invalidates the capture), hosts that hand all device memory to their own
-// pool and account for every byte (as the reference's memuse layer does for
-// its host allocations), and latency-critical serving loops that must not
-// stall on the allocator.  For them this file offers the density gather in a
+// density pass: hosts that hand all device memory to their own pool and
+// account for every byte (as the reference's memuse layer does for its host
+// allocations), and latency-critical serving loops that must not stall on
+// the allocator.  For them this file offers the density gather in a
 // form whose only scratch -- the work-queue counter and the list of work
 // groups (32-particle windows of active particles) -- lives in a file-scope
 // static device array of fixed size,

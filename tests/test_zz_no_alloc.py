@@ -1,12 +1,12 @@
 """The allocation-free density pass (sphgpu_density_noalloc) against the
 library's regular density pass, through the C ABI.
 
-Callers that cannot allocate device memory when they run the pass -- code
-inside CUDA stream capture, hosts that hand all device memory to their own
-pool, latency-bound serving loops -- use this entry point; its scratch is a
-static device array of fixed size.  The test allocates the output buffers
-itself (the entry point must not), calls the entry point twice in a row (the
-second call must not see the first call's counters), and checks each result
+Callers that cannot allocate device memory when they run the pass -- hosts
+that hand all device memory to their own pool, latency-bound serving loops --
+use this entry point; its scratch is a static device array of fixed size.
+The test allocates the output buffers itself (the entry point must not),
+calls the entry point twice in a row (the second call must not see the first
+call's counters), and checks each result
 against the regular pass: neighbour counts exactly, positive sums at 1e-4
 relative, cancelling sums at 1e-4 of the field's scale (the tolerances of
 tests/test_gpu_parity.py).  This file is collected last on purpose.

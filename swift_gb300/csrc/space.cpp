@@ -291,8 +291,20 @@ void Space::build(int64_t n, const double* x, const float* h,
       seen[i] = 1;
       perm_[k] = i;
     }
+    // top-cell counts: non-negative, adding up to n, and every particle in
+    // the range of the top cell its position falls in
     counts.resize(ntop);
-    for (int c = 0; c < ntop; c++) counts[c] = tree[5 * (size_t)c + 1];
+    long long total = 0;
+    for (int c = 0; c < ntop; c++) {
+      counts[c] = tree[5 * (size_t)c + 1];
+      if (counts[c] < 0) throw std::runtime_error("assigned tree: negative top-cell count");
+      total += counts[c];
+    }
+    if (total != n_) throw std::runtime_error("assigned tree: top-cell counts do not add up to n");
+    for (int c = 0, k = 0; c < ntop; c++)
+      for (int e = k + counts[c]; k < e; k++)
+        if (bin[perm_[k]] != c)
+          throw std::runtime_error("assigned tree: a particle is not in its top cell's range");
   } else {
     for (int k = 0; k < n_; k++) perm_[k] = k;
     bucket_permute(bin, ntop, 0, n_, counts);
@@ -512,10 +524,16 @@ void Space::adopt_tree(const int32_t* tree, int ncells) {
     if (r[1] <= 0 || r[0] < par.first || r[0] + r[1] > par.first + par.count ||
         r[2] != par.depth + 1 || par.count <= kSplitSize)
       throw std::runtime_error("assigned tree: child outside its parent");
-    const double* x = &x_[3 * (size_t)perm_[r[0]]];
     const double pivot[3] = {par.loc[0] + par.width[0] / 2, par.loc[1] + par.width[1] / 2,
                              par.loc[2] + par.width[2] / 2};
-    const int k = (x[0] >= pivot[0]) * 4 + (x[1] >= pivot[1]) * 2 + (x[2] >= pivot[2]);
+    auto octant = [&](int q) {
+      const double* x = &x_[3 * (size_t)perm_[q]];
+      return (x[0] >= pivot[0]) * 4 + (x[1] >= pivot[1]) * 2 + (x[2] >= pivot[2]);
+    };
+    const int k = octant(r[0]);
+    // every particle of the child lies in the child's octant of the parent
+    for (int q = r[0] + 1; q < r[0] + r[1]; q++)
+      if (octant(q) != k) throw std::runtime_error("assigned tree: a particle outside its octant");
     Cell p;
     for (int d = 0; d < 3; d++) {
       p.loc[d] = par.loc[d];
@@ -537,9 +555,24 @@ void Space::adopt_tree(const int32_t* tree, int ncells) {
     cells_[pc].progeny[k] = c;
     cells_[pc].split = 1;
   }
-  for (const Cell& c : cells_)
+  for (const Cell& c : cells_) {
     if (c.count > kSplitSize && !c.split)
       throw std::runtime_error("assigned tree: a cell of more than 400 particles is not split");
+    if (!c.split) continue;
+    // the children tile the parent: in octant order their ranges follow one
+    // another from the parent's first particle to its last (the split's
+    // bucket order), with no gap and no overlap
+    int next = c.first;
+    for (int k = 0; k < 8; k++) {
+      const int p = c.progeny[k];
+      if (p < 0) continue;
+      if (cells_[p].first != next)
+        throw std::runtime_error("assigned tree: children do not tile their parent");
+      next += cells_[p].count;
+    }
+    if (next != c.first + c.count)
+      throw std::runtime_error("assigned tree: children do not tile their parent");
+  }
 }
 
 void Space::finalize_h(int c) {

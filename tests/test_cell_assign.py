@@ -185,6 +185,72 @@ def test_space_rejects_an_inconsistent_tree():
         api.Space(box, assigned=(order, t2), **run)
 
 
+def _leaves(tree):
+    parent = tree[:, 3]
+    split = np.zeros(len(tree), bool)
+    split[parent[parent >= 0]] = True
+    return np.nonzero(~split & (tree[:, 1] > 0))[0]
+
+
+def test_space_rejects_bad_top_counts():
+    """Top-cell counts that are negative, or that do not add up to the
+    particle count, are refused before any cell is filled."""
+    box = ics.clustered(24, seed=7)
+    run = {"max_top_level_cells": 3}
+    order, tree, _, _ = host_assignment(box, run)
+    ntop = int(np.sum(tree[:, 3] < 0))
+    for delta in (+1, -1):
+        t2 = tree.copy()
+        t2[0, 1] += delta                 # one top count too large / too small
+        with pytest.raises(api.SphGpuError, match="top-cell count"):
+            api.Space(box, assigned=(order, t2), **run)
+    t2 = tree.copy()
+    t2[0, 1] = -t2[0, 1]                  # negative
+    with pytest.raises(api.SphGpuError, match="top-cell count"):
+        api.Space(box, assigned=(order, t2), **run)
+    assert ntop == 27
+
+
+def test_space_rejects_a_particle_in_the_wrong_leaf():
+    """Swapping two particles of different leaves (same top cell, so the
+    order stays a permutation and the counts stay right) puts each outside
+    its octant: refused.  Swapping across top cells is refused too."""
+    box = ics.clustered(24, seed=7)
+    run = {"max_top_level_cells": 3}
+    order, tree, _, _ = host_assignment(box, run)
+    leaves = _leaves(tree)
+    # two leaves of the same top cell with different parents' octants
+    by_top = {}
+    for c in leaves:
+        by_top.setdefault(int(tree[c, 4]), []).append(int(c))
+    top, ls = next((t, v) for t, v in by_top.items() if len(v) >= 2)
+    a, b = ls[0], ls[-1]
+    bad = order.copy()
+    i, j = int(tree[a, 0]), int(tree[b, 0])
+    bad[i], bad[j] = bad[j], bad[i]
+    with pytest.raises(api.SphGpuError, match="octant|top cell"):
+        api.Space(box, assigned=(bad, tree), **run)
+    # across top cells
+    tops = np.nonzero((tree[:, 3] < 0) & (tree[:, 1] > 0))[0]
+    bad = order.copy()
+    i, j = int(tree[tops[0], 0]), int(tree[tops[1], 0])
+    bad[i], bad[j] = bad[j], bad[i]
+    with pytest.raises(api.SphGpuError, match="top cell"):
+        api.Space(box, assigned=(bad, tree), **run)
+
+
+def test_space_rejects_children_that_do_not_tile_their_parent():
+    """A child range shortened by one particle leaves a gap in its parent."""
+    box = ics.clustered(24, seed=7)
+    run = {"max_top_level_cells": 3}
+    order, tree, _, _ = host_assignment(box, run)
+    kids = np.nonzero((tree[:, 3] >= 0) & (tree[:, 1] > 1))[0]
+    t2 = tree.copy()
+    t2[kids[0], 1] -= 1
+    with pytest.raises(api.SphGpuError, match="tile"):
+        api.Space(box, assigned=(order, t2), **run)
+
+
 @pytest.mark.gpu
 def test_space_from_device_assignment_matches_host_space():
     """The whole pass on a space built from the device's cell assignment:

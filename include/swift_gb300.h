@@ -176,9 +176,10 @@ int sphgpu_phase_times(sphgpu_space *s, double ms_sum[3], int64_t *steps,
 int sphgpu_count_hits(sphgpu_space *s, int64_t hits[4]);
 
 /* The first density pass of a resident space with no device allocation:
- * for callers that cannot allocate when they run it -- inside CUDA stream
- * capture, under a host that owns all device memory through its own pool,
- * or in a latency-bound serving loop.  No counterpart in the reference.
+ * for callers that cannot call cudaMalloc when they run it -- a host that
+ * hands all device memory to its own pool and accounts for every byte, or a
+ * latency-bound serving loop that must not stall on the allocator.  No
+ * counterpart in the reference.
  * The space must already be resident on the device (any earlier GPU call on
  * it allocates and uploads); the first call on a device also looks up the
  * library's static scratch array, so make it before any stream capture.
@@ -190,10 +191,24 @@ int sphgpu_count_hits(sphgpu_space *s, int64_t hits[4]);
  * Outputs, in the caller's particle order, go to device buffers the caller
  * provides: d_fields float [n][8] = rho, rho_dh, wcount, wcount_dh, div_v,
  * rot_v[3] (the raw sums of sphgpu_download columns 0-7) and d_ngb int32 [n]
- * neighbour counts.  Asynchronous on `stream` (NULL: the space's stream). */
+ * neighbour counts.  Asynchronous on `stream` (NULL: the space's stream).
+ * The pass reads the space's device state: a caller that passes a stream
+ * other than the space's own must order it after the work it queued on the
+ * space's stream (for example sphgpu_step_host_async uploads), e.g. with an
+ * event recorded there and cudaStreamWaitEvent on `stream`. */
 #define SPHGPU_NOALLOC_MAX_PARTICLES (1 << 20)
 int sphgpu_density_noalloc(sphgpu_space *s, float *d_fields, int32_t *d_ngb,
                            void *stream);
+
+/* New velocities, masses and internal energies of every particle (input
+ * order: v float [n][3], m, u float [n]), e.g. after the kicks of a step, for
+ * the loops that follow.  Positions and h stay the space's (a drift that
+ * moves particles needs a new space).  Replaces the copy of these
+ * struct part fields that the reference's loops read in place
+ * (hydro/Minimal/hydro_part.h:103-240).  Synchronous; on a machine without
+ * a GPU the host copies are updated and SPHGPU_ENODEV is returned. */
+int sphgpu_space_update(sphgpu_space *s, const float *v, const float *m, const float *u,
+                        void *stream);
 
 /* Same pass through host buffers: copies x, v, m, h, u (input order) from
  * host memory, runs the step, copies the results back.  `fields` receives

@@ -89,6 +89,7 @@ SIGNATURES = {
     "sphgpu_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
     "sphgpu_step": (ctypes.c_int, [_P, _I32, _P]),
     "sphgpu_step_host": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "sphgpu_space_update": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "sphgpu_step_plain": (ctypes.c_int, [_P, _P]),
     "sphgpu_step_host_async": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "sphgpu_step_host_wait": (ctypes.c_int, [_P]),
@@ -381,6 +382,13 @@ class Space:
             self.step_plain()
         else:
             self.step(stages)
+
+    def update(self, v, m, u, stream=None):
+        """New velocities, masses and internal energies (input order), e.g.
+        after a kick; positions and h stay the space's."""
+        arrs = [np.ascontiguousarray(v, np.float32), np.ascontiguousarray(m, np.float32),
+                np.ascontiguousarray(u, np.float32)]
+        _check(lib().sphgpu_space_update(self._h, *[_ptr(a) for a in arrs], stream))
 
     def step_host(self, box=None, fields=None, stream=None):
         b = self._keep if box is None else {

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <exception>
@@ -1029,6 +1030,37 @@ int sphgpu_step_host(sphgpu_space* s, const double* x, const float* v,
       CK(cudaStreamSynchronize(st));
     }
     if (rc == SPHGPU_ENOCONV) return fail(rc, g_err);
+    return SPHGPU_OK;
+  });
+}
+
+int sphgpu_space_update(sphgpu_space* s, const float* v, const float* m, const float* u,
+                        void* stream) {
+  if (!s || !v || !m || !u) return fail(SPHGPU_EINVAL, "null argument");
+  const int n = s->space->n();
+  for (int k = 0; k < n; k++)
+    if (!(m[k] > 0.f) || !std::isfinite(m[k]) || !std::isfinite(u[k]) ||
+        !std::isfinite(v[3 * (size_t)k]) || !std::isfinite(v[3 * (size_t)k + 1]) ||
+        !std::isfinite(v[3 * (size_t)k + 2]))
+      return fail(SPHGPU_EINVAL, "sphgpu_space_update: non-finite v or u, or mass <= 0 "
+                                 "(particle " + std::to_string(k) + ")");
+  return guard([&]() {
+    // the host copies feed the next upload (first GPU call, re-plans)
+    s->v_in.assign(v, v + 3 * (size_t)n);
+    s->m_in.assign(m, m + n);
+    s->u_in.assign(u, u + n);
+    ensure_device(s);
+    cudaStream_t st = pick(s, stream);
+    if (!s->v_stage.p) {
+      s->v_stage.alloc(3 * (size_t)n);
+      s->m_stage.alloc(n);
+      s->u_stage.alloc(n);
+    }
+    CK(cudaMemcpyAsync(s->v_stage.p, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->m_stage.p, m, sizeof(float) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->u_stage.p, u, sizeof(float) * n, cudaMemcpyHostToDevice, st));
+    CK(launch_permute_vmu_in(s->P, s->perm.p, s->v_stage.p, s->m_stage.p, s->u_stage.p, st));
+    CK(cudaStreamSynchronize(st));
     return SPHGPU_OK;
   });
 }

@@ -170,6 +170,8 @@ cudaError_t launch_prepare_posh(DevParticles p, const int32_t* top_of,
                                 const double* top_loc, cudaStream_t s);
 // Host-order v, m, u -> store; sets *differ when x or h differ from the
 // space's own (x_ref: the space's input positions, input order).
+cudaError_t launch_permute_vmu_in(DevParticles p, const int32_t* perm, const float* v,
+                                  const float* m, const float* u, cudaStream_t s);
 cudaError_t launch_permute_in(DevParticles p, const int32_t* perm,
                               const double* x_in, const double* x_ref,
                               const float* v_in, const float* m_in,

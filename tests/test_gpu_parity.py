@@ -214,6 +214,33 @@ def test_step_host_matches_resident_step_and_checks_inputs():
             sp.step_host(grown, fields)
 
 
+def test_space_update_gives_the_step_of_the_new_state():
+    """sphgpu_space_update (new v, m, u after a kick) followed by a resident
+    step gives the results, bit for bit, of the host-buffer step on the same
+    new state; bad values are refused."""
+    box = ics.make("clustered:20", seed=4)
+    n = box["x"].shape[0]
+    rng = np.random.default_rng(2)
+    v2 = (box["v"] + rng.normal(0, 0.05, box["v"].shape)).astype(np.float32)
+    m2 = (box["m"] * (1 + 0.1 * rng.random(n))).astype(np.float32)
+    u2 = (box["u"] * (1 + 0.5 * rng.random(n))).astype(np.float32)
+    new = dict(box, v=v2, m=m2, u=u2)
+    with api.Space(box) as sp:
+        sp.step()
+        fields = np.zeros((n, 24), np.float32)
+        sp.step_host(new, fields)
+    with api.Space(box) as sp:
+        sp.step()
+        sp.update(v2, m2, u2)
+        sp.step()
+        out = sp.download()
+        bad = m2.copy()
+        bad[3] = 0.0
+        with pytest.raises(api.SphGpuError):
+            sp.update(v2, bad, u2)
+    assert np.array_equal(out["fields"].view(np.uint32), fields.view(np.uint32))
+
+
 def test_step_host_async_pipeline_matches_step_host():
     """The pipelined host-buffer step: three steps in flight two at a time
     give, bit for bit, the results of the synchronous call on the same

@@ -19,6 +19,19 @@ from .io import COLS, INT_COLS
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libsphoracle.so")
+# The timed CPU baseline: the same restatement built with the reference's own
+# optimisation flags (m4/ax_cc_maxopt.m4 for gcc: -O3 -ffast-math
+# -funroll-loops -fomit-frame-pointer and the host's own CPU tuning).  Its
+# sums are not bit-identical to the parity build's; it is never used to check.
+LIB_STOCK = os.path.join(BUILD, "libsphoracle_stock.so")
+
+
+def stock_flags():
+    import platform
+    native = "-march=native" if platform.machine() in ("x86_64", "AMD64") else "-mcpu=native"
+    return ["-O3", "-ffast-math", "-funroll-loops", "-fomit-frame-pointer", native]
+
+
 NFIELDS, NINTS = 24, 11
 STAGE_DENSITY, STAGE_GHOST, STAGE_FORCE = 1, 2, 4
 ALL = 7
@@ -31,7 +44,8 @@ class Params(ctypes.Structure):
                 ("alpha", ctypes.c_float), ("max_iter", ctypes.c_int32),
                 ("max_active_bin", ctypes.c_int32),
                 ("max_top_level_cells", ctypes.c_int32),
-                ("subsize_self", ctypes.c_int32), ("subsize_pair", ctypes.c_int32)]
+                ("subsize_self", ctypes.c_int32), ("subsize_pair", ctypes.c_int32),
+                ("reverse_tasks", ctypes.c_int32)]
 
 
 class Result(ctypes.Structure):
@@ -41,31 +55,34 @@ class Result(ctypes.Structure):
                 ("status", ctypes.c_int32), ("ntasks", ctypes.c_int32)]
 
 
-def build(force=False):
+def build(force=False, stock=False):
+    """Compile the restatement: the parity build (no fast-math, no FMA
+    contraction; the checker) or, with stock=True, the timed baseline."""
     srcs = [os.path.join(HERE, f) for f in ("sph_oracle.c", "sph_integrate.c")]
+    out = LIB_STOCK if stock else LIB
     newest = max(os.path.getmtime(f) for f in srcs + [os.path.join(HERE, "sph_oracle.h")])
-    if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest):
-        return LIB
+    if (not force and os.path.exists(out) and os.path.getmtime(out) >= newest):
+        return out
     os.makedirs(BUILD, exist_ok=True)
-    tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.run(["gcc", "-std=gnu11", "-O2", "-fno-fast-math",
-                    "-ffp-contract=off", "-fPIC", "-shared"] + srcs + ["-o", tmp,
-                    "-lm"], check=True)
-    os.replace(tmp, LIB)
-    return LIB
+    tmp = out + ".tmp%d" % os.getpid()
+    flags = stock_flags() if stock else ["-O2", "-fno-fast-math", "-ffp-contract=off"]
+    subprocess.run(["gcc", "-std=gnu11"] + flags + ["-fPIC", "-shared"] + srcs +
+                   ["-o", tmp, "-lm"], check=True)
+    os.replace(tmp, out)
+    return out
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        build()
-        _lib = ctypes.CDLL(LIB)
-        _lib.sph_oracle_run.restype = ctypes.c_int
-        _lib.sph_oracle_exact64.restype = None
-    return _lib
+def lib(stock=False):
+    if stock not in _libs:
+        path = build(stock=stock)
+        L = ctypes.CDLL(path)
+        L.sph_oracle_run.restype = ctypes.c_int
+        L.sph_oracle_exact64.restype = None
+        _libs[stock] = L
+    return _libs[stock]
 
 
 def make_params(box, **kw):
@@ -85,6 +102,8 @@ def make_params(box, **kw):
     # Scheduler:cell_sub_size_self_hydro / cell_sub_size_pair_hydro split
     p.subsize_self = kw.get("subsize_self", 0)
     p.subsize_pair = kw.get("subsize_pair", 0)
+    # 1: the same tasks in reverse order (a second legal task order)
+    p.reverse_tasks = kw.get("reverse_tasks", 0)
     return p
 
 
@@ -92,9 +111,11 @@ def _ptr(a, t):
     return a.ctypes.data_as(ctypes.POINTER(t))
 
 
-def run(box, stages=ALL, **kw):
-    """One density -> ghost -> force pass of the restated reference loops."""
-    L = lib()
+def run(box, stages=ALL, stock=False, **kw):
+    """One density -> ghost -> force pass of the restated reference loops
+    (stock=True: the build with the reference's optimisation flags, for
+    timing only)."""
+    L = lib(stock)
     n = box["x"].shape[0]
     x = np.ascontiguousarray(box["x"], np.float64)
     v = np.ascontiguousarray(box["v"], np.float32)
@@ -119,6 +140,39 @@ def run(box, stages=ALL, **kw):
         out[name] = fields[:, col]
     for name, col in INT_COLS.items():
         out[name] = ints[:, col]
+    return out
+
+
+def first_pass_tops(box, tops, **kw):
+    """The first density pass of the tasks that touch the given top cells:
+    the particles of those cells get their complete sums and neighbour
+    counts (the bits of run()'s first pass); ``out["in_tops"]`` marks them."""
+    L = lib()
+    n = box["x"].shape[0]
+    x = np.ascontiguousarray(box["x"], np.float64)
+    v = np.ascontiguousarray(box["v"], np.float32)
+    m = np.ascontiguousarray(box["m"], np.float32)
+    h = np.ascontiguousarray(box["h"], np.float32)
+    u = np.ascontiguousarray(box["u"], np.float32)
+    tb = np.ascontiguousarray(box["time_bin"], np.int8)
+    t = np.ascontiguousarray(tops, np.int32)
+    fields = np.zeros((n, NFIELDS), np.float32)
+    ints = np.zeros((n, NINTS), np.int32)
+    res = Result()
+    res.fields = _ptr(fields, ctypes.c_float)
+    res.ints = _ptr(ints, ctypes.c_int32)
+    prm = make_params(box, **kw)
+    L.sph_oracle_first_pass_tops(ctypes.byref(prm), ctypes.c_int(n), _ptr(x, ctypes.c_double),
+                                 _ptr(v, ctypes.c_float), _ptr(m, ctypes.c_float),
+                                 _ptr(h, ctypes.c_float), _ptr(u, ctypes.c_float),
+                                 _ptr(tb, ctypes.c_byte), ctypes.c_int(len(t)),
+                                 _ptr(t, ctypes.c_int32), ctypes.byref(res))
+    out = {"res": fields, "ints": ints, "cdim": tuple(res.cdim)}
+    for name, col in COLS.items():
+        out[name] = fields[:, col]
+    for name, col in INT_COLS.items():
+        out[name] = ints[:, col]
+    out["in_tops"] = np.isin(out["top"], t)
     return out
 
 

@@ -1613,10 +1613,12 @@ static void split_task(ospace *s, int ti) {
   }
 }
 
-static void build_space(ospace *s, const oracle_params *prm, int n,
-                        const double *x, const float *v, const float *m,
-                        const float *h, const float *u,
-                        const signed char *time_bin) {
+/* sort_all = 0 leaves every cell unsorted: the caller sorts the cells its
+ * tasks need. */
+static void build_space_sorted(ospace *s, const oracle_params *prm, int n,
+                               const double *x, const float *v, const float *m,
+                               const float *h, const float *u,
+                               const signed char *time_bin, int sort_all) {
   memset(s, 0, sizeof(*s));
   s->e.prm = prm;
   for (int k = 0; k < 3; k++) s->e.dim[k] = prm->dim[k];
@@ -1703,7 +1705,7 @@ static void build_space(ospace *s, const oracle_params *prm, int n,
   }
   free(counts);
   for (int cid = 0; cid < ntop; cid++)
-    if (s->top[cid].count > 0) do_sort(&s->top[cid]);
+    if (s->top[cid].count > 0 && sort_all) do_sort(&s->top[cid]);
   /* Tasks, in the order oracle/ref_harness.c creates them: per non-empty
    * top cell its self task, then its pair tasks with the non-empty
    * neighbours of higher index (26-neighbourhood, periodic). */
@@ -1743,6 +1745,12 @@ static void build_space(ospace *s, const oracle_params *prm, int n,
       if (s->tasks[t].ci != NULL) s->tasks[kept++] = s->tasks[t];
     s->ntasks = kept;
   }
+  if (prm->reverse_tasks)
+    for (int a = 0, z = s->ntasks - 1; a < z; a++, z--) {
+      const otask t = s->tasks[a];
+      s->tasks[a] = s->tasks[z];
+      s->tasks[z] = t;
+    }
   /* Density links on the cells each task holds (engine_maketasks.c:
    * 2311-2333), in task order. */
   s->links = ocalloc((size_t)2 * s->ntasks + 1, sizeof(olink));
@@ -1751,6 +1759,13 @@ static void build_space(ospace *s, const oracle_params *prm, int n,
     link_add(s, tk->ci, tk);
     if (tk->is_pair) link_add(s, tk->cj, tk);
   }
+}
+
+static void build_space(ospace *s, const oracle_params *prm, int n,
+                        const double *x, const float *v, const float *m,
+                        const float *h, const float *u,
+                        const signed char *time_bin) {
+  build_space_sorted(s, prm, n, x, v, m, h, u, time_bin, 1);
 }
 
 static void free_space(ospace *s) {
@@ -1908,6 +1923,103 @@ int sph_oracle_run(const oracle_params *prm, int n, const double *x,
   res->ntasks = s.ntasks;
   free_space(&s);
   return status;
+}
+
+/* The first density pass restricted to the tasks that touch the top cells
+ * tops[0..ntops): those cells and their neighbours are sorted, the tasks
+ * run in sph_oracle_run's order, and every particle of a listed top cell
+ * gets its complete first-pass sums and neighbour count -- the same bits
+ * as the whole pass, since it receives the same contributions from the
+ * same tasks in the same order.  Other particles' values are partial.
+ * Fields 0-7 and all ints are written.  For boxes whose whole pass would
+ * take minutes. */
+int sph_oracle_first_pass_tops(const oracle_params *prm, int n, const double *x,
+                               const float *v, const float *m, const float *h,
+                               const float *u, const signed char *time_bin,
+                               int ntops, const int32_t *tops, oracle_result *res) {
+  /* the tree without sorts; the listed cells and their neighbours are
+   * sorted below */
+  ospace s;
+  build_space_sorted(&s, prm, n, x, v, m, h, u, time_bin, 0);
+  const int *cdim = s.cdim;
+  const int ntop = cdim[0] * cdim[1] * cdim[2];
+  unsigned char *sel = (unsigned char *)ocalloc((size_t)ntop, 1);
+  unsigned char *near = (unsigned char *)ocalloc((size_t)ntop, 1);
+  for (int t = 0; t < ntops; t++) {
+    const int cid = tops[t];
+    if (cid < 0 || cid >= ntop) continue;
+    sel[cid] = 1;
+    const int i = cid / (cdim[1] * cdim[2]), j = (cid / cdim[2]) % cdim[1], k = cid % cdim[2];
+    for (int di = -1; di <= 1; di++)
+      for (int dj = -1; dj <= 1; dj++)
+        for (int dk = -1; dk <= 1; dk++) {
+          int ii = i + di, jj = j + dj, kk = k + dk;
+          if (prm->periodic) {
+            ii = (ii + cdim[0]) % cdim[0];
+            jj = (jj + cdim[1]) % cdim[1];
+            kk = (kk + cdim[2]) % cdim[2];
+          } else if (ii < 0 || ii >= cdim[0] || jj < 0 || jj >= cdim[1] || kk < 0 ||
+                     kk >= cdim[2])
+            continue;
+          near[kk + cdim[2] * (jj + cdim[1] * ii)] = 1;
+        }
+  }
+  for (int cid = 0; cid < ntop; cid++)
+    if (near[cid] && s.top[cid].count > 0) do_sort(&s.top[cid]);
+  for (int k = 0; k < n; k++) init_part(&s.parts[k]);
+  for (int t = 0; t < s.ntasks; t++) {
+    const otask *tk = &s.tasks[t];
+    const int ci = (int)(tk->ci - s.top);
+    const int cj = tk->is_pair ? (int)(tk->cj - s.top) : ci;
+    if (!sel[ci] && !sel[cj]) continue;
+    if (!tk->is_pair)
+      dosub_self1(&s.e, tk->ci, 0);
+    else
+      dosub_pair1(&s.e, tk->ci, tk->cj, 0);
+  }
+  for (int k = 0; k < n; k++) {
+    const opart *p = &s.parts[k];
+    float *o = &res->fields[ORACLE_NFIELDS * p->id];
+    o[0] = p->rho;
+    o[1] = p->rho_dh;
+    o[2] = p->wcount;
+    o[3] = p->wcount_dh;
+    o[4] = p->div_v;
+    o[5] = p->rot_v[0];
+    o[6] = p->rot_v[1];
+    o[7] = p->rot_v[2];
+  }
+  for (int c = 0; c < s.pool.ncells; c++) {
+    const ocell *cc = &s.pool.cells[c];
+    if (cc->split || cc->count == 0) continue;
+    const ocell *top = cc;
+    while (top->parent) top = top->parent;
+    for (int k = 0; k < cc->count; k++) {
+      const opart *p = &cc->parts[k];
+      int32_t *ip = &res->ints[ORACLE_NINTS * p->id];
+      ip[0] = (int32_t)(cc->parts - s.parts);
+      ip[1] = cc->count;
+      ip[2] = cc->depth;
+      ip[3] = p->depth_h;
+      ip[4] = (int32_t)(p - s.parts);
+      ip[5] = (int32_t)(top - s.top);
+      ip[6] = p->ngb_d;
+      ip[7] = p->ngb_d;
+      ip[8] = 0;
+      ip[9] = 0;
+      ip[10] = 0;
+    }
+  }
+  res->cdim[0] = cdim[0];
+  res->cdim[1] = cdim[1];
+  res->cdim[2] = cdim[2];
+  res->ncells = s.pool.ncells;
+  res->status = 0;
+  res->ntasks = s.ntasks;
+  free(sel);
+  free(near);
+  free_space(&s);
+  return 0;
 }
 
 /* The force loops alone on a given state: every particle takes h, rho,

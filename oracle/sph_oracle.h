@@ -35,6 +35,10 @@ typedef struct {
    * both 0 keeps one task per top cell and top-cell pair; otherwise the
    * tasks are split as the reference's scheduler splits them. */
   int32_t subsize_self, subsize_pair;
+  /* 0: the tasks in the reference driver's creation order; 1: the same
+   * tasks in reverse order (another order the reference's scheduler may
+   * run them in: density and force tasks are independent of each other). */
+  int32_t reverse_tasks;
 } oracle_params;
 
 typedef struct {
@@ -57,6 +61,14 @@ int sph_oracle_run_state(const oracle_params *prm, int n, const double *x,
                          const float *v, const float *m, const float *u,
                          const signed char *time_bin, const float *state,
                          oracle_result *res);
+
+/* The first density pass of the tasks touching the top cells tops[0..ntops)
+ * only: complete (bit-identical to sph_oracle_run) for the particles of
+ * those cells, partial elsewhere; fields 0-7 and the ints are written. */
+int sph_oracle_first_pass_tops(const oracle_params *prm, int n, const double *x,
+                               const float *v, const float *m, const float *h,
+                               const float *u, const signed char *time_bin,
+                               int ntops, const int32_t *tops, oracle_result *res);
 
 /* Sort arrays of every non-empty cell, depth first: rec [ncells][3] =
  * first (cell-sorted order), count, depth; d / idx: per cell 13 arrays of

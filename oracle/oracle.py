@@ -176,8 +176,10 @@ def first_pass_tops(box, tops, **kw):
     return out
 
 
-def exact64(box, out):
-    """FP64 sums (rho, wcount, div_v, a[3], u_dt) at the oracle's final h."""
+def exact64(box, out, which=None):
+    """FP64 sums (rho, wcount, div_v, a[3], u_dt) at the oracle's final h;
+    with ``which`` (bool per particle) only for those particles (zeros
+    elsewhere)."""
     L = lib()
     n = box["x"].shape[0]
     x = np.ascontiguousarray(box["x"], np.float64)
@@ -187,11 +189,19 @@ def exact64(box, out):
             for k in ("h", "rho", "f", "pressure", "soundspeed", "balsara")]
     res = np.zeros((n, 7), np.float64)
     prm = make_params(box)
-    L.sph_oracle_exact64(ctypes.byref(prm), ctypes.c_int(n),
-                         _ptr(x, ctypes.c_double), _ptr(v, ctypes.c_float),
-                         _ptr(m, ctypes.c_float),
-                         *[_ptr(a, ctypes.c_float) for a in arrs],
-                         _ptr(res, ctypes.c_double))
+    if which is None:
+        L.sph_oracle_exact64(ctypes.byref(prm), ctypes.c_int(n),
+                             _ptr(x, ctypes.c_double), _ptr(v, ctypes.c_float),
+                             _ptr(m, ctypes.c_float),
+                             *[_ptr(a, ctypes.c_float) for a in arrs],
+                             _ptr(res, ctypes.c_double))
+    else:
+        w = np.ascontiguousarray(which, np.uint8)
+        L.sph_oracle_exact64_some(ctypes.byref(prm), ctypes.c_int(n),
+                                  _ptr(x, ctypes.c_double), _ptr(v, ctypes.c_float),
+                                  _ptr(m, ctypes.c_float),
+                                  *[_ptr(a, ctypes.c_float) for a in arrs],
+                                  _ptr(w, ctypes.c_ubyte), _ptr(res, ctypes.c_double))
     return res
 
 

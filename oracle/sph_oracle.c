@@ -2150,10 +2150,11 @@ static inline void kernel_deval_d(double u, double *W, double *dW) {
   *dW = C / (kg * kg * kg * kg) * (-20.0) * x * om * om * om;
 }
 
-void sph_oracle_exact64(const oracle_params *prm, int n, const double *x,
-                        const float *v, const float *m, const float *h,
-                        const float *rho, const float *f, const float *P,
-                        const float *cs, const float *bal, double *out) {
+static void exact64_impl(const oracle_params *prm, int n, const double *x,
+                         const float *v, const float *m, const float *h,
+                         const float *rho, const float *f, const float *P,
+                         const float *cs, const float *bal, const unsigned char *which,
+                         double *out) {
   /* out per particle: rho, wcount, div_v, a[3], u_dt (7 doubles) */
   double hmax = 0;
   for (int k = 0; k < n; k++) hmax = fmax(hmax, h[k]);
@@ -2181,6 +2182,7 @@ void sph_oracle_exact64(const oracle_params *prm, int n, const double *x,
   }
   const int reach[3] = {cd[0] < 3 ? 0 : 1, cd[1] < 3 ? 0 : 1, cd[2] < 3 ? 0 : 1};
   for (int i = 0; i < n; i++) {
+    if (which && !which[i]) continue;
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
     const double hi = h[i], hi_inv = 1.0 / hi;
     int ix[3];
@@ -2253,4 +2255,21 @@ void sph_oracle_exact64(const oracle_params *prm, int n, const double *x,
   }
   free(head);
   free(next);
+}
+
+void sph_oracle_exact64(const oracle_params *prm, int n, const double *x,
+                        const float *v, const float *m, const float *h,
+                        const float *rho, const float *f, const float *P,
+                        const float *cs, const float *bal, double *out) {
+  exact64_impl(prm, n, x, v, m, h, rho, f, P, cs, bal, NULL, out);
+}
+
+/* The same sums for the particles with which[i] != 0 only (the others'
+ * rows of out are left as they are). */
+void sph_oracle_exact64_some(const oracle_params *prm, int n, const double *x,
+                             const float *v, const float *m, const float *h,
+                             const float *rho, const float *f, const float *P,
+                             const float *cs, const float *bal,
+                             const unsigned char *which, double *out) {
+  exact64_impl(prm, n, x, v, m, h, rho, f, P, cs, bal, which, out);
 }

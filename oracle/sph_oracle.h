@@ -84,6 +84,11 @@ void sph_oracle_exact64(const oracle_params *prm, int n, const double *x,
                         const float *v, const float *m, const float *h,
                         const float *rho, const float *f, const float *P,
                         const float *cs, const float *bal, double *out);
+void sph_oracle_exact64_some(const oracle_params *prm, int n, const double *x,
+                             const float *v, const float *m, const float *h,
+                             const float *rho, const float *f, const float *P,
+                             const float *cs, const float *bal,
+                             const unsigned char *which, double *out);
 /* Time integration (sph_integrate.c).  State arrays are SoA in the
  * caller's order: x[3 n] (double), v_full, v (predicted), a (a_hydro) [3 n];
  * u_full, u (predicted), u_dt, h, h_dt, rho, P, c, v_sig [n]; time_bin [n]. */

@@ -39,16 +39,26 @@ __global__ void block_hmax(const int2* __restrict__ fc, float4* __restrict__ lo,
   }
 }
 
-template <bool FORCE, int WPB, int MINB, bool LISTS = false, int TPP = 1>
+template <bool FORCE, int WPB, int MINB, bool LISTS = false, int TPP = 1, bool BULK = false>
 static cudaError_t launch_variant(const G2Args& a, int num_sms, int max_units,
                                   cudaStream_t s) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS, TPP>, WPB * 32, 0);
+      &per_sm, gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS, TPP, BULK>, WPB * 32, 0);
   int grid = std::max(1, per_sm) * num_sms;
   grid = std::max(1, std::min(grid, (max_units + WPB - 1) / WPB));
-  gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS, TPP><<<grid, WPB * 32, 0, s>>>(a);
+  gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS, TPP, BULK><<<grid, WPB * 32, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+// The bulk-copy staging (G2Args::bulk) exists for the 8-warp tile shape with
+// one or two lanes per particle; other shapes stage with loads.
+template <int TPP>
+static cudaError_t launch_bulk(const G2Args& a, bool force, bool lists, int num_sms,
+                               int max_units, cudaStream_t s) {
+  if (force) return launch_variant<true, 8, 3, false, TPP, true>(a, num_sms, max_units, s);
+  if (lists) return launch_variant<false, 8, 3, true, TPP, true>(a, num_sms, max_units, s);
+  return launch_variant<false, 8, 3, false, TPP, true>(a, num_sms, max_units, s);
 }
 
 template <int TPP>
@@ -68,6 +78,9 @@ static cudaError_t launch_shape(const G2Args& a, bool force, int num_sms, int ma
 // or two lanes.
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
                           cudaStream_t s, int block_warps, bool lists, int tpp) {
+  if (a.bulk && block_warps == 8 && (tpp == 1 || tpp == 2))
+    return tpp == 2 ? launch_bulk<2>(a, force, lists, num_sms, max_units, s)
+                    : launch_bulk<1>(a, force, lists, num_sms, max_units, s);
   if (lists && !force) {
     if (tpp == 2)
       return block_warps == 4 ? launch_variant<false, 4, 6, true, 2>(a, num_sms, max_units, s)

@@ -123,6 +123,52 @@ struct LaneSmem {
   float4 ftab[27];     // frame offsets of the 27 partner top cells (offset_of)
 };
 
+// Per-warp staging of the bulk-copy variant (BULK): the next block's records
+// as they lie in the store, and the mbarrier its copy completes on.
+struct BulkSmem {
+  float4 raw[32];
+  unsigned long long bar;  // transaction bytes of one copy
+  unsigned parity;         // phase of bar the next copy completes
+};
+
+// --- bulk copies (the TMA engine's untiled cp.async.bulk) ------------------
+// A j-block is a contiguous run of the store, so its records (16 bytes
+// each, 16-byte aligned) can be fetched by one bulk copy issued by one lane
+// into the warp's shared memory, completing on an mbarrier.
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void bulk_bar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  // the barrier's initialisation is seen by the async proxy before any copy
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_fetch(float4* dst, const float4* src, int count,
+                                           unsigned long long* bar) {
+  const unsigned bytes = 16u * (unsigned)count;
+  // earlier generic-proxy reads of dst are ordered before the async write
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+// Wait for the barrier's phase `parity` to complete, at most `tries` polls
+// (each poll may suspend the thread for a while); false when it did not.
+__device__ __forceinline__ bool bulk_wait(unsigned long long* bar, unsigned parity, int tries) {
+  for (int t = 0; t < tries; t++) {
+    unsigned done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+#define BULK_WAIT_TRIES (1 << 20)
+
 // Frame offset of a partner top cell from its index in the 3x3x3
 // neighbourhood of the group's top cell (ix + 3 iy + 9 iz, each in 0..2).
 __device__ __forceinline__ float3 offset_of(int idx, float3 tw) {
@@ -150,14 +196,18 @@ __device__ __forceinline__ float3 offset_of(int idx, float3 tw) {
 // TPP (threads per particle, 1 or 2): a warp serves 32 / TPP particles of a
 // window; the TPP lanes of a particle split each staged block's candidates
 // and add their partial sums at the end.
+// BULK: each surviving j-block is fetched into shared memory by one bulk
+// copy (cp.async.bulk, one lane) while the previous one is tested, instead
+// of a register load per lane.
 template <bool FORCE, int OUT = OUT_STORE, int WPB = WARPS_PER_BLOCK, int MINB = 3,
-          bool LISTS = false, int TPP = 1>
+          bool LISTS = false, int TPP = 1, bool BULK = false>
 __global__ void __launch_bounds__(WPB * 32, MINB)
 gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
   static_assert(TPP == 1 || TPP == 2 || TPP == 4, "one, two or four lanes per particle");
   static_assert(TPP == 1 || (OUT == OUT_STORE && (!LISTS || TPP == 2)),
                 "several lanes: stored sums; lists with one or two lanes");
   __shared__ LaneSmem smem[WPB];
+  __shared__ BulkSmem bsm[BULK ? WPB : 1];
   const int lane = threadIdx.x & 31;
   const int sub = lane % TPP, pl = lane / TPP;  // lane within the particle, particle
   LaneSmem& ws = smem[threadIdx.x >> 5];
@@ -177,6 +227,14 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
     __syncwarp();
   };
   fill_ftab();
+  BulkSmem& wb = bsm[BULK ? (threadIdx.x >> 5) : 0];
+  if (BULK) {
+    if (lane == 0) {
+      bulk_bar_init(&wb.bar);
+      wb.parity = 0u;
+    }
+    __syncwarp();
+  }
   for (;;) {
     int u = 0;
     if (lane == 0) u = atomicAdd(a.queue, 1);
@@ -491,12 +549,40 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
       }
       __syncwarp();
       const int nsurv = __popc(mask);
-      // positions of the next surviving block, loaded one block ahead
+      // positions of the next surviving block, loaded one block ahead: by
+      // every lane into registers, or (bulk) by one bulk copy into the
+      // warp's shared memory
       float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (nsurv > 0 && lane < ws.scount[0]) qn = P.posh[ws.sfirst[0] + lane];
+      if (BULK) {
+        if (nsurv > 0 && lane == 0) bulk_fetch(wb.raw, P.posh + ws.sfirst[0], ws.scount[0], &wb.bar);
+      } else if (nsurv > 0 && lane < ws.scount[0]) {
+        qn = P.posh[ws.sfirst[0] + lane];
+      }
       for (int k = 0; k < nsurv; k++) {
-        const float4 q = qn;
-        if (k + 1 < nsurv && lane < ws.scount[k + 1]) qn = P.posh[ws.sfirst[k + 1] + lane];
+        float4 q = qn;
+        if (BULK) {
+          // the copy of block k has landed: take this lane's record, then
+          // start the copy of block k + 1 into the same buffer
+          int ok = 1;
+          if (lane == 0) ok = bulk_wait(&wb.bar, wb.parity, BULK_WAIT_TRIES);
+          ok = __shfl_sync(FULL, ok, 0);
+          if (!ok) {
+            // give up on the launch: report, let the copy in flight finish
+            // (bounded), leave
+            if (lane == 0) {
+              if (a.err) atomicExch(a.err, 1);
+              bulk_wait(&wb.bar, wb.parity, BULK_WAIT_TRIES);
+            }
+            return;
+          }
+          if (lane == 0) wb.parity ^= 1u;
+          if (lane < ws.scount[k]) q = wb.raw[lane];
+          __syncwarp();
+          if (k + 1 < nsurv && lane == 0)
+            bulk_fetch(wb.raw, P.posh + ws.sfirst[k + 1], ws.scount[k + 1], &wb.bar);
+        } else if (k + 1 < nsurv && lane < ws.scount[k + 1]) {
+          qn = P.posh[ws.sfirst[k + 1] + lane];
+        }
         const float4 sfd = ws.sf[k];
         const float4 slo = ws.slo[k], shi = ws.shi[k];
         const int eidx = ws.se[k];
@@ -787,25 +873,33 @@ static __global__ void __launch_bounds__(256, 4)
               if ((pk[u] & 0x07ffffff) >= P.n || ((unsigned)pk[u] >> 27) > 26) pk[u] = i;
             }
 #pragma unroll
+            for (int u = 0; u < 3; u++) q[u] = P.posh[pk[u] & 0x07ffffff];
+            // a row recorded at another h holds many items beyond this
+            // particle's radius: only the partners that can be hits (r^2
+            // below the band's top) have their velocity and mass read; a
+            // miss is evaluated with zeros beyond the kernel's support
+            float dxs[3], dys[3], dzs[3], r2s[3];
+#pragma unroll
             for (int u = 0; u < 3; u++) {
-              q[u] = P.posh[pk[u] & 0x07ffffff];
-              vm[u] = P.velm[pk[u] & 0x07ffffff];
+              const float4 fd = ftab[(unsigned)pk[u] >> 27];
+              dxs[u] = pi.x - (q[u].x + fd.x);
+              dys[u] = pi.y - (q[u].y + fd.y);
+              dzs[u] = pi.z - (q[u].z + fd.z);
+              r2s[u] = dxs[u] * dxs[u] + dys[u] * dys[u] + dzs[u] * dzs[u];
+              vm[u] = r2s[u] < U2 ? P.velm[pk[u] & 0x07ffffff] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
 #pragma unroll
             for (int u = 0; u < 3; u++) {
               const int j = pk[u] & 0x07ffffff;
-              const float4 fd = ftab[(unsigned)pk[u] >> 27];
-              const float dx = pi.x - (q[u].x + fd.x), dy = pi.y - (q[u].y + fd.y),
-                          dz = pi.z - (q[u].z + fd.z);
-              const float r2 = dx * dx + dy * dy + dz * dz;
+              const float r2 = r2s[u];
               const bool item = t0 + u * LPP < cnt;
               bool hit = item && r2 < L2;
               if (item && !hit && r2 < U2) {
                 const Entry* E = rerun_entry(a, P.leaf_of[i], a.blk_of[j], P.depth_h[i]);
                 hit = E != nullptr && exact_r2_2(P.xd, i, j, E) < hig2;
               }
-              density_hit(dx, dy, dz, hit ? r2 : 4.f * U2, vi, vm[u], hi_inv, s0, s1, s2, s3, s4,
-                          s5, s6, s7);
+              density_hit(dxs[u], dys[u], dzs[u], hit ? r2 : 4.f * U2, vi, vm[u], hi_inv, s0, s1,
+                          s2, s3, s4, s5, s6, s7);
               ngb += hit;
             }
           }

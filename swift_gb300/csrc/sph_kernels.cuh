@@ -87,6 +87,11 @@ struct G2Args {
   int force_rows = 0;
   int nl_seg = 1;
   const int* blk_of = nullptr;  // j-block of every particle (frame lookups)
+  // j-blocks staged by bulk copies (cp.async.bulk into shared memory, one
+  // per block, completing on an mbarrier) instead of a load per lane; a
+  // wait that runs out sets *err (the host reports it) and ends the warp
+  int bulk = 0;
+  int* err = nullptr;
 };
 
 // Later re-runs from the lists: particles whose list covers their new

@@ -1,13 +1,17 @@
 #!/usr/bin/env python3
 """Benchmark: SPH pair-interactions/s of one density -> ghost -> force step.
 
-Workload (default): the 128^3 = 2,097,152-particle periodic box drawn from a
-clustered density field (lattice displaced by a seeded Gaussian random field
-with P(k) ~ k^-2, rms displacement 0.3 of the spacing), Minimal SPH with the
-Wendland C2 kernel, all particles active.  A step is one full pass -- density
-loop, the ghost's Newton iterations on h with density re-runs, force loop --
-starting from h0 = eta * spacing, run by the batched form (one persistent
-gather launch per loop, one CUDA graph per step).
+Workload (default): the 384^3 = 56,623,104-particle periodic box drawn from a
+strongly clustered density field (lattice displaced by a seeded Gaussian
+random field with P(k) ~ k^-2, rms displacement 1.0 of the spacing, density
+contrast rms ~5), Minimal SPH with the Wendland C2 kernel, all particles
+active -- the largest of the workloads that fits one GPU.  A step is one full
+pass -- density loop, the ghost's Newton iterations on h with density
+re-runs, force loop -- starting from h0 = eta * spacing, run by the batched
+form (one persistent gather launch per loop, CUDA graphs per step).
+The same line carries the two targets of the batched and serving forms
+(`targets`): the sparse-activity 256^3 Sedov box in the batched and the plain
+per-task forms, and the serving loop's boxes/s and p50/p99 latency.
 
   value   interactions/s with the particle state resident in HBM;
   e2e     the same through the C ABI with host buffers: every step copies the
@@ -65,6 +69,10 @@ WORKLOADS = {
                      "time integration kernels (drift, kick2, timestep, kick1) over "
                      "384^3=56,623,104 particles of device-resident state; plus the "
                      "engine sequence on a 32^3 jittered lattice"),
+    "sort128": ("sort", 128, 0.3,
+                "per-cell 13-axis sort arrays (runner_do_hydro_sort) of every cell of the "
+                "128^3=2,097,152-particle clustered box (rms 0.3 spacing): leaves sorted, "
+                "split cells merged, deepest first"),
     "rebuild384": ("rebuild", 384, 1.0,
                    "device-resident cell assignment (top-level grid, top cell per particle, "
                    "octree split, depth_h) of 384^3=56,623,104 particles, lattice displaced "
@@ -108,12 +116,18 @@ def peaks():
         return {}
 
 
-def fp32_peak_tflops(pk):
-    """FP32 issue peak: 152 SMs x 128 FP32 lanes x 2 flop (FMA) x SM clock.
+def sm_count(device=0):
+    """Streaming multiprocessors of the GPU (cudaDevAttrMultiProcessorCount)."""
+    import torch
+    return int(torch.cuda.get_device_properties(device).multi_processor_count)
+
+
+def fp32_peak_tflops(pk, sms):
+    """FP32 issue peak: SMs x 128 FP32 lanes x 2 flop (FMA) x SM clock.
     MEASURED_PEAKS.json carries no FP32 figure; its measured maximum SM clock
     is used, else the nominal 2070 MHz."""
     mhz = float(pk.get("sm_max_mhz", 2070.0))
-    return 152 * 128 * 2 * mhz * 1e6 / 1e12, mhz
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, mhz
 
 
 class ClockSampler:
@@ -168,27 +182,44 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------------
 # CPU leg: the oracle's restatement of the reference loops, one box per core.
+# The reference itself cannot run on the GPU host (its tree is not there), so
+# the timed CPU path is the restatement built with the reference's stock
+# optimisation flags (-O3 -ffast-math -funroll-loops -fomit-frame-pointer and
+# the host CPU's own tuning).
+
+# Per workload: the sample the CPU times -- a box of the same generator and
+# parameters (same neighbour-count distribution per particle), at the size one
+# core finishes in a few seconds.
+CPU_SAMPLE = {"large384": "clustered:64:1.0", "clustered128": "clustered:64:0.3"}
+
+
+def _parse_sample(spec):
+    parts = spec.split(":")
+    kind, n = parts[0], int(parts[1])
+    rms = float(parts[2]) if len(parts) > 2 else 0.3
+    return kind, n, rms
+
 
 def _cpu_box_worker(args):
     spec, seed = args
     sys.path.insert(0, ROOT)
     from swift_gb300 import ics
     from oracle import oracle
-    kind, n = spec.split(":")
-    box = (ics.clustered(int(n), seed=seed, rms=0.3) if kind == "clustered"
-           else ics.lattice(int(n), seed=seed))
+    kind, n, rms = _parse_sample(spec)
+    box = (ics.clustered(n, seed=seed, rms=rms) if kind == "clustered"
+           else ics.lattice(n, seed=seed))
     t0 = time.perf_counter()
-    out = oracle.run(box)
+    out = oracle.run(box, stock=True)
     dt = time.perf_counter() - t0
     hits = int(out["ngb_final"].sum()) + int(out["ngb_force"].sum())
-    return hits, dt
+    return hits, dt, box["x"].shape[0]
 
 
-def cpu_baseline(spec="clustered:48", boxes_per_core=1, cores=None):
-    """Interactions/s of the reference loops restated in C (oracle), run as
-    independent boxes on all host cores (spawned workers)."""
+def cpu_baseline(spec="clustered:64:1.0", boxes_per_core=1, cores=None):
+    """Interactions/s of the reference loops restated in C (oracle, stock
+    flags), run as independent boxes on all host cores (spawned workers)."""
     from oracle import oracle
-    oracle.build()
+    oracle.build(stock=True)
     cores = cores or os.cpu_count() or 1
     jobs = [(spec, 1000 + k) for k in range(cores * boxes_per_core)]
     ctx = mp.get_context("spawn")
@@ -202,10 +233,13 @@ def cpu_baseline(spec="clustered:48", boxes_per_core=1, cores=None):
     # slowest one bounds the sample (process start-up and IC generation are
     # excluded)
     loop_s = max(r[1] for r in res) * boxes_per_core
+    kind, n, rms = _parse_sample(spec)
+    gen = f"clustered rms {rms:g} spacing" if kind == "clustered" else kind
     return {"value": hits / loop_s, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{len(jobs)} independent {spec.replace(':', ' ')}^3 boxes "
-                      f"(same generator), one per worker process; {cpu_s:.1f} s of "
-                      f"CPU work, {wall:.1f} s wall"}
+            "build": "oracle/sph_oracle.c with " + " ".join(oracle.stock_flags()),
+            "sample": f"{len(jobs)} independent {n}^3 = {res[0][2]:,}-particle boxes of "
+                      f"the workload's generator ({gen}), one per worker process; "
+                      f"{cpu_s:.1f} s of CPU work, {wall:.1f} s wall"}
 
 
 # ---------------------------------------------------------------------------
@@ -216,8 +250,9 @@ def run_reference_arm(args):
         return 0
     t0 = time.perf_counter()
     vals = []
+    spec = args.cpu_sample or CPU_SAMPLE.get(args.workload, "clustered:64:1.0")
     for _ in range(max(1, args.steps)):
-        cb = cpu_baseline(args.cpu_sample)
+        cb = cpu_baseline(spec)
         vals.append(cb["value"])
     value = statistics.median(vals)
     wall = time.perf_counter() - t0
@@ -228,7 +263,7 @@ def run_reference_arm(args):
         "vs_baseline": None, "dtype": "f32 (f64 positions)",
         "data": "synthetic (seeded generators)",
         "config": {"workload": WORKLOADS[args.workload][3],
-                   "sample": args.cpu_sample, "parallelism": "replicas"},
+                   "sample": spec, "parallelism": "replicas"},
         "cpu_baseline": {**cb, "value": value},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -238,12 +273,12 @@ def run_reference_arm(args):
     return 0
 
 
-def traffic_from_profile(workload, tuning):
-    """DRAM bytes per force-gather launch from the committed ncu summary of
-    this workload: the capture made with the same j-block depth and lanes per
-    particle (lines "traffic_bytes_per_launch: N (...) — jtile J,
-    threads_per_particle T")."""
-    path = os.path.join(ROOT, "profiles", f"force_gather_{workload}.md")
+def traffic_from_profile(kernel, workload, tuning):
+    """DRAM bytes per launch of a gather (kernel "density_gather" or
+    "force_gather") from the committed ncu summary of this workload: the
+    capture made with the same j-block depth and lanes per particle (lines
+    "traffic_bytes_per_launch: N (...) — jtile J, threads_per_particle T")."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     want = (f"jtile {tuning.get('jtile')}",
             f"threads_per_particle {tuning.get('threads_per_particle', 1)}")
     try:
@@ -256,7 +291,7 @@ def traffic_from_profile(workload, tuning):
     return None
 
 
-def run_sparse(args):
+def sparse_record(workload, steps, warmup, plain_steps, seed):
     """Sparse activity (256^3 Sedov blast, 8 time bins): after one step with
     every particle active (untimed, it gives every particle a density and
     force state), each step activates the bins the power-of-two time-line
@@ -271,11 +306,11 @@ def run_sparse(args):
     from swift_gb300 import api, ics
     rank, local_rank, world = dist_env()
     torch.cuda.set_device(local_rank)
-    box = make_box(args.workload, seed=args.seed + rank)
+    box = make_box(workload, seed=seed + rank)
     n = box["x"].shape[0]
     sp = api.Space(box)
     nb = int(box.get("bin_base", 20))
-    seq = [ics.max_active_bin_for_step(k, base=nb) for k in range(1, 1 + args.warmup + args.steps)]
+    seq = [ics.max_active_bin_for_step(k, base=nb) for k in range(1, 1 + warmup + steps)]
     active_frac = {b: float(np.mean(box["time_bin"] <= b)) for b in set(seq)}
 
     def prime():
@@ -292,13 +327,13 @@ def run_sparse(args):
         return time.perf_counter() - t0
 
     prime()
-    for b in seq[:args.warmup]:
+    for b in seq[:warmup]:
         one(b, False)
     sp.phase_times(reset=True)
     sp.host_times(reset=True)
     clocks = ClockSampler(local_rank)
     t_b, inter = [], []
-    for b in seq[args.warmup:]:
+    for b in seq[warmup:]:
         t_b.append(one(b, False))
         hits = sp.count_hits()  # untimed replay of the same step, instrumented
         inter.append(int(hits[3]) + int(hits[2]))
@@ -307,23 +342,23 @@ def run_sparse(args):
     host_ms = {k: v / max(1, len(t_b)) for k, v in sp.host_times(reset=True).items()}
     # plain form: same state origin, same steps
     prime()
-    for b in seq[:min(args.warmup, 1)]:
+    for b in seq[:min(warmup, 1)]:
         one(b, True)
-    t_p = [one(b, True) for b in seq[args.warmup:][:args.plain_steps]]
+    t_p = [one(b, True) for b in seq[warmup:][:plain_steps]]
     sp.close()
     ms_b = 1e3 * sum(t_b) / len(t_b)
     ms_p = 1e3 * sum(t_p) / len(t_p)
     ms_p_same = 1e3 * sum(t_b[:len(t_p)]) / len(t_p)
     out = {
         "metric": METRIC, "value": sum(inter) / sum(t_b), "unit": UNIT,
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": 1, "steps": steps, "warmup": warmup,
         "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (f64 positions)",
         "data": "synthetic (seeded generators, no dataset)",
-        "config": {"workload": WORKLOADS[args.workload][3], "particles": n,
+        "config": {"workload": WORKLOADS[workload][3], "particles": n,
                    "form": "batched persistent; steps timed on the host clock "
                            "including host planning",
-                   "max_active_bin_per_step": seq[args.warmup:],
+                   "max_active_bin_per_step": seq[warmup:],
                    "active_fraction": {str(k): v for k, v in sorted(active_frac.items())}},
         "phases_ms_gpu": {"density": phase_ms[0] / max(1, nsteps),
                           "ghost_rounds": phase_ms[1] / max(1, nsteps),
@@ -335,7 +370,12 @@ def run_sparse(args):
         "interactions_per_step": inter,
         "clocks": clk,
     }
-    print(json.dumps(out), flush=True)
+    return out
+
+
+def run_sparse(args):
+    print(json.dumps(sparse_record(args.workload, args.steps, args.warmup, args.plain_steps,
+                                   args.seed)), flush=True)
 
 
 def run_integrate(args):
@@ -524,7 +564,7 @@ def run_rebuild(args):
     print(json.dumps(out), flush=True)
 
 
-def run_serving(args):
+def serving_record(workload, seed, plain_boxes):
     """Continuous-batching serving loop over a seeded stream of boxes.
 
     1. capacity: a burst of the first 300 requests, all arriving at t = 0,
@@ -538,8 +578,8 @@ def run_serving(args):
     import torch
     from swift_gb300 import api, serve
     torch.cuda.set_device(0)
-    count = WORKLOADS[args.workload][1]
-    specs = serve.request_stream(count, seed=args.seed)
+    count = WORKLOADS[workload][1]
+    specs = serve.request_stream(count, seed=seed)
     t = time.perf_counter()
     boxes = serve.make_boxes(specs, processes=min(16, os.cpu_count() or 1))
     gen_s = time.perf_counter() - t
@@ -552,7 +592,7 @@ def run_serving(args):
     capacity = burst / wall_b
     # 2. the stream at 80% of capacity
     rate = 0.8 * capacity
-    arr = serve.poisson_arrivals(count, rate, seed=args.seed)
+    arr = serve.poisson_arrivals(count, rate, seed=seed)
     clocks = ClockSampler(0)
     with api.Server() as srv:
         lat, wall, _ = serve.serve(srv, boxes, arr, serve.STEPS)
@@ -563,7 +603,7 @@ def run_serving(args):
     # 3. one box at a time: plain per-task form and single-box batched form
     # boxes at evenly spaced quantiles of N, so that the sample's mean size
     # is the stream's
-    k = min(args.plain_boxes, count)
+    k = min(plain_boxes, count)
     by_n = np.argsort(nparts, kind="stable")
     sample = sorted(int(by_n[int((q + 0.5) * count / k)]) for q in range(k))
 
@@ -586,7 +626,7 @@ def run_serving(args):
         "warmup": 0, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (f64 positions)",
         "data": "synthetic (seeded request stream)",
-        "config": {"workload": WORKLOADS[args.workload][3], "requests": count,
+        "config": {"workload": WORKLOADS[workload][3], "requests": count,
                    "particles_total": int(nparts.sum()),
                    "particles_mean": float(nparts.mean()),
                    "box_generation_s": gen_s,
@@ -602,7 +642,75 @@ def run_serving(args):
                               "particles_mean": float(nparts[sample].mean())},
         "clocks": clk,
     }
+    return out
+
+
+def run_sort(args):
+    """The whole tree's sort arrays (sphgpu_hydro_sort, all 13 axes), CUDA
+    events around each call on the launching stream.  Algorithmic bytes: a
+    leaf reads its particles' positions once (24 B each) and writes 13
+    arrays of count + 1 entries (8 B each); a split cell reads its
+    progeny's 13 arrays and writes its own (8 B per entry each way)."""
+    import numpy as np
+    import torch
+    from swift_gb300 import api, ics
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    kind, side, rms, desc = WORKLOADS[args.workload]
+    box = ics.clustered(side, seed=args.seed, rms=rms)
+    stream = torch.cuda.Stream()
+    sh = ctypes_stream(stream)
+    import ctypes
+    with api.Space(box) as sp:
+        tree = sp.tree()
+        parent = tree[:, 3]
+        split = np.zeros(len(tree), bool)
+        split[parent[parent >= 0]] = True
+        cnt = tree[:, 1].astype(np.int64)
+        nonempty = cnt > 0
+        leaf_b = np.sum(24 * cnt[~split & nonempty] + 13 * 8 * (cnt[~split & nonempty] + 1))
+        split_b = np.sum(2 * 13 * 8 * (cnt[split & nonempty] + 1))
+        algo = int(leaf_b + split_b)
+        entries = int(np.sum(13 * (cnt[nonempty] + 1)))
+        L = api.lib()
+        for _ in range(args.warmup):
+            api._check(L.sphgpu_hydro_sort(sp._h, 0x1FFF, sh))
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local_rank)
+        ms = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            api._check(L.sphgpu_hydro_sort(sp._h, 0x1FFF, sh))
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        clk = clocks.stop()
+    t = statistics.median(ms) / 1e3
+    hbm = float(peaks().get("hbm_gbs", 6800.0))
+    gbs = algo / t / 1e9
+    out = {
+        "metric": "sort entries/s (13 axes, every cell of the tree)", "value": entries / t,
+        "unit": "entries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 keys rounded to f32", "data": "synthetic",
+        "config": {"workload": desc, "particles": int(box["x"].shape[0]),
+                   "cells": int(nonempty.sum()), "split_cells": int((split & nonempty).sum()),
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "kernel": "sort_leaves + sort_merge", "achieved": gbs,
+                     "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                     "algorithmic_bytes": algo, "traffic": None,
+                     "peak_note": "hbm_gbs of MEASURED_PEAKS.json",
+                     "limiter": "one thread per (cell, axis) runs the reference's sequential "
+                                "quicksort / 8-way merge, kept for the reference's tie order"},
+        "gpu_launches": None,
+        "clocks": clk,
+    }
     print(json.dumps(out), flush=True)
+
+
+def run_serving(args):
+    print(json.dumps(serving_record(args.workload, args.seed, args.plain_boxes)), flush=True)
 
 
 def run_ours(args):
@@ -624,11 +732,18 @@ def run_ours(args):
     sp.step(stream=sh)
     if args.tuning:
         jt, bw, *tp = (int(v) for v in args.tuning.split(","))
-        sp.set_tuning(tpp=tp[0] if tp else 1, jtile=jt, block_warps=bw)
+        sp.set_tuning(tpp=tp[0] if tp else 1, jtile=jt, block_warps=bw,
+                      bulk_stage=tp[1] if len(tp) > 1 else 0,
+                      row_widen=float(args.row_widen), row_cap=int(args.row_cap))
         sp.step(stream=sh)
     if args.no_tune or args.tuning:
         tuning, tune_ms = (dict(zip(("threads_per_particle", "jtile", "rerun_lists",
                                      "block_warps"), sp.tuning())), {})
+        tuning["bulk_stage"] = sp.bulk_stage()
+        if args.row_widen:
+            tuning["row_widen"] = args.row_widen
+        if args.row_cap:
+            tuning["row_cap"] = args.row_cap
     else:
         tuning, tune_ms = sp.autotune(reps=2)
     for _ in range(args.warmup):
@@ -682,18 +797,45 @@ def run_ours(args):
         total_inter = float(inter_per_step)
 
     out = None
+    sp.close()
     if rank == 0:
         pk = peaks()
-        peak, mhz = fp32_peak_tflops(pk)
+        sms = sm_count(local_rank)
+        peak, mhz = fp32_peak_tflops(pk, sms)
         force_ms = phase_ms[2] / max(1, nsteps)
         dens_ms = phase_ms[0] / max(1, nsteps)
         ghost_ms = phase_ms[1] / max(1, nsteps)
-        achieved = FLOPS_FORCE * float(hits[2]) / (force_ms / 1e3) / 1e12
         step_flops = (FLOPS_DENSITY * float(hits[0] + hits[1])
                       + FLOPS_FORCE * float(hits[2]))
+        # Each phase is bracketed by event-record nodes inside the step's
+        # graphs (on the stream the kernels run on).  Its algorithmic work:
+        # density = 71 flop x first-pass hits; ghost = 71 flop x re-run hits
+        # (the per-particle solver from the rows and the catch-up gathers);
+        # force = 132 flop x force hits.
+        phase = {
+            "density": {"ms": dens_ms, "flop": FLOPS_DENSITY * float(hits[0]),
+                        "kernel": "gather_lanes<density, records rows> (first density pass)",
+                        "profile": "density_gather"},
+            "ghost": {"ms": ghost_ms, "flop": FLOPS_DENSITY * float(hits[1]),
+                      "kernel": "solve_from_lists + catch-up gathers (ghost re-runs)",
+                      "profile": None},
+            "force": {"ms": force_ms, "flop": FLOPS_FORCE * float(hits[2]),
+                      "kernel": "gather_lanes<force>", "profile": "force_gather"},
+        }
+        for v in phase.values():
+            v["tflops"] = v["flop"] / (v["ms"] / 1e3) / 1e12 if v["ms"] > 0 else 0.0
+            v["frac"] = v["tflops"] / peak
+        dom = max(phase, key=lambda k: phase[k]["ms"])
+        D = phase[dom]
+        traffic = (traffic_from_profile(D["profile"], args.workload, tuning)
+                   if D["profile"] else None)
         cb = None
+        spec = args.cpu_sample or CPU_SAMPLE.get(args.workload, "clustered:64:1.0")
         if not args.no_cpu:
-            cb = cpu_baseline(args.cpu_sample)
+            cb = cpu_baseline(spec)
+        targets = None
+        if args.workload == "large384" and not args.no_targets and world == 1:
+            targets = run_targets(args)
         out = {
             "metric": METRIC, "value": total_inter / t_step, "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -703,27 +845,37 @@ def run_ours(args):
             "data": "synthetic (seeded generators, no dataset)",
             "config": {
                 "workload": WORKLOADS[args.workload][3],
-                "particles_per_gpu": n, "form": "batched persistent, one CUDA graph per step",
+                "particles_per_gpu": n,
+                "form": "batched persistent: per step one CUDA graph for density + ghost "
+                        "rounds and one for the force",
                 "active": "all", "h0": "eta*spacing (ghost iterates every step)",
                 "l2": "inputs larger than L2 (particle state ~150 B/particle)",
                 "parallelism": "replicas" if world > 1 else "single",
                 "interactions_per_step": inter_per_step,
                 "tuning": tuning, "autotune_ms_per_step": tune_ms,
+                "sms": sms,
+                "cpu_sample": spec,
             },
             "phases_ms": {"density": dens_ms, "ghost_rounds": ghost_ms,
                           "force": force_ms},
+            "phases_roofline": {k: {"kernel": v["kernel"], "ms": v["ms"],
+                                    "tflops": v["tflops"], "frac": v["frac"]}
+                                for k, v in phase.items()},
             "hits_per_step": {"density_first": int(hits[0]),
                               "density_reruns": int(hits[1]),
                               "force": int(hits[2])},
             "step_tflops": step_flops / t_step / 1e12,
             "roofline": {
-                "bound": "fp32", "kernel": "gather_lanes<force>",
-                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak,
-                "peak_note": f"derived: 152 SMs x 128 FP32 lanes x 2 x {mhz:.0f} MHz "
+                "bound": "fp32", "kernel": D["kernel"], "phase": dom,
+                "achieved": D["tflops"], "peak": peak, "unit": "TFLOP/s",
+                "frac": D["frac"],
+                "peak_note": f"derived: {sms} SMs x 128 FP32 lanes x 2 x {mhz:.0f} MHz "
                              "(sm_max_mhz of MEASURED_PEAKS.json; no measured FP32 "
                              "figure there)",
-                "traffic": traffic_from_profile(args.workload, tuning),
+                "traffic": traffic,
+                "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum per launch "
+                                f"from profiles/{D['profile']}_{args.workload}.md"
+                                if traffic else None,
             },
             "e2e": {"value": total_inter / e2e_s, "unit": UNIT,
                     "h2d_bytes_per_step": int(n * (24 + 12 + 4 + 4 + 4)),
@@ -739,13 +891,51 @@ def run_ours(args):
             "gpu_launches": (6 + 8 * 3 + (2 if tuning.get("rerun_lists") else 0)) * args.steps,
             "clocks": clk,
             "cpu_baseline": cb,
+            "targets": targets,
         }
         print(json.dumps(out), flush=True)
-    sp.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def run_targets(args):
+    """The two targets of the batched and serving forms, each bounded to well
+    under a minute: (1) the sparse-activity 256^3 Sedov box, batched form
+    against the plain per-task form on the same steps; (2) the serving loop
+    over the 2,000-box stream (capacity burst, Poisson arrivals at 80 % of it,
+    p50/p99 latency), with two boxes timed one by one in the plain and the
+    single-box batched forms."""
+    out = {}
+    try:
+        r = sparse_record("sedov256", steps=4, warmup=3, plain_steps=2, seed=args.seed)
+        out["batched_over_plain"] = {
+            "workload": WORKLOADS["sedov256"][3], "target": ">= 3",
+            "value": r["plain_over_batched"],
+            "batched_ms_per_step": r["ms_per_step"],
+            "plain_ms_per_step": r["plain_ms_per_step"],
+            "host_ms_per_step": r["host_ms_per_step"],
+            "phases_ms_gpu": r["phases_ms_gpu"],
+            "active_fraction": r["config"]["active_fraction"],
+            "clocks": r["clocks"]}
+    except Exception as e:  # recorded, not fatal to the headline line
+        out["batched_over_plain"] = {"error": repr(e)}
+    try:
+        r = serving_record("serve2000", seed=args.seed, plain_boxes=2)
+        out["serving"] = {
+            "workload": WORKLOADS["serve2000"][3], "target": ">= 2 x plain",
+            "boxes_per_s": r["value"], "latency": r["latency"],
+            "capacity_boxes_per_s": r["capacity_boxes_per_s"],
+            "serve_over_plain": r["serve_over_plain"],
+            "serve_over_single_box_batched": r["value"] / r["single_box_batched_boxes_per_s"],
+            "plain_boxes_per_s": r["plain_boxes_per_s"],
+            "single_box_batched_boxes_per_s": r["single_box_batched_boxes_per_s"],
+            "one_by_one_sample": r["one_by_one_sample"],
+            "clocks": r["clocks"]}
+    except Exception as e:
+        out["serving"] = {"error": repr(e)}
+    return out
 
 
 def reduce_over_ranks(t_step, e2e_s, interactions, device):
@@ -771,20 +961,29 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="clustered128")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="large384")
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--cpu-sample", default="clustered:48")
+    ap.add_argument("--cpu-sample", default="",
+                    help="KIND:SIDE[:RMS] boxes the CPU leg times (default: per workload)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-targets", action="store_true",
+                    help="large384: skip the sparse-activity and serving target records")
     ap.add_argument("--plain-boxes", type=int, default=24,
                     help="serving workload: boxes timed one by one per form")
     ap.add_argument("--plain-steps", type=int, default=4,
                     help="sparse workload: steps timed in the plain form")
+    ap.add_argument("--row-widen", type=float, default=0.0,
+                    help="with --tuning: the first pass's row bound as a multiple of "
+                         "(gamma h)^2 (0: the library's default)")
+    ap.add_argument("--row-cap", type=int, default=0,
+                    help="with --tuning: items per particle row (0: the library's default)")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default gather configuration")
     ap.add_argument("--integ-side", type=int, default=0,
                     help="integration workload: particles = side^3 (default 384)")
     ap.add_argument("--tuning", default="",
-                    help="JTILE,BLOCK_WARPS[,TPP]: fixed gather configuration, no autotune")
+                    help="JTILE,BLOCK_WARPS[,TPP[,BULK]]: fixed gather configuration, no "
+                         "autotune (BULK 1: j-blocks staged by bulk copies)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -798,6 +997,8 @@ def main():
         return run_integrate(args)
     if WORKLOADS[args.workload][0] == "rebuild":
         return run_rebuild(args)
+    if WORKLOADS[args.workload][0] == "sort":
+        return run_sort(args)
     return run_ours(args)
 
 

@@ -89,6 +89,25 @@ typedef struct {
                                    free HBM); 0: every re-run gathers */
   int32_t block_warps;          /* tile shape: 8 warps x 3 blocks per SM,
                                    or 4 warps x 6 blocks per SM */
+  int32_t bulk_stage;           /* 1: each culled j-block (a contiguous run
+                                   of the store) is fetched into shared
+                                   memory by one bulk copy (the TMA
+                                   engine's cp.async.bulk) instead of one
+                                   load per lane; 0: loads (8-warp tile
+                                   shape, one or two lanes per particle;
+                                   other shapes always load) */
+  float row_widen;              /* the first density pass records each
+                                   particle's candidates within
+                                   sqrt(row_widen) x its search radius
+                                   (capped by its depth_h cell's width)
+                                   for the ghost's re-runs and the force;
+                                   0: the default 1.21; else 1 to 4 */
+  int32_t row_cap;              /* items per particle row (a particle with
+                                   more candidates is gathered instead);
+                                   0: the default 160; else a multiple of
+                                   16 in [64, 512]; the rows are kept only
+                                   while they fit in a quarter of the free
+                                   HBM */
 } sphgpu_tuning;
 
 int sphgpu_abi_version(void);

@@ -51,7 +51,8 @@ class Params(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("threads_per_particle", ctypes.c_int32),
                 ("jtile", ctypes.c_int32), ("rerun_lists", ctypes.c_int32),
-                ("block_warps", ctypes.c_int32)]
+                ("block_warps", ctypes.c_int32), ("bulk_stage", ctypes.c_int32),
+                ("row_widen", ctypes.c_float), ("row_cap", ctypes.c_int32)]
 
 
 class IntegParams(ctypes.Structure):
@@ -319,9 +320,16 @@ class Space:
         return geom, ints
 
     # -- configuration -----------------------------------------------------
-    def set_tuning(self, tpp=1, jtile=16, rerun_lists=1, block_warps=8):
-        t = Tuning(tpp, jtile, rerun_lists, block_warps)
+    def set_tuning(self, tpp=1, jtile=16, rerun_lists=1, block_warps=8, bulk_stage=0,
+                   row_widen=0.0, row_cap=0):
+        t = Tuning(tpp, jtile, rerun_lists, block_warps, bulk_stage, row_widen, row_cap)
         _check(lib().sphgpu_set_tuning(self._h, ctypes.byref(t)))
+
+    def bulk_stage(self):
+        """1 when the gathers stage j-blocks by bulk copies."""
+        t = Tuning()
+        _check(lib().sphgpu_get_tuning(self._h, ctypes.byref(t)))
+        return t.bulk_stage
 
     def tuning(self):
         t = Tuning()

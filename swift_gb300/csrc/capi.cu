@@ -51,7 +51,7 @@ struct sphgpu_space {
   // list solver: [0] particles handed to the catch-up rounds, [r + 1] those
   // catch-up round r sends on
   DBuf<int> catchup;
-  sphgpu_tuning tune{1, SPH_JBLOCK, 1, 8};
+  sphgpu_tuning tune{1, SPH_JBLOCK, 1, 8, 0, 0.f, 0};
 
   // host plans
   Plan plan_d, plan_s, plan_f;
@@ -88,6 +88,7 @@ struct sphgpu_space {
   DBuf<int4> units;              // gather work groups (device-built)
   // neighbour lists of the ghost's re-runs (when they fit in HBM)
   bool lists = false;
+  int rows_cap = 0;  // items per row the rows were allocated with
   DBuf<int> nl, nl_cnt, blk_of;
   DBuf<float> nl_T;
   int max_units = 0;             // 32-particle windows of all leaves
@@ -119,6 +120,7 @@ struct sphgpu_space {
   double phase_ms[3] = {0, 0, 0};
   long long phase_steps = 0;
   DBuf<unsigned long long> hit_ctr;
+  DBuf<int> err;  // set by a kernel that gave up (a bounded wait ran out)
   bool count_hits = false;
   // per-cell sort arrays (sphgpu_hydro_sort)
   DBuf<SortCell> sort_cells;
@@ -187,8 +189,31 @@ void build_plans(sphgpu_space* s) {
 
 void upload_activity(sphgpu_space* s, cudaStream_t st);
 
-// Re-run neighbour lists: at most kListCap items per particle.
+// Re-run neighbour lists: at most kListCap items per particle (the
+// default of sphgpu_tuning::row_cap).
 constexpr int kListCap = 160;
+int row_cap(const sphgpu_space* s);
+
+// The particle rows of the first density pass (row_cap items each), kept
+// only while they fit in a quarter of the free HBM.
+void alloc_rows(sphgpu_space* s, cudaStream_t st) {
+  const int n = s->P.n;
+  s->nl.release();
+  s->nl_cnt.release();
+  s->nl_T.release();
+  s->lists = false;
+  size_t fr = 0, tot = 0;
+  CK(cudaMemGetInfo(&fr, &tot));
+  const size_t bytes = (size_t)n * row_cap(s) * sizeof(int);
+  if (bytes <= fr / 4) {
+    s->nl.alloc((size_t)n * row_cap(s));
+    s->nl_cnt.alloc(n);
+    s->nl_T.alloc(n);
+    CK(cudaMemsetAsync(s->nl_cnt.p, 0xff, sizeof(int) * n, st));  // -1: no list
+    s->lists = true;
+  }
+  s->rows_cap = row_cap(s);
+}
 // The first density pass records each particle's candidates within
 // sqrt(kListWiden) its search radius (capped by its depth_h cell's width), so
 // that the ghost's re-runs -- Newton's first step moves h by less than 10 %
@@ -331,18 +356,9 @@ void ensure_device(sphgpu_space* s) {
   s->redo.alloc(std::max(1, s->prm.max_iter));
   s->catchup.alloc(s->prm.max_iter + 1);
   s->hit_ctr.alloc(4);
-  {
-    size_t fr = 0, tot = 0;
-    CK(cudaMemGetInfo(&fr, &tot));
-    const size_t bytes = (size_t)n * kListCap * sizeof(int);
-    if (bytes <= fr / 4) {
-      s->nl.alloc((size_t)n * kListCap);
-      s->nl_cnt.alloc(n);
-      s->nl_T.alloc(n);
-      CK(cudaMemsetAsync(s->nl_cnt.p, 0xff, sizeof(int) * n, st));  // -1: no list
-      s->lists = true;
-    }
-  }
+  s->err.alloc(1);
+  CK(cudaMemsetAsync(s->err.p, 0, sizeof(int), st));
+  alloc_rows(s, st);
   for (auto& e : s->ev) CK(cudaEventCreate(&e));
   CK(cudaMemsetAsync(s->fin0.p, 0, sizeof(float4) * n, st));
   CK(cudaMemsetAsync(s->fin1.p, 0, sizeof(float2) * n, st));
@@ -424,6 +440,8 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   a.force_rows = 0;
   a.nl_seg = 1;
   a.blk_of = s->blk_of.p;
+  a.bulk = s->tune.bulk_stage;
+  a.err = s->err.p;
   return a;
 }
 
@@ -460,15 +478,16 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
     a.nl = s->nl.p;
     a.nl_cnt = s->nl_cnt.p;
     a.nl_T = s->nl_T.p;
-    a.nl_cap = kListCap;
-    if (mode == MODE_FIRST) a.nl_widen = kListWiden;
+    a.nl_cap = row_cap(s);
+    if (mode == MODE_FIRST)
+      a.nl_widen = s->tune.row_widen > 0.f ? s->tune.row_widen : kListWiden;
   }
   if (force && force_rows) {
     // the force reads the rows the first pass recorded this step
     a.nl = s->nl.p;
     a.nl_cnt = s->nl_cnt.p;
     a.nl_T = s->nl_T.p;
-    a.nl_cap = kListCap;
+    a.nl_cap = row_cap(s);
     a.nl_seg = rec_tpp(s);
     a.force_rows = 1;
   }
@@ -481,7 +500,7 @@ ListArgs largs(sphgpu_space* s, const int* gate) {
   l.nl = s->nl.p;
   l.nl_cnt = s->nl_cnt.p;
   l.nl_T = s->nl_T.p;
-  l.nl_cap = kListCap;
+  l.nl_cap = row_cap(s);
   l.nl_seg = rec_tpp(s);
   l.leaf_pair_begin = s->dplan_s.lpb.p;
   l.pair_block = s->dplan_s.pb.p;
@@ -518,6 +537,7 @@ GhostArgs ghargs(sphgpu_space* s, int iter, int lo, int hi) {
 // (subset gather lists); both kernels return at once when the previous
 // round sent none (gates on the redo counts).
 bool lists_on(const sphgpu_space* s) { return s->lists && s->tune.rerun_lists; }
+int row_cap(const sphgpu_space* s) { return s->tune.row_cap > 0 ? s->tune.row_cap : kListCap; }
 
 // The step graph holds the first kGraphRounds ghost rounds (h converges in
 // 2-4 for almost every particle); the rare later ones run outside it, only
@@ -568,10 +588,16 @@ void enqueue_force(sphgpu_space* s, cudaStream_t st) {
 }
 
 int check_conv(sphgpu_space* s, cudaStream_t st) {
-  int last = 0;
+  int last = 0, err = 0;
   CK(cudaMemcpyAsync(&last, s->redo.p + s->prm.max_iter - 1, sizeof(int),
                      cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&err, s->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  if (err) {
+    CK(cudaMemsetAsync(s->err.p, 0, sizeof(int), st));
+    return fail(SPHGPU_ECUDA, "a gather gave up waiting for a bulk copy of a j-block; "
+                              "the step's results are incomplete");
+  }
   if (last > 0)
     return fail(SPHGPU_ENOCONV, "smoothing length failed to converge on " +
                                     std::to_string(last) + " particles");
@@ -798,15 +824,21 @@ int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
   if (!(t->threads_per_particle == 1 || t->threads_per_particle == 2 ||
         t->threads_per_particle == 4) ||
       !(t->jtile == 8 || t->jtile == 16 || t->jtile == 32) ||
-      !(t->block_warps == 4 || t->block_warps == 8))
+      !(t->block_warps == 4 || t->block_warps == 8) ||
+      !(t->bulk_stage == 0 || t->bulk_stage == 1) ||
+      !(t->row_widen == 0.f || (t->row_widen >= 1.f && t->row_widen <= 4.f)) ||
+      !(t->row_cap == 0 || (t->row_cap >= 64 && t->row_cap <= 512 && t->row_cap % 16 == 0)))
     return fail(SPHGPU_EINVAL,
-                "tuning: threads_per_particle 1, 2 or 4, jtile 8, 16 or 32, block_warps 4 or 8");
+                "tuning: threads_per_particle 1, 2 or 4, jtile 8, 16 or 32, block_warps 4 or 8, "
+                "bulk_stage 0 or 1, row_widen 0 or in [1, 4], row_cap 0 or a multiple of 16 "
+                "in [64, 512]");
   return guard([&]() {
     if (s->dev) CK(cudaStreamSynchronize(s->stream));
     const bool reblock = t->jtile != s->tune.jtile;
     s->tune = *t;
     s->tune.rerun_lists = t->rerun_lists ? 1 : 0;
     drop_graph(s);
+    if (s->dev && row_cap(s) != s->rows_cap) alloc_rows(s, s->stream);
     if (reblock) {
       // blocks, candidate lists and every plan referring to them change
       s->space->set_jblock(t->jtile);
@@ -1347,7 +1379,8 @@ int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms
   // j-tile outermost: only a new j-tile re-plans the blocks
   for (int a = 0; a < 3; a++)
     for (int c = 0; c < 4; c++, k++) {
-      sphgpu_tuning t{1 + (c >> 1), jt[a], s->tune.rerun_lists, bw[c & 1]};
+      sphgpu_tuning t{1 + (c >> 1), jt[a], s->tune.rerun_lists, bw[c & 1],
+                      s->tune.bulk_stage, s->tune.row_widen, s->tune.row_cap};
       int rc = sphgpu_set_tuning(s, &t);
       if (rc) return rc;
       rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);  // plan + capture + warm

@@ -197,7 +197,7 @@ int row_cap(const sphgpu_space* s);
 // The particle rows of the first density pass (row_cap items each), kept
 // only while they fit in a quarter of the free HBM.
 void alloc_rows(sphgpu_space* s, cudaStream_t st) {
-  const int n = s->P.n;
+  const int n = s->space->n();  // (s->P is not filled in yet on the first call)
   s->nl.release();
   s->nl_cnt.release();
   s->nl_T.release();

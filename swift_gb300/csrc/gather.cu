@@ -110,7 +110,10 @@ cudaError_t launch_solve_from_lists(const ListArgs& a, const GhostArgs& g, int m
   long long grid = ((long long)a.p.n * 4 + 255) / 256;  // four lanes per particle
   const long long cap = 16LL * sm_count();
   grid = grid < 1 ? 1 : (grid > cap ? cap : grid);
-  solve_from_lists<<<(int)grid, 256, 0, s>>>(a, g, max_iter);
+  if (a.leaf_tw)
+    solve_from_lists<true><<<(int)grid, 256, 0, s>>>(a, g, max_iter);
+  else
+    solve_from_lists<false><<<(int)grid, 256, 0, s>>>(a, g, max_iter);
   return cudaGetLastError();
 }
 

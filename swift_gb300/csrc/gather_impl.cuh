@@ -820,6 +820,8 @@ static __device__ const Entry* rerun_entry(const ListArgs& a, int leaf, int b, i
 // whose h_k is beyond its list stops there and is handed to the catch-up
 // rounds (gathers; *a.handover counts them).  Same sums, same updates, in
 // the same order as the rounds one at a time.
+// ARENA: boxes of different sizes share the store (ListArgs::leaf_tw).
+template <bool ARENA = false>
 static __global__ void __launch_bounds__(256, 4)
     solve_from_lists(ListArgs a, GhostArgs g, int max_iter) {
   constexpr int LPP = 4;
@@ -848,6 +850,13 @@ static __global__ void __launch_bounds__(256, 4)
       }
     }
     const int* row = a.nl + (size_t)(i < P.n ? i : 0) * a.nl_cap;
+    // boxes of different sizes in one store (the serving arena): the frame
+    // offsets come from the particle's own top-cell width
+    float3 twi = a.top_width;
+    if (ARENA && i < P.n) {
+      const float4 t = a.leaf_tw[P.leaf_of[i]];
+      twi = make_float3(t.x, t.y, t.z);
+    }
     for (int it = 1; it < max_iter && __any_sync(FULL, going); it++) {
       float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f, s5 = 0.f, s6 = 0.f, s7 = 0.f;
       int ngb = 0;
@@ -881,7 +890,13 @@ static __global__ void __launch_bounds__(256, 4)
             float dxs[3], dys[3], dzs[3], r2s[3];
 #pragma unroll
             for (int u = 0; u < 3; u++) {
-              const float4 fd = ftab[(unsigned)pk[u] >> 27];
+              float4 fd;
+              if (ARENA) {
+                const float3 o = offset_of((unsigned)pk[u] >> 27, twi);
+                fd = make_float4(o.x, o.y, o.z, 0.f);
+              } else {
+                fd = ftab[(unsigned)pk[u] >> 27];
+              }
               dxs[u] = pi.x - (q[u].x + fd.x);
               dys[u] = pi.y - (q[u].y + fd.y);
               dzs[u] = pi.z - (q[u].z + fd.z);

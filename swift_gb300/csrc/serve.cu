@@ -12,11 +12,17 @@
 // when the server starts, so admission is admission by free HBM.
 //
 // One pump advances every resident box by one step: one begin-step kernel,
-// one density gather over the windows of all boxes, the ghost rounds (each a
-// ghost kernel and a gated re-run gather over all boxes), one force gather.  Every index a box's lists hold is rebased to its
-// arena ranges when it is uploaded, and the gather takes the top-cell width
-// per leaf, so boxes of different sizes share a launch and never see each
-// other's particles.  A box joining in the middle of the stream has its force
+// one density gather over the windows of all boxes that also records every
+// particle's row of candidates, ghost round 0, the per-particle ghost solver
+// over the rows with gated catch-up rounds (a re-run gather and a round
+// update) for the particles whose h outgrew their row, one force gather that
+// takes a group's partners from the rows where they cover them -- the
+// single-space path's kernels and configuration (when the rows do not fit
+// beside the arena, the ghost rounds re-run by gathers instead).  Every
+// index a box's lists hold is rebased to its arena ranges when it is
+// uploaded, and the gathers and the solver take the top-cell width per leaf,
+// so boxes of different sizes share a launch and never see each other's
+// particles.  A box joining in the middle of the stream has its force
 // lists planned after its first ghost (the recursion reads the post-ghost
 // h_max), inside the pump that runs its first step.  Finished boxes are read
 // back and their ranges freed for the next admissions.
@@ -114,6 +120,7 @@ struct Job {
   std::vector<int> lwb;
   std::vector<LeafInfo> li;
   std::vector<int2> bfc;
+  std::vector<int32_t> bo;  // j-block of every store particle
   int nleaves = 0, nwin = 0, nblk = 0, ntop = 0;
   float4 tw{0.f, 0.f, 0.f, 0.f};
   std::string err;
@@ -208,6 +215,9 @@ void plan_job(Job& j) {
     j.bhi[b] = make_float4(jb.hi[3 * b], jb.hi[3 * b + 1], jb.hi[3 * b + 2], 0.f);
     j.bfc[b] = make_int2(jb.first[b], jb.count[b]);
   }
+  j.bo.assign(n, 0);
+  for (int b = 0; b < j.nblk; b++)
+    for (int k = jb.first[b]; k < jb.first[b] + jb.count[b]; k++) j.bo[k] = b;
   const double* wd = sp.width();
   j.tw = make_float4((float)wd[0], (float)wd[1], (float)wd[2], 0.f);
   // Host copies of the inputs are no longer needed.
@@ -218,6 +228,10 @@ void plan_job(Job& j) {
 }
 
 constexpr float kServeBand = 2.44140625e-4f;  // 2^-12, as the single-space path
+// Rows of the first density pass, as the single-space path's defaults: at
+// most kRowCap candidates per particle, within sqrt(kRowWiden) x its radius.
+constexpr int kRowCap = 160;
+constexpr float kRowWiden = 1.21f;
 
 }  // namespace
 
@@ -242,6 +256,11 @@ struct sphgpu_server {
   DBuf<Entry> ent[3];
   DBuf<int> pblk[3], pent[3], lpb[3];
   DBuf<int> queue, redo;
+  // rows of the first density pass (the ghost's per-particle solver and the
+  // force read them), on when they fit with the arena
+  bool rows = false;
+  DBuf<int> nl, nl_cnt, blk_of, catchup;
+  DBuf<float> nl_T;
   DBuf<float> stage_f;
   DBuf<int32_t> stage_i;
   DevParticles P{};
@@ -490,6 +509,12 @@ struct sphgpu_server {
     if (j.nwin) CK(cudaMemsetAsync(units.p + r.w0, 0, sizeof(int4) * j.nwin, st));
     std::vector<int2> bfc(j.bfc);
     for (auto& b : bfc) b.x += (int)p0;
+    if (rows) {
+      std::vector<int32_t> bo(j.bo);
+      for (auto& b : bo) b += (int32_t)r.b0;
+      CK(cudaMemcpyAsync(blk_of.p + p0, bo.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+      CK(cudaMemsetAsync(nl_cnt.p + p0, 0xff, sizeof(int) * n, st));  // -1: no row yet
+    }
     if (j.nblk) {
       CK(cudaMemcpyAsync(bb_lo.p + r.b0, j.blo.data(), sizeof(float4) * j.nblk, cudaMemcpyHostToDevice, st));
       CK(cudaMemcpyAsync(bb_hi.p + r.b0, j.bhi.data(), sizeof(float4) * j.nblk, cudaMemcpyHostToDevice, st));
@@ -555,18 +580,56 @@ struct sphgpu_server {
     a.gate = gate;
     a.band = kServeBand;
     a.mode = mode;
-    a.nl = nullptr;  // no re-run lists in the arena
+    a.nl = nullptr;
     a.nl_cnt = nullptr;
     a.nl_T = nullptr;
     a.nl_cap = 0;
+    a.leaves = leaves.p;
+    a.blk_of = blk_of.p;
     return a;
   }
 
-  void gather(int k, int qslot, int mode, bool force, int need, const int* gate) {
+  // lists: the first pass records the rows; force_rows: the force reads
+  // them where they cover a group's partners
+  void gather(int k, int qslot, int mode, bool force, int need, const int* gate,
+              bool lists = false, bool force_rows = false) {
     CK(cudaMemsetAsync(queue.p + qslot, 0, sizeof(int), st));
     CK(launch_build_units(leaves.p, (int)hwL, lwb.p, flags.p, need, 0, lpb[k].p, units.p, gate,
                           st));
-    CK(launch_gather(gargs(k, qslot, mode, gate), force, num_sms, (int)hwW, st, 8));
+    G2Args a = gargs(k, qslot, mode, gate);
+    if (lists || force_rows) {
+      a.nl = nl.p;
+      a.nl_cnt = nl_cnt.p;
+      a.nl_T = nl_T.p;
+      a.nl_cap = kRowCap;
+      a.nl_seg = 1;
+    }
+    if (lists) a.nl_widen = kRowWiden;
+    if (force_rows) a.force_rows = 1;
+    CK(launch_gather(a, force, num_sms, (int)hwW, st, 8, lists, 1));
+  }
+
+  ListArgs largs() {
+    ListArgs l;
+    l.p = P;
+    l.p.n = (int)hwP;
+    l.nl = nl.p;
+    l.nl_cnt = nl_cnt.p;
+    l.nl_T = nl_T.p;
+    l.nl_cap = kRowCap;
+    l.nl_seg = 1;
+    l.leaf_pair_begin = lpb[1].p;
+    l.pair_block = pblk[1].p;
+    l.pair_entry = pent[1].p;
+    l.entries = ent[1].p;
+    l.blk_of = blk_of.p;
+    l.top_width = make_float3(1.f, 1.f, 1.f);
+    l.leaf_tw = leaf_tw.p;
+    l.band = kServeBand;
+    l.gate = redo.p;
+    l.hits = nullptr;
+    l.handover = catchup.p;
+    return l;
   }
 
   GhostArgs ghargs(int iter) {
@@ -673,10 +736,24 @@ struct sphgpu_server {
     }
     CK(cudaEventRecord(ev[0], st));
     CK(launch_begin_step(view(0, (int)hwP), phys.max_iter, redo.p, phys.h_max, st));
-    gather(0, 0, MODE_FIRST, false, 1, nullptr);
-    for (int k = 0; k < phys.max_iter; k++) {
-      CK(launch_ghost(ghargs(k), st));
-      gather(1, 1, MODE_REDO, false, 3, redo.p + k);
+    gather(0, 0, MODE_FIRST, false, 1, nullptr, rows);
+    if (rows) {
+      // as the single-space path with rows: round 0, then every particle
+      // iterates on its own from its row; those whose h outgrew it catch up
+      // by gathers, each at its own round count
+      CK(launch_ghost(ghargs(0), st));
+      CK(cudaMemsetAsync(catchup.p, 0, sizeof(int) * (phys.max_iter + 1), st));
+      CK(launch_solve_from_lists(largs(), ghargs(1), phys.max_iter, st));
+      for (int r = 0; r < phys.max_iter; r++) {
+        gather(1, 1, MODE_REDO, false, 3, catchup.p + r);
+        CK(launch_ghost_catchup(ghargs(0), phys.max_iter, catchup.p + r, catchup.p + r + 1,
+                                st));
+      }
+    } else {
+      for (int k = 0; k < phys.max_iter; k++) {
+        CK(launch_ghost(ghargs(k), st));
+        gather(1, 1, MODE_REDO, false, 3, redo.p + k);
+      }
     }
     int last = 0;
     CK(cudaMemcpyAsync(&last, redo.p + phys.max_iter - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -707,7 +784,7 @@ struct sphgpu_server {
     }
     CK(cudaEventRecord(ev[2], st));
     CK(launch_block_hmax(bb_fc.p, bb_lo.p, posh.p, (int)hwB, st));
-    gather(2, 2, MODE_FIRST, true, 1, nullptr);  // writes the finished sums
+    gather(2, 2, MODE_FIRST, true, 1, nullptr, false, rows);  // writes the finished sums
     CK(cudaEventRecord(ev[3], st));
     CK(cudaStreamSynchronize(st));
     if (!to_workers.empty()) {
@@ -777,14 +854,20 @@ int sphgpu_server_create(const sphgpu_params* prm, int64_t max_particles,
     const double per_particle = 8 * 3 + 16 * 7 + 8 * 2 + 4 * 4 + 3 + 4 * 7 +
                                 (sizeof(LeafInfo) + 16 + 4 * 4) / 4.0 + 16 / 8.0 +
                                 36 / 8.0 + 24 / 2.0 + 3 * (sizeof(Entry) / 2.0 + 8 * 4.0);
+    // the rows of the first density pass and the j-block of every slot
+    const double per_particle_rows = 4.0 * kRowCap + 4 + 4 + 4;
     int64_t cap = max_particles;
     const int64_t afford = (int64_t)(0.5 * (double)fr / per_particle);
+    // rows while the arena with them still fits in half the free HBM
+    const int64_t afford_rows =
+        (int64_t)(0.5 * (double)fr / (per_particle + per_particle_rows));
     if (cap == 0) cap = std::min<int64_t>(afford, (int64_t)1 << 24);
     if (cap > afford)
       return fail(SPHGPU_ENOMEM, "sphgpu_server_create: arena larger than half the free HBM");
     if (cap > ((int64_t)1 << 26))  // partner indices are packed in 27 bits
       return fail(SPHGPU_EINVAL, "sphgpu_server_create: at most 2^26 particles");
     if (cap < 4096) cap = 4096;
+    s->rows = cap <= afford_rows;
     const int64_t capL = cap / 4 + 1024, capW = cap / 32 + capL, capB = cap / 8 + capL,
                   capT = cap / 2 + 1728, capE = cap / 2 + 64 * 1024, capQ = 4 * cap;
     s->rP.init(cap);
@@ -835,6 +918,15 @@ int sphgpu_server_create(const sphgpu_params* prm, int64_t max_particles,
     }
     s->queue.alloc(16);
     s->redo.alloc(std::max(1, P.max_iter));
+    s->catchup.alloc(P.max_iter + 1);
+    if (s->rows) {
+      s->nl.alloc((size_t)cap * kRowCap);
+      s->nl_cnt.alloc(cap);
+      s->nl_T.alloc(cap);
+      s->blk_of.alloc(cap);
+    } else {
+      s->blk_of.alloc(1);
+    }
     cudaStream_t st = s->st;
     CK(cudaMemsetAsync(s->flags.p, 0, cap, st));
     CK(cudaMemsetAsync(s->leaves.p, 0, sizeof(LeafInfo) * capL, st));

@@ -116,6 +116,8 @@ struct ListArgs {
   const int* gate;              // do nothing when *gate == 0
   unsigned long long* hits;     // optional: total neighbour hits
   int* handover;                // solver: particles left to the catch-up rounds
+  const float4* leaf_tw = nullptr;  // per leaf top-cell width (boxes of different
+                                    // sizes in one store), else top_width
 };
 
 struct GhostArgs {

@@ -98,7 +98,9 @@ def test_server_matches_single_space_and_oracle(oracle_lib):
         srv.submit(7, box, nsteps=3)
         out = _run_until_done(srv, [7])[7]
     with api.Space(box) as sp:
-        sp.set_tuning(jtile=16, rerun_lists=0, block_warps=8)  # the arena's configuration
+        # the arena's configuration: j-blocks of 16, one lane per particle,
+        # 8 warps per block, rows of the first pass for the ghost and force
+        sp.set_tuning(jtile=16, rerun_lists=1, block_warps=8)
         sp.step()
         one = sp.download()
     # the same lists and kernels as the single-box batched form

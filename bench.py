@@ -277,10 +277,13 @@ def traffic_from_profile(kernel, workload, tuning):
     """DRAM bytes per launch of a gather (kernel "density_gather" or
     "force_gather") from the committed ncu summary of this workload: the
     capture made with the same j-block depth and lanes per particle (lines
-    "traffic_bytes_per_launch: N (...) — jtile J, threads_per_particle T")."""
+    "traffic_bytes_per_launch: N (...) — jtile J, threads_per_particle T,
+    row_widen W")."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    rw = float(tuning.get("row_widen") or 1.21)
     want = (f"jtile {tuning.get('jtile')}",
-            f"threads_per_particle {tuning.get('threads_per_particle', 1)}")
+            f"threads_per_particle {tuning.get('threads_per_particle', 1)}",
+            f"row_widen {rw:g}")
     try:
         with open(path) as f:
             for line in f:

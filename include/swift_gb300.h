@@ -166,7 +166,8 @@ int sphgpu_get_tuning(const sphgpu_space *s, sphgpu_tuning *t);
  * (j-block depth x lanes per particle x tile shape), keeps the fastest and
  * returns it in *best; ms[k] receives the mean step time of candidate k (up
  * to 16 candidates, order: jtile 32/16/8 x threads_per_particle 1/2 x
- * block_warps 8/4), *ncand their number. */
+ * block_warps 8/4, then -- when the rows are on -- the fastest of those with
+ * row_widen 1.32, 1.44, 1.56, 1.69), *ncand their number. */
 int sphgpu_autotune(sphgpu_space *s, int32_t reps, sphgpu_tuning *best,
                     float ms[16], int32_t *ncand);
 

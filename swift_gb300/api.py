@@ -361,12 +361,15 @@ class Space:
         n = ctypes.c_int32()
         _check(lib().sphgpu_autotune(self._h, int(reps), ctypes.byref(best),
                                      _ptr(ms), ctypes.byref(n)))
-        cands = [(jt, tpp, bw) for jt in (32, 16, 8) for tpp in (1, 2) for bw in (8, 4)]
-        table = {tuning_key(jt, tpp, bw): float(ms[k])
-                 for k, (jt, tpp, bw) in enumerate(cands[:n.value])}
+        cands = [tuning_key(jt, tpp, bw) for jt in (32, 16, 8) for tpp in (1, 2)
+                 for bw in (8, 4)]
+        shape = tuning_key(best.jtile, best.threads_per_particle, best.block_warps)
+        cands += [f"{shape},row_widen={w}" for w in (1.32, 1.44, 1.56, 1.69)]
+        table = {name: float(ms[k]) for k, name in enumerate(cands[:n.value])}
         return ({"threads_per_particle": best.threads_per_particle,
                  "jtile": best.jtile, "rerun_lists": best.rerun_lists,
-                 "block_warps": best.block_warps}, table)
+                 "block_warps": best.block_warps,
+                 "row_widen": round(float(best.row_widen), 4)}, table)
 
     def set_active(self, max_active_bin):
         _check(lib().sphgpu_set_active(self._h, int(max_active_bin)))

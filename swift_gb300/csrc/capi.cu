@@ -90,6 +90,7 @@ struct sphgpu_space {
   bool lists = false;
   int rows_cap = 0;  // items per row the rows were allocated with
   DBuf<int> nl, nl_cnt, blk_of;
+  DBuf<float4> sb_lo, sb_hi;  // sub-boxes of the j-blocks (4 per block)
   DBuf<float> nl_T;
   int max_units = 0;             // 32-particle windows of all leaves
   DBuf<int> leaf_window_begin;   // per leaf: its first window
@@ -234,6 +235,13 @@ void upload_blocks(sphgpu_space* s, cudaStream_t st) {
   s->bb_lo.upload(blo.data(), nb, st);
   s->bb_hi.upload(bhi.data(), nb, st);
   s->bb_fc.upload(bfc.data(), nb, st);
+  std::vector<float4> slo(4 * nb), shi(4 * nb);
+  for (size_t q = 0; q < 4 * nb; q++) {
+    slo[q] = make_float4(jb.sub_lo[3 * q], jb.sub_lo[3 * q + 1], jb.sub_lo[3 * q + 2], 0.f);
+    shi[q] = make_float4(jb.sub_hi[3 * q], jb.sub_hi[3 * q + 1], jb.sub_hi[3 * q + 2], 0.f);
+  }
+  s->sb_lo.upload(slo.data(), 4 * nb, st);
+  s->sb_hi.upload(shi.data(), 4 * nb, st);
   s->bb_n = (int)nb;
   std::vector<int> bo(s->space->n());
   for (size_t b = 0; b < nb; b++)
@@ -442,6 +450,8 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   a.blk_of = s->blk_of.p;
   a.bulk = s->tune.bulk_stage;
   a.err = s->err.p;
+  a.sb_lo = s->sb_lo.p;
+  a.sb_hi = s->sb_hi.p;
   return a;
 }
 
@@ -1399,6 +1409,34 @@ int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms
         bt = t;
       }
     }
+  // then the rows' radius for the chosen shape: wider rows cover more of the
+  // ghost's iterates and of the force's partners on boxes where h moves far
+  // from its input, at the price of recording and reading more items
+  if (s->lists && s->tune.rerun_lists) {
+    const float widen[4] = {1.32f, 1.44f, 1.56f, 1.69f};
+    const sphgpu_tuning shape = bt;
+    for (int w = 0; w < 4 && k < 16; w++, k++) {
+      sphgpu_tuning t = shape;
+      t.row_widen = widen[w];
+      int rc = sphgpu_set_tuning(s, &t);
+      if (rc) return rc;
+      rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);
+      if (rc) return rc;
+      double sum[3];
+      int64_t n = 0;
+      sphgpu_phase_times(s, sum, &n, 1);
+      for (int r = 0; r < reps; r++) {
+        rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);
+        if (rc) return rc;
+      }
+      sphgpu_phase_times(s, sum, &n, 1);
+      ms[k] = (float)((sum[0] + sum[1] + sum[2]) / std::max<int64_t>(1, n));
+      if (ms[k] < best_ms) {
+        best_ms = ms[k];
+        bt = t;
+      }
+    }
+  }
   *ncand = k;
   const int rc = sphgpu_set_tuning(s, &bt);
   if (rc) return rc;

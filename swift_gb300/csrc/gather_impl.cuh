@@ -114,7 +114,8 @@ struct LaneSmem {
   int sfirst[32];      // surviving candidate blocks of the current chunk
   int scount[32];
   int se[32];
-  int sdep[32];        // their entries' depth window: min | max << 8
+  int sdep[32];        // their entries' depth window: min | max << 8, and the
+                       // runs of 8 the group can reach << 16
   float4 sf[32];       // their frame offsets (w: frame-offset index)
   float4 slo[32];      // their boxes
   float4 shi[32];
@@ -534,6 +535,22 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
           const int ix = (int)rintf(fd.x / tw.x) + 1, iy = (int)rintf(fd.y / tw.y) + 1,
                     iz = (int)rintf(fd.z / tw.z) + 1;
           fd.w = __int_as_float(ix + 3 * iy + 9 * iz);
+          // the block's runs of 8 particles the group's box can reach (bits
+          // 16-19 of the depth word); the force's radius depends on each
+          // partner's h, so it tests every run
+          unsigned runs = 0xfu;
+          if (!FORCE && a.sb_lo) {
+            runs = 0u;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const float4 sl = a.sb_lo[4 * b + q], sh = a.sb_hi[4 * b + q];
+              const float ex = fmaxf(fmaxf(sl.x + fd.x - gx1, gx0 - sh.x - fd.x), 0.f);
+              const float ey = fmaxf(fmaxf(sl.y + fd.y - gy1, gy0 - sh.y - fd.y), 0.f);
+              const float ez = fmaxf(fmaxf(sl.z + fd.z - gz1, gz0 - sh.z - fd.z), 0.f);
+              if (ex * ex + ey * ey + ez * ez < R2 * (1.f + 4.f * band) + 1e-30f) runs |= 1u << q;
+            }
+          }
+          dep |= (int)(runs << 16);
         }
       }
       const unsigned mask = __ballot_sync(FULL, ov);
@@ -591,7 +608,7 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         // does this lane's own sphere reach the block, and may it use the
         // entry (depth filter)?
         bool mine = false;
-        if (valid && dh >= (sdep & 0xff) && dh <= (sdep >> 8)) {
+        if (valid && dh >= (sdep & 0xff) && dh <= ((sdep >> 8) & 0xff)) {
           const float px = pi.x - sfd.x, py = pi.y - sfd.y, pz = pi.z - sfd.z;
           const float dx = fmaxf(fmaxf(slo.x - px, px - shi.x), 0.f);
           const float dy = fmaxf(fmaxf(slo.y - py, py - shi.y), 0.f);
@@ -622,7 +639,11 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
         // candidates are decided by the exact FP64 predicate in the reference
         // frame (rare: the warp votes once per chunk).
         auto cidx = [&](int t0, int u) { return t0 + 2 * TPP * (u >> 1) + 2 * sub + (u & 1); };
+        const unsigned runs = (unsigned)sdep >> 16;
         for (int t0 = 0; t0 < bcount; t0 += 8 * TPP) {
+          // candidates t0 .. t0 + 8 TPP - 1 are the block's runs t0 / 8 ..;
+          // none of them within any lane's reach: nothing to test
+          if (!((runs >> (t0 >> 3)) & ((1u << TPP) - 1u))) continue;
           unsigned hm = 0u, cm = 0u, wm = 0u;
 #pragma unroll
           for (int v = 0; v < 4; v++) {

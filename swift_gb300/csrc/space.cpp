@@ -432,6 +432,22 @@ void Space::build_gpu_order() {
         jb_.lo.push_back(lo[d]);
         jb_.hi.push_back(hi[d]);
       }
+      for (int q = 0; q < 4; q++) {
+        float sl[3] = {3.4e38f, 3.4e38f, 3.4e38f}, sh[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+        const int k0 = b0 + q * kSubBlock, k1 = std::min(b0 + bc, k0 + kSubBlock);
+        for (int k = k0; k < k1; k++) {
+          const double* x = &x_[3 * (size_t)gperm_[k]];
+          for (int d = 0; d < 3; d++) {
+            const float o = (float)(x[d] - top.loc[d]);
+            sl[d] = std::min(sl[d], o);
+            sh[d] = std::max(sh[d], o);
+          }
+        }
+        for (int d = 0; d < 3; d++) {
+          jb_.sub_lo.push_back(sl[d]);
+          jb_.sub_hi.push_back(sh[d]);
+        }
+      }
     }
   }
   leaf_block_begin[leaves_.size()] = (int)jb_.first.size();

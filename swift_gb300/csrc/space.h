@@ -51,9 +51,14 @@ struct Plan {
   std::vector<int> leaf_pair_begin;
 };
 
+constexpr int kSubBlock = 8;  // particles per sub-box of a j-block (4 per block of 32)
+
 struct JBlocks {
   std::vector<int32_t> first, count;   // particle range (GPU order)
   std::vector<float> lo, hi;           // [3 * nblocks] bounding box, top frame
+  // [4 * 3 * nblocks] boxes of the block's runs of 8 particles (kSubBlock);
+  // a run past the block's end is empty (lo > hi)
+  std::vector<float> sub_lo, sub_hi;
   std::vector<int32_t> cell_begin, cell_end;  // per cell: block range
 };
 

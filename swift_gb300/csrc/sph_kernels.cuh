@@ -92,6 +92,10 @@ struct G2Args {
   // wait that runs out sets *err (the host reports it) and ends the warp
   int bulk = 0;
   int* err = nullptr;
+  // density gathers: the boxes of each j-block's runs of 8 particles (4 per
+  // block); a run no particle of the group can reach is not tested
+  const float4* sb_lo = nullptr;
+  const float4* sb_hi = nullptr;
 };
 
 // Later re-runs from the lists: particles whose list covers their new

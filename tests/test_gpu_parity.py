@@ -226,9 +226,12 @@ def test_autotune_picks_a_candidate():
     with api.Space(box) as sp:
         sp.step()
         best, table = sp.autotune(reps=1)
-        assert len(table) == 12 and all(v > 0 for v in table.values())
+        # 12 tile shapes, then 4 row radii for the fastest shape
+        assert len(table) == 16 and all(v > 0 for v in table.values())
         key = api.tuning_key(best["jtile"], best["threads_per_particle"],
                              best["block_warps"])
+        if best["row_widen"] > 0:
+            key += f",row_widen={best['row_widen']:g}"
         assert table[key] == min(table.values())
         assert sp.tuning()[1] == best["jtile"]
         sp.step()

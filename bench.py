@@ -334,10 +334,14 @@ def sparse_record(workload, steps, warmup, plain_steps, seed):
         one(b, False)
     sp.phase_times(reset=True)
     sp.host_times(reset=True)
+    sp.step_stats(reset=True)
     clocks = ClockSampler(local_rank)
     t_b, inter = [], []
+    graphs = {"graph_steps": 0, "force_replans": 0, "late_rounds": 0, "captures": 0}
     for b in seq[warmup:]:
         t_b.append(one(b, False))
+        for k, v in sp.step_stats(reset=True).items():
+            graphs[k] += v
         hits = sp.count_hits()  # untimed replay of the same step, instrumented
         inter.append(int(hits[3]) + int(hits[2]))
     clk = clocks.stop()
@@ -370,6 +374,7 @@ def sparse_record(workload, steps, warmup, plain_steps, seed):
         "batched_ms_per_step": [round(1e3 * t, 3) for t in t_b],
         "plain_ms_per_step": [round(1e3 * t, 3) for t in t_p],
         "plain_over_batched": ms_p / ms_p_same,
+        "step_graphs": graphs,
         "interactions_per_step": inter,
         "clocks": clk,
     }
@@ -754,6 +759,7 @@ def run_ours(args):
     hits = sp.count_hits()
     inter_per_step = int(hits[3]) + int(hits[2])
     sp.phase_times(reset=True)
+    sp.step_stats(reset=True)
 
     def barrier():
         torch.cuda.synchronize()
@@ -773,6 +779,7 @@ def run_ours(args):
     ms_total = e0.elapsed_time(e1)
     clk = clocks.stop()
     phase_ms, nsteps = sp.phase_times(reset=True)
+    step_graphs = sp.step_stats(reset=True)
 
     # End to end through host buffers (pinned), same step.
     pinned = {}
@@ -891,7 +898,11 @@ def run_ours(args):
             # graph (ghost, units, gather; gated) -- with the lists ghost round 0
             # and the per-particle solver come first and the 8 rounds are
             # catch-up rounds -- force (h_max, units, gather)
-            "gpu_launches": (6 + 8 * 3 + (2 if tuning.get("rerun_lists") else 0)) * args.steps,
+            "gpu_launches": (7 + 8 * 3 + (2 if tuning.get("rerun_lists") else 0)) * args.steps,
+            # each timed step one CUDA graph (density, ghost rounds, the force
+            # plan's check, force); re-plans and late rounds count the rare
+            # steps that finished outside it
+            "step_graphs": step_graphs,
             "clocks": clk,
             "cpu_baseline": cb,
             "targets": targets,
@@ -921,6 +932,7 @@ def run_targets(args):
             "host_ms_per_step": r["host_ms_per_step"],
             "phases_ms_gpu": r["phases_ms_gpu"],
             "active_fraction": r["config"]["active_fraction"],
+            "step_graphs": r["step_graphs"],
             "clocks": r["clocks"]}
     except Exception as e:  # recorded, not fatal to the headline line
         out["batched_over_plain"] = {"error": repr(e)}

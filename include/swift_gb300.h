@@ -178,6 +178,14 @@ int sphgpu_autotune(sphgpu_space *s, int32_t reps, sphgpu_tuning *best,
  * SPHGPU_ENOCONV if some h did not converge in max_iter rounds. */
 int sphgpu_step(sphgpu_space *s, int32_t stages, void *stream);
 
+/* Steps of the batched form since the last reset: out[0] steps run as one
+ * CUDA graph (density, ghost rounds, the force plan's check, force), out[1]
+ * of them whose force lists -- planned before the step from each active
+ * particle's last converged h -- the post-ghost h changed (the host
+ * re-planned them and ran the force again), out[2] that needed ghost rounds
+ * beyond the graph's, out[3] graph captures. */
+int sphgpu_step_stats(sphgpu_space *s, int64_t out[4], int32_t reset);
+
 /* Host time (ms, summed since the last reset) of the planning that steps
  * need: [0] sphgpu_set_active's cell refresh and list building, [1] its
  * uploads, [2] the force lists planned inside steps after a ghost. */

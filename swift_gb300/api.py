@@ -91,6 +91,7 @@ SIGNATURES = {
     "sphgpu_step": (ctypes.c_int, [_P, _I32, _P]),
     "sphgpu_step_host": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "sphgpu_space_update": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "sphgpu_step_stats": (ctypes.c_int, [_P, _P, _I32]),
     "sphgpu_step_plain": (ctypes.c_int, [_P, _P]),
     "sphgpu_step_host_async": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "sphgpu_step_host_wait": (ctypes.c_int, [_P]),
@@ -393,6 +394,14 @@ class Space:
             self.step_plain()
         else:
             self.step(stages)
+
+    def step_stats(self, reset=False):
+        """{graph_steps, force_replans, late_rounds, captures} since the last
+        reset."""
+        out = np.zeros(4, np.int64)
+        _check(lib().sphgpu_step_stats(self._h, _ptr(out), int(bool(reset))))
+        return dict(zip(("graph_steps", "force_replans", "late_rounds", "captures"),
+                        (int(v) for v in out)))
 
     def update(self, v, m, u, stream=None):
         """New velocities, masses and internal energies (input order), e.g.

@@ -31,11 +31,16 @@ namespace {
 struct DevPlan {
   DBuf<Entry> entries;
   DBuf<int> lpb, pb, pe;  // leaf_pair_begin, pair_block, pair_entry
-  void upload(const Plan& pl, cudaStream_t s) {
+  // true when a buffer had to grow (its address changed: a captured step
+  // graph that reads it is stale)
+  bool upload(const Plan& pl, cudaStream_t s) {
+    const void* before[4] = {entries.p, lpb.p, pb.p, pe.p};
     entries.upload(pl.entries.data(), pl.entries.size(), s);
     lpb.upload(pl.leaf_pair_begin.data(), pl.leaf_pair_begin.size(), s);
     pb.upload(pl.pair_block.data(), pl.pair_block.size(), s);
     pe.upload(pl.pair_entry.data(), pl.pair_entry.size(), s);
+    return before[0] != entries.p || before[1] != lpb.p || before[2] != pb.p ||
+           before[3] != pe.p;
   }
 };
 
@@ -112,8 +117,8 @@ struct sphgpu_space {
   DBuf<int> differ;
   DBuf<float> v_stage, m_stage, h_stage, u_stage, out_stage;
   // The batched step is one CUDA graph (density first pass, ghost rounds,
-  // force); event-record nodes inside it time each loop of every step.
-  // graph[0]: density + the first kGraphRounds ghost rounds; graph[1]: force
+  // the force plan's check, force) in graph[0]; event-record nodes inside it
+  // time each loop of every step (graph[1] is unused)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double plan_ms = 0;  // host planning inside steps (force re-plans)
@@ -122,6 +127,16 @@ struct sphgpu_space {
   long long phase_steps = 0;
   DBuf<unsigned long long> hit_ctr;
   DBuf<int> err;  // set by a kernel that gave up (a bounded wait ran out)
+  // the force recursion's decisions the force lists were planned with, per
+  // checked cell, and the flag the step's verification sets
+  DBuf<int4> chk;
+  DBuf<uint8_t> chk_pred;
+  DBuf<int> vflag;
+  int nchk = 0;
+  // [0] steps run as one graph, [1] of them whose force plan the real h
+  // changed (re-planned on the host), [2] that needed ghost rounds beyond the
+  // graph's, [3] graph captures
+  int64_t step_stats[4] = {0, 0, 0, 0};
   bool count_hits = false;
   // per-cell sort arrays (sphgpu_hydro_sort)
   DBuf<SortCell> sort_cells;
@@ -366,6 +381,16 @@ void ensure_device(sphgpu_space* s) {
   s->hit_ctr.alloc(4);
   s->err.alloc(1);
   CK(cudaMemsetAsync(s->err.p, 0, sizeof(int), st));
+  {
+    const auto& fc = s->space->force_checks();
+    static_assert(sizeof(ForceCheck) == sizeof(int4), "one int4 per checked cell");
+    s->nchk = (int)fc.size();
+    s->chk.upload(reinterpret_cast<const int4*>(fc.data()), fc.size(), st);
+    if (!s->chk.p) s->chk.alloc(1);
+    s->chk_pred.alloc(std::max<size_t>(1, fc.size()));
+    CK(cudaMemsetAsync(s->chk_pred.p, 0, std::max<size_t>(1, fc.size()), st));
+    s->vflag.alloc(1);
+  }
   alloc_rows(s, st);
   for (auto& e : s->ev) CK(cudaEventCreate(&e));
   CK(cudaMemsetAsync(s->fin0.p, 0, sizeof(float4) * n, st));
@@ -645,10 +670,24 @@ void fetch_active_h(sphgpu_space* s, cudaStream_t st) {
 
 // The force loop's recursion depends on the post-ghost h_max of every cell
 // (cell.h:966-1010 use hydro.h_max); plan it once the ghost has run.
+void drop_graph(sphgpu_space* s);
+
+// The force lists and the decisions they were planned with (one per checked
+// cell) to the device; false when the buffers kept their addresses.
+bool upload_force_plan(sphgpu_space* s, const std::vector<uint8_t>& pred, cudaStream_t st) {
+  const bool moved = s->dplan_f.upload(s->plan_f, st);
+  if (!pred.empty())
+    CK(cudaMemcpyAsync(s->chk_pred.p, pred.data(), pred.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));  // the host vectors may change after this
+  return moved;
+}
+
 void plan_force(sphgpu_space* s, cudaStream_t st) {
   fetch_active_h(s, st);
   s->space->plan_density(s->plan_f, true);
-  s->dplan_f.upload(s->plan_f, st);
+  std::vector<uint8_t> pred;
+  s->space->force_decisions(pred);
+  if (upload_force_plan(s, pred, st)) drop_graph(s);
   s->force_planned = true;
   s->h_stale = false;
 }
@@ -887,24 +926,43 @@ int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
     s->force_planned = false;
     s->task_d.clear();
     s->task_f.clear();
-    drop_graph(s);
     if (s->dev) {
       upload_activity(s, s->stream);
-      s->dplan_d.upload(s->plan_d, s->stream);
-      s->dplan_s.upload(s->plan_s, s->stream);
+      bool moved = s->dplan_d.upload(s->plan_d, s->stream);
+      moved |= s->dplan_s.upload(s->plan_s, s->stream);
       CK(cudaStreamSynchronize(s->stream));
       s->act_upload_ms += std::chrono::duration<double, std::milli>(
                               std::chrono::steady_clock::now() - t1).count();
+      // the force lists ahead of the step, from each active particle's last
+      // converged h; the step checks the plan's decisions on the device
+      // after its ghost and re-plans on the host if any differs
+      const auto t2 = std::chrono::steady_clock::now();
+      std::vector<uint8_t> pred;
+      s->space->plan_force_predicted(s->plan_f, pred);
+      moved |= upload_force_plan(s, pred, s->stream);
+      s->force_planned = true;
+      s->plan_ms += std::chrono::duration<double, std::milli>(
+                        std::chrono::steady_clock::now() - t2).count();
+      // the step graph reads the plans in place: it stays valid unless a
+      // buffer moved
+      if (moved) drop_graph(s);
+    } else {
+      drop_graph(s);
     }
     return SPHGPU_OK;
   });
 }
 
 namespace {
-// A planned step: graph[0] (density + the first rounds), the rare later
-// rounds (a host check of the round counter, only when the graph's rounds
-// did not finish the ghost), graph[1] (force).  Events ev[0..3] bracket the
-// phases; nothing waits for the force.
+// A planned step is one CUDA graph: density, the first kGraphRounds ghost
+// rounds, the check of the force plan's decisions against the post-ghost
+// h_max, force.  Events ev[0..3] bracket the phases (ev[1], ev[2] are
+// event-record nodes inside the graph).  After it the host reads two words:
+// particles still iterating after the graph's rounds (rare: the remaining
+// rounds run here) and the check's flag (a decision of the force recursion
+// that the real h changed: the lists are re-planned on the host); either
+// way the force runs again on the host's plan, so the results are always
+// those of the force lists the post-ghost h gives.
 void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
   s->h_stale = true;
   const int rounds = std::min(kGraphRounds, s->prm.max_iter);
@@ -914,21 +972,35 @@ void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
       enqueue_density(s, st, true);
       CK(cudaEventRecordWithFlags(s->ev[1], st, cudaEventRecordExternal));
       enqueue_ghost_rounds(s, st, 0, rounds);
+      CK(cudaEventRecordWithFlags(s->ev[2], st, cudaEventRecordExternal));
+      CK(cudaMemsetAsync(s->vflag.p, 0, sizeof(int), st));
+      CK(launch_verify_force_plan(s->P, s->chk.p, s->nchk, s->chk_pred.p, s->vflag.p, st));
+      enqueue_force(s, st);
     });
-    s->graph[1] = capture(st, [&]() { enqueue_force(s, st); });
+    s->step_stats[3]++;
   }
   CK(cudaEventRecord(s->ev[0], st));
   CK(cudaGraphLaunch(s->graph[0], st));
+  CK(cudaEventRecord(s->ev[3], st));
+  s->step_stats[0]++;
+  int left = 0, changed = 0;
   if (rounds < s->prm.max_iter) {
-    // particles still iterating after the graph's rounds: the rest here
-    int left = 0;
     const int* cnt = lists_on(s) ? s->catchup.p + rounds : s->redo.p + rounds - 1;
     CK(cudaMemcpyAsync(&left, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (left > 0) enqueue_ghost_rounds(s, st, rounds, s->prm.max_iter);
   }
-  CK(cudaEventRecord(s->ev[2], st));
-  CK(cudaGraphLaunch(s->graph[1], st));
+  CK(cudaMemcpyAsync(&changed, s->vflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (left <= 0 && !changed) return;
+  if (left > 0) {
+    enqueue_ghost_rounds(s, st, rounds, s->prm.max_iter);
+    s->step_stats[2]++;
+  }
+  if (changed) s->step_stats[1]++;
+  const auto t0 = std::chrono::steady_clock::now();
+  plan_force(s, st);  // the real post-ghost h
+  s->plan_ms += std::chrono::duration<double, std::milli>(
+                    std::chrono::steady_clock::now() - t0).count();
+  enqueue_force(s, st);
   CK(cudaEventRecord(s->ev[3], st));
 }
 }  // namespace
@@ -1441,6 +1513,14 @@ int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms
   const int rc = sphgpu_set_tuning(s, &bt);
   if (rc) return rc;
   *best = bt;
+  return SPHGPU_OK;
+}
+
+int sphgpu_step_stats(sphgpu_space* s, int64_t out[4], int32_t reset) {
+  if (!s || !out) return fail(SPHGPU_EINVAL, "null argument");
+  for (int k = 0; k < 4; k++) out[k] = s->step_stats[k];
+  if (reset)
+    for (int k = 0; k < 4; k++) s->step_stats[k] = 0;
   return SPHGPU_OK;
 }
 

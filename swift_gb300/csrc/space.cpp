@@ -367,6 +367,11 @@ void Space::build(int64_t n, const double* x, const float* h,
     if (active_[k]) active_list_.push_back(k);
   }
   cell_mark_.assign(cells_.size(), 0);
+  force_checks_.clear();
+  for (size_t c = 0; c < cells_.size(); c++)
+    if (cells_[c].split && cells_[c].count >= kRecurseSize)
+      force_checks_.push_back({cells_[c].first, cells_[c].count, cells_[c].dmin, (int)c});
+  h_conv_.clear();
 }
 
 static inline uint32_t spread10(uint32_t v) {
@@ -756,10 +761,12 @@ void Space::redrift_leaf(int c) {
 void Space::update_h_active(const float* h_active) {
   // runner_ghost.c:1617-1632: a cell's h_max only grows (atomic max with the
   // pre-ghost value); only the active particles' h changed.
+  if (h_conv_.size() != (size_t)n_) h_conv_ = h_;
   for (size_t a = 0; a < active_list_.size(); a++) {
     const int k = active_list_[a];
     const float h = h_active[a];
     h_[k] = h;
+    h_conv_[k] = h;
     for (int c = leaves_[leaf_of_[k]]; c >= 0; c = cells_[c].parent) {
       if (cells_[c].h_max >= h && cells_[c].h_max_active >= h) break;
       cells_[c].h_max = fmaxr(cells_[c].h_max, h);
@@ -1160,6 +1167,37 @@ void Space::leaf_infos(std::vector<LeafInfo>& out) const {
     }
     li.nlevels = n;
   }
+}
+
+void Space::force_decisions(std::vector<uint8_t>& pred) const {
+  pred.resize(force_checks_.size());
+  for (size_t q = 0; q < force_checks_.size(); q++) {
+    const Cell& c = cells_[force_checks_[q].cell];
+    pred[q] = (SPH_KG * c.h_max + 0.f) < 0.5f * c.dmin ? 1 : 0;
+  }
+}
+
+void Space::plan_force_predicted(Plan& plan, std::vector<uint8_t>& pred) {
+  if (h_conv_.size() != (size_t)n_) h_conv_ = h_;
+  // the cells' h_max as update_h_active would leave it, with each active
+  // particle at its last converged h
+  std::vector<float> saved(cells_.size());
+  for (size_t c = 0; c < cells_.size(); c++) saved[c] = cells_[c].h_max;
+  for (int k : active_list_) {
+    const float h = h_conv_[k];
+    for (int c = leaves_[leaf_of_[k]]; c >= 0; c = cells_[c].parent) {
+      if (cells_[c].h_max >= h) break;
+      cells_[c].h_max = h;
+    }
+  }
+  force_decisions(pred);
+  try {
+    plan_density(plan, true);
+  } catch (...) {
+    for (size_t c = 0; c < cells_.size(); c++) cells_[c].h_max = saved[c];
+    throw;
+  }
+  for (size_t c = 0; c < cells_.size(); c++) cells_[c].h_max = saved[c];
 }
 
 void Space::update_h_after_ghost(const float* h_sorted) {

@@ -51,6 +51,14 @@ struct Plan {
   std::vector<int> leaf_pair_begin;
 };
 
+// A cell whose decision the force recursion can read (16 bytes: uploaded as
+// one int4 per cell, dmin's bits in the third word).
+struct ForceCheck {
+  int32_t first, count;
+  float dmin;
+  int32_t cell;
+};
+
 constexpr int kSubBlock = 8;  // particles per sub-box of a j-block (4 per block of 32)
 
 struct JBlocks {
@@ -105,6 +113,18 @@ class Space {
   // (second=true, call update_h_after_ghost first); ghost re-runs.
   void plan_density(Plan& plan, bool second) const;
   void plan_subset(Plan& plan) const;
+  // The force pass's lists planned before the step's ghost, with every
+  // active particle at the h it converged to the last time a ghost ran on
+  // it (the cells' post-ghost h_max predicted); the force recursion's
+  // decision of every checked cell (force_checks) goes to pred[] -- the
+  // step verifies them against the real post-ghost h_max on the device.
+  void plan_force_predicted(Plan& plan, std::vector<uint8_t>& pred);
+  // Decisions of the force recursion (cell.h:966-1010: gamma h_max <
+  // dmin / 2) for the checked cells at the cells' current h_max.
+  void force_decisions(std::vector<uint8_t>& pred) const;
+  // The cells whose decision the force recursion can read: split, with at
+  // least kRecurseSize particles (first, count, dmin, cell id).
+  const std::vector<ForceCheck>& force_checks() const { return force_checks_; }
   void leaf_infos(std::vector<LeafInfo>& out) const;
   void update_h_after_ghost(const float* h_sorted);
 
@@ -193,6 +213,8 @@ class Space {
   int threads_ = 0;
   std::vector<double> x_;
   std::vector<float> h_in_, h_;
+  std::vector<float> h_conv_;        // each particle's h after its last ghost
+  std::vector<ForceCheck> force_checks_;
   std::vector<int8_t> tb_in_;
   std::vector<uint8_t> active_;
   std::vector<int> active_list_;

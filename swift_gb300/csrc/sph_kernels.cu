@@ -125,6 +125,33 @@ __global__ void permute_in(DevParticles P, const int32_t* __restrict__ perm,
   }
 }
 
+// The force recursion's decisions at the step's post-ghost h_max (per
+// checked cell: the larger of the step's starting h and the ghost's result
+// over its particles, runner_ghost.c:1617-1632; gamma h_max < dmin / 2,
+// cell.h:966-1010) against the ones the force lists were planned with; any
+// difference sets *flag.  One warp per cell.
+__global__ void verify_force_plan(DevParticles P, const int4* __restrict__ chk, int nchk,
+                                  const uint8_t* __restrict__ planned, int* flag) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int q = warp; q < nchk; q += nwarps) {
+    const int4 c = chk[q];
+    float m = 0.f;
+    for (int k = c.x + lane; k < c.x + c.y; k += 32) {
+      float h = P.posh[k].w;
+      if (P.flags[k] & 1) h = fmaxf(h, P.h0[k]);
+      m = fmaxf(m, h);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if (lane == 0) {
+      const bool d = __fmul_rn(SPH_KG, m) < __fmul_rn(0.5f, __int_as_float(c.z));
+      if ((uint8_t)(d ? 1 : 0) != planned[q]) atomicOr(flag, 1);
+    }
+  }
+}
+
 // New velocities, masses and internal energies (input order) into the
 // store; positions and h stay the space's.
 __global__ void permute_vmu_in(DevParticles P, const int32_t* __restrict__ perm,
@@ -240,6 +267,16 @@ cudaError_t launch_permute_in(DevParticles p, const int32_t* perm,
                               cudaStream_t s) {
   permute_in<<<grid_for(p.n), 256, 0, s>>>(p, perm, x_in, x_ref, v_in, m_in, h_in, u_in,
                                            differ);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_verify_force_plan(DevParticles p, const int4* chk, int nchk,
+                                    const uint8_t* planned, int* flag, cudaStream_t s) {
+  if (nchk <= 0) return cudaSuccess;
+  int g = (nchk + 7) / 8;  // 8 warps per block, one warp per cell
+  const int cap = 16 * sm_count();
+  g = g > cap ? cap : g;
+  verify_force_plan<<<g, 256, 0, s>>>(p, chk, nchk, planned, flag);
   return cudaGetLastError();
 }
 

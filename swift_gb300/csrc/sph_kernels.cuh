@@ -181,6 +181,8 @@ cudaError_t launch_prepare_posh(DevParticles p, const int32_t* top_of,
                                 const double* top_loc, cudaStream_t s);
 // Host-order v, m, u -> store; sets *differ when x or h differ from the
 // space's own (x_ref: the space's input positions, input order).
+cudaError_t launch_verify_force_plan(DevParticles p, const int4* chk, int nchk,
+                                    const uint8_t* planned, int* flag, cudaStream_t s);
 cudaError_t launch_permute_vmu_in(DevParticles p, const int32_t* perm, const float* v,
                                   const float* m, const float* u, cudaStream_t s);
 cudaError_t launch_permute_in(DevParticles p, const int32_t* perm,

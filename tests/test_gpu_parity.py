@@ -465,6 +465,54 @@ def test_primed_sparse_step(cfg, mab, oracle_lib):
     assert np.mean(out["ngb_final"][act] == ref["ngb_final"][act]) > 0.99
 
 
+def test_sparse_steps_replay_one_graph(oracle_lib):
+    """After the all-active step, every sparse step is one CUDA graph: the
+    force lists are planned when the active set is set, from each active
+    particle's last converged h, and checked on the device against the
+    post-ghost h (on a static box the check always passes, so no step
+    re-plans and the graph captured for the first sparse step serves them
+    all).  The last step matches the oracle's primed sparse step."""
+    box = ics.make("sedov:32", seed=6)
+    mab = 21
+    ref = oracle_lib.run(box, api.STAGE_PRIME | api.STAGE_ALL, max_active_bin=mab)
+    act = box["time_bin"] <= mab
+    with api.Space(box) as sp:
+        sp.set_active(api.ALL_ACTIVE)
+        sp.step()
+        sp.step_stats(reset=True)
+        for b in (22, 20, 23, 21, 22, mab):
+            sp.set_active(b)
+            sp.step()
+        st = sp.step_stats()
+        out = sp.download()
+    assert st["graph_steps"] == 6 and st["captures"] == 1, st
+    assert st["force_replans"] == 0 and st["late_rounds"] == 0, st
+    assert np.array_equal(out["ngb_first"][act], ref["ngb_first"][act])
+    assert rel_err(out["h"], ref["h"]).max() < 2e-4
+    for k in ("rho", "pressure", "soundspeed", "v_sig"):
+        assert rel_err(out[k], ref[k]).max() < 3e-4, k
+    for k in ("ax", "ay", "az", "u_dt", "h_dt"):
+        assert scaled_err(out[k][act], ref[k][act]).max() < 1e-3, k
+    assert np.mean(out["ngb_force"][act] == ref["ngb_force"][act]) > 0.99
+
+
+def test_all_active_steps_replay_one_graph():
+    """All-active steps after the first: one graph each, the force plan of
+    the first step verified on the device every step."""
+    box = ics.make("clustered:24", seed=3)
+    with api.Space(box) as sp:
+        sp.step()
+        a = sp.download()
+        sp.step_stats(reset=True)
+        for _ in range(3):
+            sp.step()
+        st = sp.step_stats()
+        b = sp.download()
+    assert st == {"graph_steps": 3, "force_replans": 0, "late_rounds": 0, "captures": 1}, st
+    assert np.array_equal(a["ngb_force"], b["ngb_force"])
+    assert np.array_equal(a["ngb_first"], b["ngb_first"])
+
+
 def test_primed_sparse_plain_equals_batched():
     box = ics.make("sedov:24", seed=8)
     with api.Space(box) as sp:

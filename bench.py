@@ -335,6 +335,7 @@ def sparse_record(workload, steps, warmup, plain_steps, seed):
     sp.phase_times(reset=True)
     sp.host_times(reset=True)
     sp.step_stats(reset=True)
+    sp.plan_times(reset=True)
     clocks = ClockSampler(local_rank)
     t_b, inter = [], []
     graphs = {"graph_steps": 0, "force_replans": 0, "late_rounds": 0, "captures": 0}
@@ -347,6 +348,7 @@ def sparse_record(workload, steps, warmup, plain_steps, seed):
     clk = clocks.stop()
     phase_ms, nsteps = sp.phase_times(reset=True)
     host_ms = {k: v / max(1, len(t_b)) for k, v in sp.host_times(reset=True).items()}
+    dp_ms, dp_steps = sp.plan_times(reset=True)
     # plain form: same state origin, same steps
     prime()
     for b in seq[:min(warmup, 1)]:
@@ -371,6 +373,10 @@ def sparse_record(workload, steps, warmup, plain_steps, seed):
                           "ghost_rounds": phase_ms[1] / max(1, nsteps),
                           "force": phase_ms[2] / max(1, nsteps)},
         "host_ms_per_step": host_ms,
+        # gather lists planned inside each step's graph (device time, part of
+        # phases_ms_gpu) by the steps that planned on the device
+        "device_planning_ms_per_step": dp_ms / max(1, dp_steps),
+        "device_planned_steps": dp_steps,
         "batched_ms_per_step": [round(1e3 * t, 3) for t in t_b],
         "plain_ms_per_step": [round(1e3 * t, 3) for t in t_p],
         "plain_over_batched": ms_p / ms_p_same,

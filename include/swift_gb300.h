@@ -47,6 +47,7 @@ extern "C" {
 #define SPHGPU_ENOCONV -4  /* smoothing lengths did not converge */
 #define SPHGPU_ESTATE -5   /* call out of order (e.g. no step run yet) */
 #define SPHGPU_ENODEV -6   /* no CUDA device */
+#define SPHGPU_EREBUILD -7 /* particles moved too far for the cell tree: rebuild */
 
 /* Stages of a step (bit mask). */
 #define SPHGPU_STAGE_DENSITY 1
@@ -179,17 +180,66 @@ int sphgpu_autotune(sphgpu_space *s, int32_t reps, sphgpu_tuning *best,
 int sphgpu_step(sphgpu_space *s, int32_t stages, void *stream);
 
 /* Steps of the batched form since the last reset: out[0] steps run as one
- * CUDA graph (density, ghost rounds, the force plan's check, force), out[1]
- * of them whose force lists -- planned before the step from each active
- * particle's last converged h -- the post-ghost h changed (the host
- * re-planned them and ran the force again), out[2] that needed ghost rounds
- * beyond the graph's, out[3] graph captures. */
+ * CUDA graph, out[1] of them that ran a second time outside it (host
+ * planning: the force lists planned before the step from each active
+ * particle's last converged h, whose recursion decisions the post-ghost h
+ * changed, were re-planned; device planning: a plan outgrew its buffers,
+ * which grew), out[2] that needed ghost rounds beyond the graph's, out[3]
+ * graph captures. */
 int sphgpu_step_stats(sphgpu_space *s, int64_t out[4], int32_t reset);
 
 /* Host time (ms, summed since the last reset) of the planning that steps
  * need: [0] sphgpu_set_active's cell refresh and list building, [1] its
- * uploads, [2] the force lists planned inside steps after a ghost. */
+ * uploads, [2] the force lists planned inside steps after a ghost.  With
+ * device planning [0] is the time sphgpu_set_active takes and [1], [2]
+ * stay 0. */
 int sphgpu_host_times(sphgpu_space *s, double ms[3], int32_t reset);
+
+/* Device planning.  After sphgpu_set_active with a max_active_bin that
+ * leaves some particles inactive, on a space resident on the device (one
+ * GPU call has run on it), every batched step plans its own gather lists
+ * inside its CUDA graph: the flags from the time bins, each cell's h_max,
+ * h_max_active and activity from its particles, the density and re-run
+ * lists of the reference's recursions for every active leaf, and after the
+ * ghost the force lists from the post-ghost h_max -- the lists the host
+ * planner gives for the same state.  Activations with every particle
+ * active keep the host's plans (they stay valid from step to step).  The
+ * host planner takes over again, with the device's h, for the plain form,
+ * the per-task entry points and sphgpu_force_from_state.  on = 0 turns
+ * device planning off for the space (the default is on). */
+int sphgpu_set_device_planning(sphgpu_space *s, int32_t on);
+
+/* Moves the space's particles to new positions x (3 per particle) with new
+ * smoothing lengths h, input order, host or device memory, without a
+ * rebuild: every particle stays in the cell the rebuild gave it, as the
+ * reference's drift does between rebuilds (cell_drift.c:330-382).  Each
+ * cell's dx_max_part (the largest motion of its particles since the
+ * rebuild) and h_max are measured; if cell_need_rebuild_for_hydro_pair
+ * (cell.h:1237: kernel_gamma max(h_max_i, h_max_j) + dx_max_part_i +
+ * dx_max_part_j > dmin) holds for any pair of neighbouring top-level cells
+ * the call returns SPHGPU_EREBUILD and changes nothing (create a new space
+ * from the new positions).  Otherwise the positions, the particles' h (the
+ * h the next step's active particles start from, and the h of the inactive
+ * ones), their depth_h and the j-blocks' boxes are replaced, and the
+ * recursions of later steps add dx_max_part to their cut-offs (cell.h:
+ * 934-1010); later steps plan on the device (whatever their activity).
+ * sphgpu_step_host calls this when its x or h differ from the space's. */
+int sphgpu_space_drift(sphgpu_space *s, const double *x, const float *h, void *stream);
+
+/* Device time (ms, summed since the last reset) of the planning inside
+ * device-planned steps (cell state and lists, before the density loop and
+ * after the ghost), and the number of those steps. */
+int sphgpu_plan_times(sphgpu_space *s, double *ms, int64_t *steps, int32_t reset);
+
+/* Self-check of device planning: after a device-planned step, rebuilds the
+ * host planner's density, re-run and force lists from the device's state
+ * (the step's starting h, its activity and its post-ghost h) and compares
+ * them with the lists the step planned on the device, leaf by leaf.
+ * out[0..2]: (j-block, entry) pairs that differ in the density, re-run and
+ * force lists (a leaf whose pair count differs counts all its pairs);
+ * out[3..5]: the pairs of each device plan.  SPHGPU_ESTATE when the space
+ * is not device-planned or no step has run since the activation. */
+int sphgpu_check_device_plans(sphgpu_space *s, int64_t out[6]);
 
 /* Per-loop device time of the batched steps run so far (CUDA events on the
  * step's stream): ms_sum[0] density first pass, [1] ghost rounds (Newton
@@ -269,13 +319,29 @@ int sphgpu_step_host_wait(sphgpu_space *s);
  * would (one launch per self/pair task and loop, one ghost per top cell). */
 int sphgpu_step_plain(sphgpu_space *s, void *stream);
 
-/* Results in input order.  fields float [n][24]: 0-7 raw density sums of
- * the last density pass (rho, rho_dh, wcount, wcount_dh, div_v, rot_v[3]),
- * 8-14 after the ghost (h, rho, f, pressure, soundspeed, balsara, v_sig
- * seed), 15-20 after the force (a_hydro[3], u_dt, h_dt, v_sig).
- * ints int32 [n][4]: density neighbours (first pass), density neighbours
- * (last pass), force neighbours, ghost rounds.  Either may be NULL. */
+/* Results in input order, into host or device memory.  fields float
+ * [n][24]: 0-7 raw density sums of the last density pass (rho, rho_dh,
+ * wcount, wcount_dh, div_v, rot_v[3]), 8-14 after the ghost (h, rho, f,
+ * pressure, soundspeed, balsara, v_sig seed), 15-20 after the force
+ * (a_hydro[3], u_dt, h_dt, v_sig), 21 the smallest time bin among the force
+ * neighbours (limiter_data.min_ngb_time_bin, num_time_bins + 1 when none),
+ * 22-23 zero.  ints int32 [n][4]: density neighbours (first pass), density
+ * neighbours (last pass), force neighbours, ghost rounds.  Either may be
+ * NULL. */
 int sphgpu_download(sphgpu_space *s, float *fields, int32_t *ints);
+
+/* A caller's particle state for the next steps (input order, host or device
+ * memory; a NULL array keeps the space's): velocities v[3], masses,
+ * internal energies u, the force inputs the inactive particles lend their
+ * active neighbours (rho, pressure, soundspeed as the reference's drift
+ * predicts them, hydro_predict_extra -- the three go together -- and the
+ * grad-h term f and the Balsara switch of their last ghost), and time bins
+ * (the activity of later sphgpu_set_active calls).  Unlike
+ * sphgpu_space_update it does not check the values on the host. */
+int sphgpu_space_set_state(sphgpu_space *s, const float *v, const float *m, const float *u,
+                           const float *rho, const float *f, const float *pressure,
+                           const float *soundspeed, const float *balsara,
+                           const int8_t *time_bin, void *stream);
 
 /* Force loop only, from caller-provided post-ghost state (input order):
  * h, rho, f, pressure, soundspeed, balsara.  For parity checks of the force

@@ -19,7 +19,7 @@ from . import build as _build
 STAGE_DENSITY, STAGE_GHOST, STAGE_FORCE, STAGE_ALL = 1, 2, 4, 7
 ALL_ACTIVE = 127  # max_active_bin that activates every time bin
 STAGE_PRIME = 8  # oracle/run flag: a full all-active step runs first
-OK, EINVAL, ECUDA, ENOMEM, ENOCONV, ESTATE, ENODEV = 0, -1, -2, -3, -4, -5, -6
+OK, EINVAL, ECUDA, ENOMEM, ENOCONV, ESTATE, ENODEV, EREBUILD = 0, -1, -2, -3, -4, -5, -6, -7
 
 FIELD_COLS = {
     "d_rho": 0, "d_rho_dh": 1, "d_wcount": 2, "d_wcount_dh": 3, "d_div_v": 4,
@@ -27,6 +27,7 @@ FIELD_COLS = {
     "h": 8, "rho": 9, "f": 10, "pressure": 11, "soundspeed": 12,
     "balsara": 13, "v_sig_ghost": 14,
     "ax": 15, "ay": 16, "az": 17, "u_dt": 18, "h_dt": 19, "v_sig": 20,
+    "min_ngb_bin": 21,
 }
 INT_COLS = {"ngb_first": 0, "ngb_final": 1, "ngb_force": 2, "ghost_iters": 3}
 CELL_COLS = {"leaf_first": 0, "leaf_count": 1, "leaf_depth": 2, "depth_h": 3,
@@ -116,6 +117,11 @@ SIGNATURES = {
     "sphgpu_do_end_hydro_force": (ctypes.c_int, [_P, _P]),
     "sphgpu_phase_times": (ctypes.c_int, [_P, _P, _P, _I32]),
     "sphgpu_host_times": (ctypes.c_int, [_P, _P, _I32]),
+    "sphgpu_set_device_planning": (ctypes.c_int, [_P, _I32]),
+    "sphgpu_space_drift": (ctypes.c_int, [_P, _P, _P, _P]),
+    "sphgpu_space_set_state": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sphgpu_plan_times": (ctypes.c_int, [_P, _P, _P, _I32]),
+    "sphgpu_check_device_plans": (ctypes.c_int, [_P, _P]),
     "sphgpu_count_hits": (ctypes.c_int, [_P, _P]),
     "sphgpu_density_noalloc": (ctypes.c_int, [_P, _P, _P, _P]),
     "sphgpu_autotune": (ctypes.c_int, [_P, _I32, _P, _P, _P]),
@@ -395,9 +401,84 @@ class Space:
         else:
             self.step(stages)
 
+    def set_state(self, v=None, m=None, u=None, rho=None, f=None, pressure=None,
+                  soundspeed=None, balsara=None, time_bin=None, stream=None):
+        """A caller's particle state (input order; numpy arrays or CUDA
+        tensors; None keeps the space's): see sphgpu_space_set_state."""
+        keep = []
+
+        def ptr(a, dtype, shape):
+            if a is None:
+                return None
+            if hasattr(a, "data_ptr"):
+                assert a.is_contiguous() and tuple(a.shape) == shape
+                assert a.element_size() == np.dtype(dtype).itemsize
+                keep.append(a)
+                return ctypes.c_void_p(a.data_ptr())
+            a = np.ascontiguousarray(a, dtype)
+            assert a.shape == shape
+            keep.append(a)
+            return _ptr(a)
+        n = self.n
+        _check(lib().sphgpu_space_set_state(
+            self._h, ptr(v, np.float32, (n, 3)), ptr(m, np.float32, (n,)),
+            ptr(u, np.float32, (n,)), ptr(rho, np.float32, (n,)), ptr(f, np.float32, (n,)),
+            ptr(pressure, np.float32, (n,)), ptr(soundspeed, np.float32, (n,)),
+            ptr(balsara, np.float32, (n,)), ptr(time_bin, np.int8, (n,)), stream))
+
+    def download_into(self, fields):
+        """Results into a caller's float32 [n][24] array (a CUDA tensor or
+        a numpy array), sphgpu_download's column layout."""
+        assert tuple(fields.shape) == (self.n, 24)
+        if hasattr(fields, "data_ptr"):
+            assert fields.is_contiguous() and fields.element_size() == 4
+            p = ctypes.c_void_p(fields.data_ptr())
+        else:
+            assert fields.flags["C_CONTIGUOUS"] and fields.dtype == np.float32
+            p = _ptr(fields)
+        _check(lib().sphgpu_download(self._h, p, None))
+        return fields
+
+    def drift(self, x, h, stream=None):
+        """New positions and h (input order; numpy arrays or CUDA tensors)
+        without a rebuild; raises SphGpuError(EREBUILD) when the particles
+        moved too far for the cell tree (the space is then unchanged)."""
+        def ptr(a, dtype, shape):
+            if hasattr(a, "data_ptr"):
+                assert a.is_contiguous() and tuple(a.shape) == shape
+                assert a.element_size() == np.dtype(dtype).itemsize and a.is_floating_point()
+                return ctypes.c_void_p(a.data_ptr()), a
+            a = np.ascontiguousarray(a, dtype)
+            assert a.shape == shape
+            return _ptr(a), a
+        px, kx = ptr(x, np.float64, (self.n, 3))
+        ph, kh = ptr(h, np.float32, (self.n,))
+        _check(lib().sphgpu_space_drift(self._h, px, ph, stream))
+        del kx, kh
+
+    def set_device_planning(self, on=True):
+        """Device planning of sparse steps' gather lists (on by default)."""
+        _check(lib().sphgpu_set_device_planning(self._h, int(bool(on))))
+
+    def plan_times(self, reset=False):
+        """(ms of device planning summed over device-planned steps, steps)."""
+        ms = ctypes.c_double()
+        steps = ctypes.c_int64()
+        _check(lib().sphgpu_plan_times(self._h, ctypes.byref(ms), ctypes.byref(steps),
+                                       int(bool(reset))))
+        return ms.value, steps.value
+
+    def check_device_plans(self):
+        """Device plans of the last step against the host planner's for the
+        same state: {density, rerun, force}: (differing pairs, pairs)."""
+        out = np.zeros(6, np.int64)
+        _check(lib().sphgpu_check_device_plans(self._h, _ptr(out)))
+        return {k: (int(out[i]), int(out[3 + i]))
+                for i, k in enumerate(("density", "rerun", "force"))}
+
     def step_stats(self, reset=False):
         """{graph_steps, force_replans, late_rounds, captures} since the last
-        reset."""
+        reset (force_replans: steps run a second time outside the graph)."""
         out = np.zeros(4, np.int64)
         _check(lib().sphgpu_step_stats(self._h, _ptr(out), int(bool(reset))))
         return dict(zip(("graph_steps", "force_replans", "late_rounds", "captures"),

@@ -18,6 +18,7 @@
 #include "../../include/swift_gb300.h"
 #include "space.h"
 #include "capi_util.h"
+#include "devplan.cuh"
 #include "sort.cuh"
 #include "sph_kernels.cuh"
 
@@ -138,6 +139,43 @@ struct sphgpu_space {
   // graph's, [3] graph captures
   int64_t step_stats[4] = {0, 0, 0, 0};
   bool count_hits = false;
+  // Device planner (devplan.cu).  After a sparse activation of a resident
+  // space every step plans its own gather lists inside its graph (density
+  // and re-run lists from the activation state, force lists from the
+  // post-ghost h_max); the host planner's h, activity and plans then lag the
+  // device's until leave_device_mode() brings them level.
+  bool dmode = false;
+  bool dp_ready = false;      // the tree is on the device for the current j-blocks
+  bool dp_usable = true;      // false: the tree is too deep, or the planner failed once
+  bool dp_off_by_caller = false;  // sphgpu_set_device_planning(s, 0)
+  bool host_refresh = false;  // the next host activation recomputes every cell
+  int dp_bin = 0;             // max_active_bin of the device-planned steps
+  int max_bin = 0;            // largest time bin of the particles
+  DPTree dpt;
+  DBuf<DPCell> dp_cell;
+  DBuf<int32_t> dp_prog, dp_leaf, dp_lbeg, dp_link;
+  DBuf<int2> dp_task;
+  DBuf<unsigned> dp_hmax, dp_hact, dp_hforce;
+  DBuf<int> dp_active;
+  DBuf<int2> dp_lane, dp_off, dp_tiles;
+  DBuf<int> dp_status, dp_bin_dev;
+  long long dp_cap_e[3] = {0, 0, 0}, dp_cap_p[3] = {0, 0, 0};
+  // events around the planning inside a step: [0, 1] the activation plans,
+  // [2, 3] the force plan
+  cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double dp_ms = 0;
+  long long dp_steps = 0;
+  // Drift without a rebuild (sphgpu_space_drift): the rebuild's positions
+  // (input order), per cell the dx_max_part in use and the one proposed, the
+  // proposed h_max, the rebuild flag; the host planner's dx_max and input h
+  // lag the device's while drift_host_stale
+  bool drifted = false;
+  bool drift_host_stale = false;
+  bool bins_host_stale = false;  // sphgpu_space_set_state gave new time bins
+  DBuf<int8_t> tb_stage;
+  DBuf<double> x_rb;
+  DBuf<unsigned> dp_dx, dp_dxn, dp_hdrift;
+  DBuf<int> drift_flag;
   // per-cell sort arrays (sphgpu_hydro_sort)
   DBuf<SortCell> sort_cells;
   DBuf<int> sort_leaf_ids, sort_split_ids, g_of_s_dev;
@@ -172,6 +210,8 @@ struct sphgpu_space {
     for (auto& g : graph)
       if (g) cudaGraphExecDestroy(g);
     for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    for (auto& e : pev)
       if (e) cudaEventDestroy(e);
     if (cin) cudaStreamDestroy(cin);
     if (cout) cudaStreamDestroy(cout);
@@ -393,6 +433,7 @@ void ensure_device(sphgpu_space* s) {
   }
   alloc_rows(s, st);
   for (auto& e : s->ev) CK(cudaEventCreate(&e));
+  for (auto& e : s->pev) CK(cudaEventCreate(&e));
   CK(cudaMemsetAsync(s->fin0.p, 0, sizeof(float4) * n, st));
   CK(cudaMemsetAsync(s->fin1.p, 0, sizeof(float2) * n, st));
   CK(cudaMemsetAsync(s->acc.p, 0, sizeof(float4) * n, st));
@@ -725,6 +766,471 @@ cudaGraphExec_t capture(cudaStream_t st, F&& body) {
   return ex;
 }
 
+// ---------------------------------------------------------------------------
+// Device planning
+
+// The tree, the tasks and the j-block ranges for the device planner (again
+// after a change of the j-block depth).
+void dp_upload_tree(sphgpu_space* s, cudaStream_t st) {
+  const Space& sp = *s->space;
+  const auto& cells = sp.cells();
+  const auto& jb = sp.jblocks();
+  const size_t nc = cells.size();
+  std::vector<DPCell> dc(nc);
+  std::vector<int32_t> prog(8 * nc);
+  int maxd = 0;
+  for (size_t c = 0; c < nc; c++) {
+    const Cell& x = cells[c];
+    DPCell& d = dc[c];
+    std::memset(&d, 0, sizeof(d));
+    for (int k = 0; k < 3; k++) d.loc[k] = x.loc[k];
+    d.dmin = x.dmin;
+    d.first = x.first;
+    d.count = x.count;
+    d.parent = x.parent;
+    d.top = x.top;
+    d.jb_begin = jb.cell_begin[c];
+    d.jb_end = jb.cell_end[c];
+    d.depth = (int16_t)x.depth;
+    d.split = (int8_t)(x.split ? 1 : 0);
+    for (int k = 0; k < 8; k++) prog[8 * c + k] = x.progeny[k];
+    maxd = std::max(maxd, x.depth);
+  }
+  const auto& tasks = sp.tasks();
+  std::vector<int2> tk(tasks.size());
+  for (size_t t = 0; t < tasks.size(); t++) tk[t] = make_int2(tasks[t].ci, tasks[t].cj);
+  const auto& links = sp.top_links();
+  std::vector<int32_t> lb(links.size() + 1, 0), lk;
+  for (size_t c = 0; c < links.size(); c++) {
+    lb[c] = (int32_t)lk.size();
+    lk.insert(lk.end(), links[c].begin(), links[c].end());
+  }
+  lb[links.size()] = (int32_t)lk.size();
+  const std::vector<int>& lv = sp.leaves();
+  s->dp_cell.upload(dc.data(), nc, st);
+  s->dp_prog.upload(prog.data(), prog.size(), st);
+  s->dp_leaf.upload(lv.data(), lv.size(), st);
+  s->dp_task.upload(tk.data(), std::max<size_t>(1, tk.size()), st);
+  s->dp_lbeg.upload(lb.data(), lb.size(), st);
+  s->dp_link.upload(lk.data(), std::max<size_t>(1, lk.size()), st);
+  if (s->dp_hmax.n < nc) {
+    s->dp_hmax.alloc(nc);
+    s->dp_hact.alloc(nc);
+    s->dp_hforce.alloc(nc);
+    s->dp_active.alloc(nc);
+  }
+  const size_t nl = lv.size();
+  if (s->dp_off.n < nl + 1) {
+    s->dp_lane.alloc(32 * nl);
+    s->dp_off.alloc(nl + 1);
+    s->dp_tiles.alloc(dp_scan_tiles((long long)nl + 1));
+  }
+  if (!s->dp_status.p) {
+    s->dp_status.alloc(8);
+    s->dp_bin_dev.alloc(1);
+  }
+  DPTree& t = s->dpt;
+  t.cell = s->dp_cell.p;
+  t.progeny = s->dp_prog.p;
+  t.leaf_cell = s->dp_leaf.p;
+  t.task = s->dp_task.p;
+  t.link_begin = s->dp_lbeg.p;
+  t.link = s->dp_link.p;
+  t.ncells = (int)nc;
+  t.nleaves = (int)nl;
+  t.ntop = (int)links.size();
+  t.ntasks = (int)tasks.size();
+  for (int k = 0; k < 3; k++) t.dim[k] = s->prm.dim[k];
+  t.periodic = s->prm.periodic;
+  CK(cudaStreamSynchronize(st));  // the host vectors above die here
+  // frames: one per level below the top cell, the root task and a margin
+  if (maxd + 3 > kDPStack) s->dp_usable = false;
+  s->dp_ready = true;
+}
+
+DPCellState dp_state(sphgpu_space* s) {
+  DPCellState cs;
+  cs.hmax = s->dp_hmax.p;
+  cs.hact = s->dp_hact.p;
+  cs.hforce = s->dp_hforce.p;
+  cs.active = s->dp_active.p;
+  cs.dx = s->drifted ? s->dp_dx.p : nullptr;
+  return cs;
+}
+
+DevPlan& dp_plan_of(sphgpu_space* s, int kind) {
+  return kind == DP_DENSITY ? s->dplan_d : (kind == DP_SUBSET ? s->dplan_s : s->dplan_f);
+}
+
+DPOut dp_out(sphgpu_space* s, int kind) {
+  DevPlan& dp = dp_plan_of(s, kind);
+  DPOut o;
+  o.entries = dp.entries.p;
+  o.lpb = dp.lpb.p;
+  o.pb = dp.pb.p;
+  o.pe = dp.pe.p;
+  o.cap_e = s->dp_cap_e[kind];
+  o.cap_p = s->dp_cap_p[kind];
+  o.lane_off = s->dp_lane.p;
+  o.leaf_off = s->dp_off.p;
+  o.tiles = s->dp_tiles.p;
+  o.status = s->dp_status.p;
+  return o;
+}
+
+// Plan buffers of at least the capacities asked for; true when one moved.
+bool dp_reserve(sphgpu_space* s) {
+  const size_t nl = s->space->leaves().size();
+  bool moved = false;
+  for (int k = 0; k < 3; k++) {
+    DevPlan& dp = dp_plan_of(s, k);
+    auto grow = [&](auto& buf, size_t want) {
+      if (buf.n >= want) return;
+      buf.alloc(want);
+      moved = true;
+    };
+    grow(dp.entries, (size_t)s->dp_cap_e[k]);
+    grow(dp.lpb, nl + 1);
+    grow(dp.pb, (size_t)s->dp_cap_p[k]);
+    grow(dp.pe, (size_t)s->dp_cap_p[k]);
+    // the capacity is what the buffers hold (they may have been larger)
+    s->dp_cap_e[k] = (long long)dp.entries.n;
+    s->dp_cap_p[k] = (long long)std::min(dp.pb.n, dp.pe.n);
+  }
+  return moved;
+}
+
+// Flags from the time bins, the step's start (begin_step), the cells'
+// activation state and the density and re-run lists.
+void enqueue_dev_plans(sphgpu_space* s, cudaStream_t st, bool timed) {
+  CK(launch_dp_flags(s->flags.p, s->tbin.p, s->P.n, s->dp_bin_dev.p, st));
+  CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, s->prm.h_max, st));
+  if (timed) CK(cudaEventRecordWithFlags(s->pev[0], st, cudaEventRecordExternal));
+  const DPCellState cs = dp_state(s);
+  CK(launch_dp_cells(s->dpt, cs, s->posh.p, s->h0.p, s->flags.p, false, st));
+  CK(launch_dp_plan(s->dpt, cs, DP_DENSITY, dp_out(s, DP_DENSITY), st));
+  CK(launch_dp_plan(s->dpt, cs, DP_SUBSET, dp_out(s, DP_SUBSET), st));
+  if (timed) CK(cudaEventRecordWithFlags(s->pev[1], st, cudaEventRecordExternal));
+}
+
+void enqueue_dev_force(sphgpu_space* s, cudaStream_t st, bool timed) {
+  if (timed) CK(cudaEventRecordWithFlags(s->pev[2], st, cudaEventRecordExternal));
+  const DPCellState cs = dp_state(s);
+  CK(launch_dp_cells(s->dpt, cs, s->posh.p, s->h0.p, s->flags.p, true, st));
+  CK(launch_dp_plan(s->dpt, cs, DP_FORCE, dp_out(s, DP_FORCE), st));
+  if (timed) CK(cudaEventRecordWithFlags(s->pev[3], st, cudaEventRecordExternal));
+  enqueue_force(s, st);
+}
+
+// The whole step with device planning: flags, plans, density, ghost rounds
+// (the first `rounds` of them), force plan, force.  `captured`: enqueued
+// into a graph capture (the phase events become external event-record
+// nodes, and the planning is timed).
+void enqueue_dev_step(sphgpu_space* s, cudaStream_t st, int rounds, bool captured) {
+  auto mark = [&](cudaEvent_t e) {
+    if (captured)
+      CK(cudaEventRecordWithFlags(e, st, cudaEventRecordExternal));
+    else
+      CK(cudaEventRecord(e, st));
+  };
+  CK(cudaMemsetAsync(s->dp_status.p, 0, 8 * sizeof(int), st));
+  enqueue_dev_plans(s, st, captured);
+  enqueue_gather(s, st, s->dplan_d, 0, MODE_FIRST, false, 1, nullptr, 0, -1, 0, lists_on(s));
+  mark(s->ev[1]);
+  enqueue_ghost_rounds(s, st, 0, rounds);
+  mark(s->ev[2]);
+  enqueue_dev_force(s, st, captured);
+}
+
+// The time bins a caller set on the device (store order) into the planner.
+void sync_host_bins(sphgpu_space* s) {
+  if (!s->bins_host_stale) return;
+  const int n = s->P.n;
+  std::vector<int8_t> tb(n);
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMemcpy(tb.data(), s->tbin.p, n, cudaMemcpyDeviceToHost));
+  const auto& gperm = s->space->gperm();
+  for (int g = 0; g < n; g++) s->tb_in[gperm[g]] = tb[g];
+  s->space->set_bins(s->tb_in.data());
+  s->bins_host_stale = false;
+}
+
+// The host planner's dx_max per cell and input h after drifts.
+void sync_host_drift(sphgpu_space* s) {
+  if (!s->drifted || !s->drift_host_stale) return;
+  cudaStream_t st = s->stream;
+  const int n = s->P.n;
+  const size_t nc = s->space->cells().size();
+  std::vector<float> dx(nc), h0(n);
+  CK(cudaMemcpyAsync(dx.data(), s->dp_dx.p, sizeof(float) * nc, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h0.data(), s->h0.p, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  s->space->set_dx_max(dx.data());
+  const auto& gperm = s->space->gperm();
+  for (int g = 0; g < n; g++) s->h_in[gperm[g]] = h0[g];
+  s->space->set_input_h(s->h_in.data());
+  s->drift_host_stale = false;
+}
+
+// Bring the host planner level with the device: every particle's current h
+// into the planner, the device flags cleared (the next host activation sets
+// them by index lists again), every cell recomputed at that activation.
+void leave_device_mode(sphgpu_space* s) {
+  if (!s->dmode) return;
+  cudaStream_t st = s->stream;
+  const int n = s->P.n;
+  std::vector<float> hw(n), hs(n);
+  CK(cudaStreamSynchronize(st));
+  // posh.w of every particle: a 4-byte column of 16-byte rows
+  CK(cudaMemcpy2DAsync(hw.data(), sizeof(float), reinterpret_cast<const char*>(s->posh.p) + 12,
+                       sizeof(float4), sizeof(float), n, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemsetAsync(s->flags.p, 0, n, st));
+  CK(cudaStreamSynchronize(st));
+  for (int g = 0; g < n; g++) hs[s->s_of_g[g]] = hw[g];
+  s->space->assign_h(hs.data());
+  sync_host_drift(s);
+  s->n_act_dev = 0;
+  s->dmode = false;
+  s->h_stale = false;
+  s->force_planned = false;
+  s->host_refresh = true;
+  drop_graph(s);
+}
+
+// The host planner's activation (the body of sphgpu_set_active without the
+// device planner).
+void host_activate(sphgpu_space* s, int32_t max_active_bin) {
+  if (s->dev) CK(cudaStreamSynchronize(s->stream));
+  if (s->dev && s->h_stale) fetch_active_h(s, s->stream);
+  sync_host_bins(s);
+  const auto t0 = std::chrono::steady_clock::now();
+  s->prm.max_active_bin = max_active_bin;
+  s->space->set_activity(max_active_bin);
+  if (s->host_refresh) {
+    s->space->refresh_all();
+    s->host_refresh = false;
+  }
+  build_plans(s);
+  const auto t1 = std::chrono::steady_clock::now();
+  s->act_plan_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+  s->force_planned = false;
+  s->task_d.clear();
+  s->task_f.clear();
+  if (s->dev) {
+    upload_activity(s, s->stream);
+    bool moved = s->dplan_d.upload(s->plan_d, s->stream);
+    moved |= s->dplan_s.upload(s->plan_s, s->stream);
+    CK(cudaStreamSynchronize(s->stream));
+    s->act_upload_ms += std::chrono::duration<double, std::milli>(
+                            std::chrono::steady_clock::now() - t1).count();
+    // the force lists ahead of the step, from each active particle's last
+    // converged h; the step checks the plan's decisions on the device
+    // after its ghost and re-plans on the host if any differs
+    // (a drifted space's recursion decisions also depend on dx_max, which
+    // the device check does not see: its force lists are planned after the
+    // ghost)
+    if (!s->drifted) {
+      const auto t2 = std::chrono::steady_clock::now();
+      std::vector<uint8_t> pred;
+      s->space->plan_force_predicted(s->plan_f, pred);
+      moved |= upload_force_plan(s, pred, s->stream);
+      s->force_planned = true;
+      s->plan_ms += std::chrono::duration<double, std::milli>(
+                        std::chrono::steady_clock::now() - t2).count();
+    }
+    // the step graph reads the plans in place: it stays valid unless a
+    // buffer moved
+    if (moved) drop_graph(s);
+  } else {
+    drop_graph(s);
+  }
+}
+
+// Entry points that use the host planner's state call this first.
+void ensure_host_state(sphgpu_space* s) {
+  if (!s->dmode) return;
+  leave_device_mode(s);
+  host_activate(s, s->prm.max_active_bin);
+}
+
+// Device planning for activations that leave some particles inactive on a
+// space that is resident already (all-active steps keep the host's plans,
+// which they reuse from step to step).
+bool want_device_plans(const sphgpu_space* s, int32_t max_active_bin) {
+  return s->dev && s->dp_usable && !s->dp_off_by_caller &&
+         (max_active_bin < s->max_bin || s->drifted);
+}
+
+void enter_device_mode(sphgpu_space* s, int32_t max_active_bin) {
+  cudaStream_t st = s->stream;
+  if (!s->dp_ready) dp_upload_tree(s, st);
+  if (!s->dp_usable) return;
+  if (!s->dmode) {
+    // first capacities: the host's current plans (usually the all-active
+    // step's) with a margin; a step that needs more grows them
+    const Plan* hp[3] = {&s->plan_d, &s->plan_s, &s->plan_f};
+    for (int k = 0; k < 3; k++) {
+      s->dp_cap_e[k] = std::max<long long>(
+          s->dp_cap_e[k], std::max<long long>(1024, 3 * (long long)hp[k]->entries.size() / 2));
+      s->dp_cap_p[k] = std::max<long long>(
+          s->dp_cap_p[k], std::max<long long>(4096, 3 * (long long)hp[k]->pair_block.size() / 2));
+    }
+    s->dmode = true;
+    drop_graph(s);  // the host-planned step graph has another shape
+  }
+  if (dp_reserve(s)) drop_graph(s);
+  s->dp_bin = max_active_bin;
+  s->prm.max_active_bin = max_active_bin;
+  // the plan buffers hold another activation's lists until a step runs
+  s->force_planned = false;
+}
+
+// One step with device planning.  After the graph the host reads the
+// planner's status and the particles still iterating: a plan that outgrew
+// its buffers makes them grow and the step run again uncaptured (the step
+// only writes the active particles' fields, which begin_step resets); a
+// planner error hands the space back to the host planner for good; late
+// ghost rounds run here, then the force plan and the force again.
+// Returns false when the step must be run by the host-planned path.
+bool run_step_device(sphgpu_space* s, cudaStream_t st) {
+  s->h_stale = true;
+  const int rounds = std::min(kGraphRounds, s->prm.max_iter);
+  CK(cudaMemcpyAsync(s->dp_bin_dev.p, &s->dp_bin, sizeof(int), cudaMemcpyHostToDevice, st));
+  if (!s->graph[0]) {
+    s->graph[0] = capture(st, [&]() { enqueue_dev_step(s, st, rounds, true); });
+    s->step_stats[3]++;
+  }
+  CK(cudaEventRecord(s->ev[0], st));
+  CK(cudaGraphLaunch(s->graph[0], st));
+  CK(cudaEventRecord(s->ev[3], st));
+  s->step_stats[0]++;
+  int status[8] = {0};
+  int left = 0;
+  auto read_back = [&]() {
+    if (rounds < s->prm.max_iter) {
+      const int* cnt = lists_on(s) ? s->catchup.p + rounds : s->redo.p + rounds - 1;
+      CK(cudaMemcpyAsync(&left, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaMemcpyAsync(status, s->dp_status.p, sizeof(status), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  };
+  read_back();
+  for (int attempt = 0; attempt < 2 && status[0] == 1; attempt++) {
+    // a plan outgrew its buffers: grow them to what it needed, run again
+    for (int k = 0; k < 3; k++) {
+      s->dp_cap_e[k] = std::max(s->dp_cap_e[k], 5LL * status[1 + 2 * k] / 4 + 1024);
+      s->dp_cap_p[k] = std::max(s->dp_cap_p[k], 5LL * status[2 + 2 * k] / 4 + 4096);
+    }
+    dp_reserve(s);
+    drop_graph(s);
+    s->step_stats[1]++;
+    CK(cudaEventRecord(s->ev[0], st));
+    enqueue_dev_step(s, st, rounds, false);
+    CK(cudaEventRecord(s->pev[0], st));  // (no planning times for this step)
+    CK(cudaEventRecord(s->pev[1], st));
+    CK(cudaEventRecord(s->pev[2], st));
+    CK(cudaEventRecord(s->pev[3], st));
+    CK(cudaEventRecord(s->ev[3], st));
+    read_back();
+  }
+  if (status[0] != 0) {
+    // too deep a recursion, too many tasks on a top cell or an
+    // inconsistent tree (or buffers that would not do): the host plans
+    s->dp_usable = false;
+    leave_device_mode(s);
+    host_activate(s, s->dp_bin);
+    return false;
+  }
+  if (left > 0) {
+    enqueue_ghost_rounds(s, st, rounds, s->prm.max_iter);
+    enqueue_dev_force(s, st, false);
+    CK(cudaEventRecord(s->ev[3], st));
+    s->step_stats[2]++;
+  }
+  s->force_planned = true;
+  return true;
+}
+
+// Staging buffers of host-side inputs (sphgpu_step_host, sphgpu_space_drift).
+void ensure_stage(sphgpu_space* s, cudaStream_t st) {
+  const int n = s->P.n;
+  if (!s->x_stage.p) {
+    s->x_stage.alloc(3 * (size_t)n);
+    s->v_stage.alloc(3 * (size_t)n);
+    s->m_stage.alloc(n);
+    s->h_stage.alloc(n);
+    s->u_stage.alloc(n);
+    s->out_stage.alloc(24 * (size_t)n);
+  }
+  if (!s->x_ref.p) {
+    s->x_ref.upload(s->x_in.data(), s->x_in.size(), st);
+    s->differ.alloc(1);
+  }
+}
+
+// The drift of x_stage / h_stage (input order): measure, check the rebuild
+// criterion, then commit (sphgpu_space_drift).
+int drift_space(sphgpu_space* s, cudaStream_t st) {
+  if (!s->dp_ready) dp_upload_tree(s, st);
+  if (!s->dp_usable)
+    return fail(SPHGPU_EINVAL, "sphgpu_space_drift: the cell tree is deeper than the device "
+                               "planner's recursion stack; create a new space instead");
+  const int n = s->P.n;
+  const size_t nc = s->space->cells().size();
+  if (!s->x_rb.p) {
+    s->x_rb.upload(s->x_in.data(), s->x_in.size(), st);
+    s->dp_dx.alloc(nc);
+    CK(cudaMemsetAsync(s->dp_dx.p, 0, sizeof(unsigned) * nc, st));
+    s->dp_dxn.alloc(nc);
+    s->dp_hdrift.alloc(nc);
+    s->drift_flag.alloc(1);
+  }
+  CK(cudaMemsetAsync(s->drift_flag.p, 0, sizeof(int), st));
+  CK(launch_drift_cells(s->dpt, s->perm.p, s->x_stage.p, s->x_rb.p, s->h_stage.p, s->dp_dxn.p,
+                        s->dp_hdrift.p, st));
+  CK(launch_drift_check(s->dpt, s->dp_dxn.p, s->dp_hdrift.p, s->drift_flag.p, st));
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, s->drift_flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (flag)
+    return fail(SPHGPU_EREBUILD,
+                "the particles moved too far for the cell tree (cell_need_rebuild_for_hydro_pair "
+                "holds for a pair of neighbouring top-level cells): create a new space");
+  CK(launch_drift_commit(s->P, s->xd.p, s->depth_h0.p, s->perm.p, s->x_stage.p, s->h_stage.p,
+                         s->top_of.p, s->top_loc.p, s->leaves.p, st));
+  CK(cudaMemcpyAsync(s->dp_dx.p, s->dp_dxn.p, sizeof(unsigned) * nc, cudaMemcpyDeviceToDevice, st));
+  CK(launch_block_boxes(s->bb_fc.p, s->posh.p, s->bb_lo.p, s->bb_hi.p, s->sb_lo.p, s->sb_hi.p,
+                        s->bb_n, st));
+  CK(cudaMemcpyAsync(s->x_ref.p, s->x_stage.p, sizeof(double) * 3 * (size_t)n,
+                     cudaMemcpyDeviceToDevice, st));
+  if (!s->drifted) drop_graph(s);  // the captured plans read no dx_max yet
+  s->drifted = true;
+  s->drift_host_stale = true;
+  s->h_stale = true;
+  s->sorted_mask = 0;
+  s->task_d.clear();
+  s->task_f.clear();
+  // the next steps plan with the new dx_max and h
+  const int b = s->prm.max_active_bin;
+  if (want_device_plans(s, b)) {
+    enter_device_mode(s, b);
+  } else if (!s->dmode) {
+    s->h_stale = false;
+    CK(cudaStreamSynchronize(st));
+    // every particle's h changed: the host planner takes them all
+    std::vector<float> hw(n), hs(n);
+    CK(cudaMemcpy2DAsync(hw.data(), sizeof(float), reinterpret_cast<const char*>(s->posh.p) + 12,
+                         sizeof(float4), sizeof(float), n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int g = 0; g < n; g++) hs[s->s_of_g[g]] = hw[g];
+    s->space->assign_h(hs.data());
+    sync_host_drift(s);
+    s->host_refresh = true;
+    host_activate(s, b);
+  }
+  return SPHGPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -804,6 +1310,7 @@ static int space_create(const sphgpu_params* prm, int64_t n, const double* x,
     s->h_in.assign(h, h + n);
     s->u_in.assign(u, u + n);
     s->tb_in.assign(time_bin, time_bin + n);
+    s->max_bin = *std::max_element(time_bin, time_bin + n);
     s->space = std::make_unique<Space>(P);
     s->space->build(n, x, h, time_bin, order, tree, ncells);
     build_plans(s.get());
@@ -891,15 +1398,24 @@ int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
     if (reblock) {
       // blocks, candidate lists and every plan referring to them change
       s->space->set_jblock(t->jtile);
-      build_plans(s);
-      s->force_planned = false;
       s->task_d.clear();
       s->task_f.clear();
-      if (s->dev) {
+      s->dp_ready = false;
+      if (s->dmode) {
+        // the steps plan on the device: only the tree's block ranges change
+        // (the host's plans are rebuilt when the host planner takes over)
         upload_blocks(s, s->stream);
-        s->dplan_d.upload(s->plan_d, s->stream);
-        s->dplan_s.upload(s->plan_s, s->stream);
-        CK(cudaStreamSynchronize(s->stream));
+        dp_upload_tree(s, s->stream);
+        s->force_planned = false;
+      } else {
+        build_plans(s);
+        s->force_planned = false;
+        if (s->dev) {
+          upload_blocks(s, s->stream);
+          s->dplan_d.upload(s->plan_d, s->stream);
+          s->dplan_s.upload(s->plan_s, s->stream);
+          CK(cudaStreamSynchronize(s->stream));
+        }
       }
     }
     return SPHGPU_OK;
@@ -915,40 +1431,16 @@ int sphgpu_get_tuning(const sphgpu_space* s, sphgpu_tuning* t) {
 int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
-    if (s->dev) CK(cudaStreamSynchronize(s->stream));
-    if (s->dev && s->h_stale) fetch_active_h(s, s->stream);
-    const auto t0 = std::chrono::steady_clock::now();
-    s->prm.max_active_bin = max_active_bin;
-    s->space->set_activity(max_active_bin);
-    build_plans(s);
-    const auto t1 = std::chrono::steady_clock::now();
-    s->act_plan_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
-    s->force_planned = false;
-    s->task_d.clear();
-    s->task_f.clear();
-    if (s->dev) {
-      upload_activity(s, s->stream);
-      bool moved = s->dplan_d.upload(s->plan_d, s->stream);
-      moved |= s->dplan_s.upload(s->plan_s, s->stream);
-      CK(cudaStreamSynchronize(s->stream));
-      s->act_upload_ms += std::chrono::duration<double, std::milli>(
-                              std::chrono::steady_clock::now() - t1).count();
-      // the force lists ahead of the step, from each active particle's last
-      // converged h; the step checks the plan's decisions on the device
-      // after its ghost and re-plans on the host if any differs
-      const auto t2 = std::chrono::steady_clock::now();
-      std::vector<uint8_t> pred;
-      s->space->plan_force_predicted(s->plan_f, pred);
-      moved |= upload_force_plan(s, pred, s->stream);
-      s->force_planned = true;
-      s->plan_ms += std::chrono::duration<double, std::milli>(
-                        std::chrono::steady_clock::now() - t2).count();
-      // the step graph reads the plans in place: it stays valid unless a
-      // buffer moved
-      if (moved) drop_graph(s);
-    } else {
-      drop_graph(s);
+    if (want_device_plans(s, max_active_bin)) {
+      // the steps plan their own lists on the device: nothing to do here
+      const auto t0 = std::chrono::steady_clock::now();
+      enter_device_mode(s, max_active_bin);
+      s->act_plan_ms += std::chrono::duration<double, std::milli>(
+                            std::chrono::steady_clock::now() - t0).count();
+      if (s->dmode) return SPHGPU_OK;
     }
+    leave_device_mode(s);
+    host_activate(s, max_active_bin);
     return SPHGPU_OK;
   });
 }
@@ -1014,6 +1506,21 @@ int sphgpu_step(sphgpu_space* s, int32_t stages, void* stream) {
   return guard([&]() {
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
+    if (s->dmode && stages == SPHGPU_STAGE_ALL) {
+      if (run_step_device(s, st)) {
+        const int rc = check_conv(s, st);  // synchronises the stream
+        float ms[3] = {0.f, 0.f, 0.f}, pm[2] = {0.f, 0.f};
+        for (int k = 0; k < 3; k++) CK(cudaEventElapsedTime(&ms[k], s->ev[k], s->ev[k + 1]));
+        CK(cudaEventElapsedTime(&pm[0], s->pev[0], s->pev[1]));
+        CK(cudaEventElapsedTime(&pm[1], s->pev[2], s->pev[3]));
+        for (int k = 0; k < 3; k++) s->phase_ms[k] += ms[k];
+        s->phase_steps++;
+        s->dp_ms += pm[0] + pm[1];
+        s->dp_steps++;
+        return rc;
+      }
+    }
+    ensure_host_state(s);
     if (stages != SPHGPU_STAGE_ALL) {
       if (stages & SPHGPU_STAGE_GHOST) s->h_stale = true;
       enqueue_density_ghost(s, st, stages);
@@ -1074,12 +1581,11 @@ int sphgpu_download(sphgpu_space* s, float* fields, int32_t* ints) {
     CK(cudaStreamSynchronize(st));
     CK(launch_collect_out(s->P, s->perm.p, fields ? df.p : nullptr,
                           ints ? di.p : nullptr, st));
+    // host or device destinations (unified addressing)
     if (fields)
-      CK(cudaMemcpyAsync(fields, df.p, sizeof(float) * 24 * (size_t)n,
-                         cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(fields, df.p, sizeof(float) * 24 * (size_t)n, cudaMemcpyDefault, st));
     if (ints)
-      CK(cudaMemcpyAsync(ints, di.p, sizeof(int32_t) * 4 * (size_t)n,
-                         cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(ints, di.p, sizeof(int32_t) * 4 * (size_t)n, cudaMemcpyDefault, st));
     CK(cudaStreamSynchronize(st));
     return SPHGPU_OK;
   });
@@ -1107,34 +1613,23 @@ int sphgpu_step_host(sphgpu_space* s, const double* x, const float* v,
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
     const int n = s->P.n;
-    if (!s->x_stage.p) {
-      s->x_stage.alloc(3 * (size_t)n);
-      s->v_stage.alloc(3 * (size_t)n);
-      s->m_stage.alloc(n);
-      s->h_stage.alloc(n);
-      s->u_stage.alloc(n);
-      s->out_stage.alloc(24 * (size_t)n);
-    }
+    ensure_stage(s, st);
     CK(cudaMemcpyAsync(s->x_stage.p, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(s->v_stage.p, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(s->m_stage.p, m, sizeof(float) * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(s->h_stage.p, h, sizeof(float) * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(s->u_stage.p, u, sizeof(float) * n, cudaMemcpyHostToDevice, st));
-    if (!s->x_ref.p) {
-      s->x_ref.upload(s->x_in.data(), s->x_in.size(), st);
-      s->differ.alloc(1);
-    }
     CK(cudaMemsetAsync(s->differ.p, 0, sizeof(int), st));
     CK(launch_permute_in(s->P, s->perm.p, s->x_stage.p, s->x_ref.p, s->v_stage.p,
                          s->m_stage.p, s->h_stage.p, s->u_stage.p, s->differ.p, st));
     int differ = 0;
     CK(cudaMemcpyAsync(&differ, s->differ.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (differ)
-      return fail(SPHGPU_EINVAL,
-                  "sphgpu_step_host: positions or smoothing lengths differ from the "
-                  "space's (its cell tree and gather lists are built from them); "
-                  "create a new space");
+    if (differ) {
+      // moved particles: a drift without a rebuild, if the tree allows it
+      const int rc = drift_space(s, st);
+      if (rc != SPHGPU_OK) return rc;
+    }
     const int rc = sphgpu_step(s, SPHGPU_STAGE_ALL, (void*)st);
     if (rc != SPHGPU_OK && rc != SPHGPU_ENOCONV) return rc;
     if (fields) {
@@ -1190,7 +1685,7 @@ int finish_slot(sphgpu_space* s, int b) {
   if (S.hflags[0])
     return fail(SPHGPU_EINVAL,
                 "sphgpu_step_host_async: positions or smoothing lengths differ from the "
-                "space's; create a new space");
+                "space's; move them with sphgpu_space_drift (or sphgpu_step_host) first");
   if (S.hflags[1] > 0)
     return fail(SPHGPU_ENOCONV, "smoothing length failed to converge on " +
                                     std::to_string(S.hflags[1]) + " particles");
@@ -1245,7 +1740,7 @@ int sphgpu_step_host_async(sphgpu_space* s, const double* x, const float* v, con
     CK(cudaMemsetAsync(S.dflags.p, 0, 2 * sizeof(int), st));
     CK(launch_permute_in(s->P, s->perm.p, S.x.p, s->x_ref.p, S.v.p, S.m.p, S.h.p, S.u.p,
                          S.dflags.p, st));
-    run_step_graphs(s, st);
+    if (!s->dmode || !run_step_device(s, st)) run_step_graphs(s, st);
     CK(cudaMemcpyAsync(S.dflags.p + 1, s->redo.p + s->prm.max_iter - 1, sizeof(int),
                        cudaMemcpyDeviceToDevice, st));
     CK(launch_collect_out(s->P, s->perm.p, S.out.p, nullptr, st));
@@ -1281,6 +1776,7 @@ int sphgpu_force_from_state(sphgpu_space* s, const float* h, const float* rho,
     return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
+    ensure_host_state(s);
     cudaStream_t st = pick(s, stream);
     const int n = s->P.n;
     const auto& gperm = s->space->gperm();
@@ -1524,6 +2020,166 @@ int sphgpu_step_stats(sphgpu_space* s, int64_t out[4], int32_t reset) {
   return SPHGPU_OK;
 }
 
+int sphgpu_space_drift(sphgpu_space* s, const double* x, const float* h, void* stream) {
+  if (!s || !x || !h) return fail(SPHGPU_EINVAL, "null argument");
+  return guard([&]() {
+    ensure_device(s);
+    cudaStream_t st = pick(s, stream);
+    const int n = s->P.n;
+    ensure_stage(s, st);
+    // host or device memory (unified addressing)
+    CK(cudaMemcpyAsync(s->x_stage.p, x, sizeof(double) * 3 * (size_t)n, cudaMemcpyDefault, st));
+    CK(cudaMemcpyAsync(s->h_stage.p, h, sizeof(float) * n, cudaMemcpyDefault, st));
+    return drift_space(s, st);
+  });
+}
+
+int sphgpu_space_set_state(sphgpu_space* s, const float* v, const float* m, const float* u,
+                           const float* rho, const float* f, const float* pressure,
+                           const float* soundspeed, const float* balsara,
+                           const int8_t* time_bin, void* stream) {
+  if (!s) return fail(SPHGPU_EINVAL, "null argument");
+  if ((rho != nullptr) != (pressure != nullptr) || (rho != nullptr) != (soundspeed != nullptr))
+    return fail(SPHGPU_EINVAL, "sphgpu_space_set_state: rho, pressure and soundspeed go together");
+  return guard([&]() {
+    ensure_device(s);
+    cudaStream_t st = pick(s, stream);
+    const int n = s->P.n;
+    ensure_stage(s, st);
+    // staged (host or device sources); the density state in out_stage
+    auto stage = [&](auto* dst, const auto* src, size_t count) -> decltype(dst) {
+      if (!src) return nullptr;
+      CK(cudaMemcpyAsync(dst, src, sizeof(*src) * count, cudaMemcpyDefault, st));
+      return dst;
+    };
+    const float* dv = stage(s->v_stage.p, v, 3 * (size_t)n);
+    const float* dm = stage(s->m_stage.p, m, n);
+    const float* du = stage(s->u_stage.p, u, n);
+    float* o = s->out_stage.p;
+    const float* dr = stage(o, rho, n);
+    const float* dp = stage(o + n, pressure, n);
+    const float* dc = stage(o + 2 * (size_t)n, soundspeed, n);
+    const float* df = stage(o + 3 * (size_t)n, f, n);
+    const float* dbs = stage(o + 4 * (size_t)n, balsara, n);
+    const int8_t* db = nullptr;
+    if (time_bin) {
+      if (s->tb_stage.n < (size_t)n) s->tb_stage.alloc(n);
+      db = stage(s->tb_stage.p, time_bin, n);
+    }
+    CK(launch_set_state(s->P, s->perm.p, dv, dm, du, dr, df, dp, dc, dbs, db, s->tbin.p, st));
+    if (time_bin) {
+      // the bins are the caller's from now on: any activation may be sparse,
+      // and the force loops keep the limiter's neighbour bin
+      s->max_bin = SPH_NUM_TIME_BINS + 1;
+      s->bins_host_stale = true;
+      if (s->P.tbin != s->tbin.p) {
+        s->P.tbin = s->tbin.p;
+        drop_graph(s);  // the captured kernels hold the particle view
+      }
+    }
+    CK(cudaStreamSynchronize(st));
+    return SPHGPU_OK;
+  });
+}
+
+int sphgpu_set_device_planning(sphgpu_space* s, int32_t on) {
+  if (!s) return fail(SPHGPU_EINVAL, "null argument");
+  return guard([&]() {
+    if (on) {
+      s->dp_off_by_caller = false;
+    } else {
+      s->dp_off_by_caller = true;
+      ensure_host_state(s);
+    }
+    return SPHGPU_OK;
+  });
+}
+
+int sphgpu_plan_times(sphgpu_space* s, double* ms, int64_t* steps, int32_t reset) {
+  if (!s || !ms || !steps) return fail(SPHGPU_EINVAL, "null argument");
+  *ms = s->dp_ms;
+  *steps = s->dp_steps;
+  if (reset) {
+    s->dp_ms = 0;
+    s->dp_steps = 0;
+  }
+  return SPHGPU_OK;
+}
+
+int sphgpu_check_device_plans(sphgpu_space* s, int64_t out[6]) {
+  if (!s || !out) return fail(SPHGPU_EINVAL, "null argument");
+  if (!s->dmode || !s->force_planned)
+    return fail(SPHGPU_ESTATE, "sphgpu_check_device_plans: no device-planned step has run "
+                               "since the last activation");
+  return guard([&]() {
+    cudaStream_t st = s->stream;
+    const int n = s->P.n;
+    Space& sp = *s->space;
+    const size_t nl = sp.leaves().size();
+    std::vector<float> hw(n), h0(n), hpre(n);
+    std::vector<uint8_t> fl(n);
+    int status[8];
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy2DAsync(hw.data(), sizeof(float), reinterpret_cast<const char*>(s->posh.p) + 12,
+                         sizeof(float4), sizeof(float), n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h0.data(), s->h0.p, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(fl.data(), s->flags.p, n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(status, s->dp_status.p, sizeof(status), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // the step's starting h: the active particles restarted from h0
+    for (int g = 0; g < n; g++) hpre[s->s_of_g[g]] = (fl[g] & 1) ? h0[g] : hw[g];
+    sync_host_drift(s);  // the cells' dx_max and the active particles' starting h
+    sync_host_bins(s);
+    sp.assign_h(hpre.data());
+    sp.set_activity(s->dp_bin);
+    sp.refresh_all();
+    Plan host[3];
+    sp.plan_density(host[0], false);
+    sp.plan_subset(host[1]);
+    // the ghost's growth of the cells' h_max with the active particles' new h
+    const auto& al = sp.active_list();
+    const auto& gos = sp.gpu_of_sorted();
+    std::vector<float> hact(al.size());
+    for (size_t a = 0; a < al.size(); a++) hact[a] = hw[gos[al[a]]];
+    sp.update_h_active(hact.data());
+    sp.plan_density(host[2], true);
+    s->host_refresh = true;  // the planner's cells hold this check's state now
+    for (int k = 0; k < 3; k++) {
+      const DevPlan& dp = dp_plan_of(s, k);
+      const long long ne = std::min<long long>(status[1 + 2 * k], dp.entries.n);
+      const long long np =
+          std::min<long long>(status[2 + 2 * k], std::min(dp.pb.n, dp.pe.n));
+      std::vector<int32_t> lpb(nl + 1), pb(np), pe(np);
+      std::vector<Entry> en(ne);
+      CK(cudaMemcpy(lpb.data(), dp.lpb.p, sizeof(int32_t) * (nl + 1), cudaMemcpyDeviceToHost));
+      if (np) {
+        CK(cudaMemcpy(pb.data(), dp.pb.p, sizeof(int32_t) * np, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(pe.data(), dp.pe.p, sizeof(int32_t) * np, cudaMemcpyDeviceToHost));
+      }
+      if (ne) CK(cudaMemcpy(en.data(), dp.entries.p, sizeof(Entry) * ne, cudaMemcpyDeviceToHost));
+      const Plan& h = host[k];
+      long long bad = 0;
+      for (size_t l = 0; l < nl; l++) {
+        const int hb = h.leaf_pair_begin[l], he = h.leaf_pair_begin[l + 1];
+        const int db = lpb[l], de = lpb[l + 1];
+        if (he - hb != de - db) {
+          bad += std::max(he - hb, de - db);
+          continue;
+        }
+        for (int w = 0; w < he - hb; w++) {
+          const int dw = db + w;
+          if (dw < 0 || dw >= np || pe[dw] < 0 || pe[dw] >= ne || pb[dw] != h.pair_block[hb + w] ||
+              std::memcmp(&en[pe[dw]], &h.entries[h.pair_entry[hb + w]], sizeof(Entry)) != 0)
+            bad++;
+        }
+      }
+      out[k] = bad;
+      out[3 + k] = np;
+    }
+    return SPHGPU_OK;
+  });
+}
+
 int sphgpu_host_times(sphgpu_space* s, double ms[3], int32_t reset) {
   if (!s || !ms) return fail(SPHGPU_EINVAL, "null argument");
   ms[0] = s->act_plan_ms;
@@ -1704,6 +2360,7 @@ int sphgpu_begin_loops(sphgpu_space* s, void* stream) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
+    ensure_host_state(s);
     ensure_task_plans(s, false);
     CK(launch_begin_step(s->P, s->prm.max_iter, s->redo.p, s->prm.h_max, pick(s, stream)));
     return SPHGPU_OK;
@@ -1714,6 +2371,7 @@ int sphgpu_dosub_self1_density(sphgpu_space* s, int32_t cell, void* stream) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
+    ensure_host_state(s);
     ensure_task_plans(s, false);
     const int t = find_task(s, cell, -1);
     if (t < 0) return SPHGPU_OK;  // empty cell: nothing to do
@@ -1725,6 +2383,7 @@ int sphgpu_dosub_pair1_density(sphgpu_space* s, int32_t ci, int32_t cj, void* st
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
+    ensure_host_state(s);
     ensure_task_plans(s, false);
     const int t = find_task(s, ci, cj);
     if (t < 0) return fail(SPHGPU_EINVAL, "cells are not neighbours");
@@ -1738,6 +2397,7 @@ int sphgpu_do_ghost(sphgpu_space* s, int32_t cell, void* stream) {
   if (cell < 0 || cell >= ntop) return fail(SPHGPU_EINVAL, "cell id out of range");
   return guard([&]() {
     ensure_device(s);
+    ensure_host_state(s);
     cudaStream_t st = pick(s, stream);
     const Cell& c = s->space->cells()[cell];
     if (c.count == 0 || !c.active) return SPHGPU_OK;
@@ -1771,6 +2431,7 @@ int sphgpu_dosub_self2_force(sphgpu_space* s, int32_t cell, void* stream) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
+    ensure_host_state(s);
     ensure_force_plans(s, pick(s, stream));
     const int t = find_task(s, cell, -1);
     if (t < 0) return SPHGPU_OK;
@@ -1782,6 +2443,7 @@ int sphgpu_dosub_pair2_force(sphgpu_space* s, int32_t ci, int32_t cj, void* stre
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
+    ensure_host_state(s);
     ensure_force_plans(s, pick(s, stream));
     const int t = find_task(s, ci, cj);
     if (t < 0) return fail(SPHGPU_EINVAL, "cells are not neighbours");
@@ -1793,6 +2455,7 @@ int sphgpu_do_end_hydro_force(sphgpu_space* s, void* stream) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
     ensure_device(s);
+    ensure_host_state(s);
     CK(launch_end_force(s->P, pick(s, stream)));
     return SPHGPU_OK;
   });

@@ -779,6 +779,28 @@ void Space::assign_h(const float* h_sorted) {
   for (int k = 0; k < n_; k++) h_[k] = h_sorted[k];
 }
 
+void Space::set_dx_max(const float* per_cell) {
+  for (size_t c = 0; c < cells_.size(); c++) cells_[c].dx_max = per_cell ? per_cell[c] : 0.f;
+}
+
+void Space::set_input_h(const float* h_input_order) {
+  for (int k = 0; k < n_; k++) h_in_[k] = h_input_order[k];
+}
+
+void Space::set_bins(const int8_t* time_bin_input_order) {
+  tb_in_.assign(time_bin_input_order, time_bin_input_order + n_);
+  bin_members_.assign(256, {});
+  for (int k = 0; k < n_; k++) bin_members_[tb_in_[perm_[k]] + 128].push_back(k);
+}
+
+void Space::refresh_all() {
+  const int ntop = cdim_[0] * cdim_[1] * cdim_[2];
+  constexpr int kTopBlock = 8;  // top cells per work block
+  parallel_blocks(threads(), (ntop + kTopBlock - 1) / kTopBlock, [&](int blk) {
+    for (int c = blk * kTopBlock; c < std::min(ntop, (blk + 1) * kTopBlock); c++) redrift(c);
+  });
+}
+
 void Space::redrift(int c) {
   Cell& cc = cells_[c];
   float h_max = 0.f, h_max_active = 0.f;
@@ -1173,7 +1195,7 @@ void Space::force_decisions(std::vector<uint8_t>& pred) const {
   pred.resize(force_checks_.size());
   for (size_t q = 0; q < force_checks_.size(); q++) {
     const Cell& c = cells_[force_checks_[q].cell];
-    pred[q] = (SPH_KG * c.h_max + 0.f) < 0.5f * c.dmin ? 1 : 0;
+    pred[q] = can_recurse_pair2(c) ? 1 : 0;
   }
 }
 

@@ -27,6 +27,9 @@ struct Cell {
   double loc[3] = {0, 0, 0}, width[3] = {0, 0, 0};
   float dmin = 0, h_min_allowed = 0, h_max_allowed = 0;
   float h_max = 0, h_max_active = 0, h_max_old = 0;
+  // largest motion of the cell's particles since the rebuild
+  // (hydro.dx_max_part, cell_drift.c:330-382); 0 until the space drifts
+  float dx_max = 0;
   int count = 0, first = 0, depth = 0, split = 0, active = 0;
   int parent = -1, top = -1, leaf = -1;
   int progeny[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
@@ -92,6 +95,17 @@ class Space {
   void set_activity(int max_active_bin);
   // Current smoothing lengths of all particles (reference sorted order).
   void assign_h(const float* h_sorted);
+  // Every cell's h_max, h_max_active, activity, h_max_old and its
+  // particles' depth_h recomputed from the current h and activity (after
+  // assign_h changed the h of particles outside the last activations).
+  void refresh_all();
+  // After the particles moved without a rebuild: every cell's dx_max (per
+  // cell, 0 where null) and the particles' new input h (input order), from
+  // which active particles restart.
+  void set_dx_max(const float* per_cell);
+  void set_input_h(const float* h_input_order);
+  // New time bins (input order): the activity of later activations.
+  void set_bins(const int8_t* time_bin_input_order);
   // New h of the active particles after a ghost (same order as
   // active_list()); cells grow their h_max as runner_ghost.c:1617-1632 does.
   void update_h_active(const float* h_active);
@@ -145,6 +159,8 @@ class Space {
   const std::vector<uint8_t>& active() const { return active_; }
   const std::vector<double>& x() const { return x_; }  // wrapped, input order
   const std::vector<TopTask>& tasks() const { return tasks_; }
+  // per top cell: its tasks, in task order
+  const std::vector<std::vector<int>>& top_links() const { return top_links_; }
   const Params& params() const { return prm_; }
 
   // Recursion entry points (also used for per-task plans of the plain form).
@@ -184,21 +200,28 @@ class Space {
                    int max_depth) const;
   void leaves_under(int c, std::vector<int>& out) const;
 
-  // cell.h:934-1010 (dx_max terms are zero: no drift between rebuild and loop)
+  // kernel_gamma * h + dx_max rounded as two operations (no fused
+  // multiply-add, whatever the host compiler contracts): the device planner
+  // evaluates the same expression with __fmul_rn / __fadd_rn
+  static float reach(float h, float dx) {
+    volatile float g = SPH_KG * h;
+    return g + dx;
+  }
+  // cell.h:934-1010 (the dx_max terms are the cells' motion since the rebuild)
   static bool can_recurse_pair1(const Cell& c) {
-    return (SPH_KG * c.h_max_active + 0.f) < 0.5f * c.dmin;
+    return reach(c.h_max_active, c.dx_max) < 0.5f * c.dmin;
   }
   static bool can_recurse_self1(const Cell& c) {
     return SPH_KG * c.h_max_active < 0.5f * c.dmin;
   }
   static bool can_recurse_pair2(const Cell& c) {
-    return (SPH_KG * c.h_max + 0.f) < 0.5f * c.dmin;
+    return reach(c.h_max, c.dx_max) < 0.5f * c.dmin;
   }
   static bool can_recurse_self2(const Cell& c) {
     return c.split && (SPH_KG * c.h_max < 0.5f * c.dmin);
   }
   static bool can_recurse_pair_old(const Cell& c) {
-    return c.split && ((SPH_KG * c.h_max_old + 0.f) < 0.5f * c.dmin);
+    return c.split && (reach(c.h_max_old, c.dx_max) < 0.5f * c.dmin);
   }
   static bool can_recurse_self_old(const Cell& c) {
     return c.split && (SPH_KG * c.h_max_old < 0.5f * c.dmin);

@@ -184,7 +184,9 @@ __global__ void collect_out(DevParticles P, const int32_t* __restrict__ perm,
       const float4 ac = P.acc[i];
       const float2 hv = P.hdt_vsig[i];
       o[15] = ac.x; o[16] = ac.y; o[17] = ac.z; o[18] = ac.w;
-      o[19] = hv.x; o[20] = hv.y; o[21] = 0.f; o[22] = 0.f; o[23] = 0.f;
+      o[19] = hv.x; o[20] = hv.y;
+      o[21] = P.ngb_bin ? (float)P.ngb_bin[i] : (float)(SPH_NUM_TIME_BINS + 1);
+      o[22] = 0.f; o[23] = 0.f;
     }
     if (ints) {
       int32_t* o = ints + 4 * k;
@@ -283,6 +285,58 @@ cudaError_t launch_verify_force_plan(DevParticles p, const int4* chk, int nchk,
 cudaError_t launch_permute_vmu_in(DevParticles p, const int32_t* perm, const float* v,
                                   const float* m, const float* u, cudaStream_t s) {
   permute_vmu_in<<<grid_for(p.n), 256, 0, s>>>(p, perm, v, m, u);
+  return cudaGetLastError();
+}
+
+// A caller's state (input order; null arrays keep the store's): velocities,
+// masses, internal energies, the force inputs (rho, pressure, sound speed
+// together; the grad-h term, the Balsara switch), time bins.
+__global__ void set_state_k(DevParticles P, const int32_t* __restrict__ perm,
+                            const float* __restrict__ v, const float* __restrict__ m,
+                            const float* __restrict__ u, const float* __restrict__ rho,
+                            const float* __restrict__ gf, const float* __restrict__ pr,
+                            const float* __restrict__ cs, const float* __restrict__ bal,
+                            const int8_t* __restrict__ tb, int8_t* __restrict__ tbin) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n;
+       i += gridDim.x * blockDim.x) {
+    const size_t k = (size_t)perm[i];
+    if (v || m) {
+      float4 vm = P.velm[i];
+      if (v) {
+        vm.x = v[3 * k];
+        vm.y = v[3 * k + 1];
+        vm.z = v[3 * k + 2];
+      }
+      if (m) vm.w = m[k];
+      P.velm[i] = vm;
+    }
+    if (u) P.u[i] = u[k];
+    if (rho || gf || bal) {
+      // hydro_prepare_force's force inputs (as sphgpu_force_from_state)
+      float4 f0 = P.fin0[i];
+      float2 f1 = P.fin1[i];
+      if (rho) {
+        f0.x = rho[k];
+        f0.z = pr[k] / (rho[k] * rho[k]);
+        f0.w = cs[k];
+        f1.y = pr[k];
+      }
+      if (gf) f0.y = gf[k];
+      if (bal) f1.x = bal[k];
+      P.fin0[i] = f0;
+      P.fin1[i] = f1;
+    }
+    if (tb) tbin[i] = tb[k];
+  }
+}
+
+cudaError_t launch_set_state(DevParticles p, const int32_t* perm, const float* v,
+                             const float* m, const float* u, const float* rho,
+                             const float* f, const float* pressure, const float* soundspeed,
+                             const float* balsara, const int8_t* time_bin, int8_t* tbin,
+                             cudaStream_t s) {
+  set_state_k<<<grid_for(p.n), 256, 0, s>>>(p, perm, v, m, u, rho, f, pressure, soundspeed,
+                                            balsara, time_bin, tbin);
   return cudaGetLastError();
 }
 

@@ -190,6 +190,11 @@ cudaError_t launch_permute_in(DevParticles p, const int32_t* perm,
                               const float* v_in, const float* m_in,
                               const float* h_in, const float* u_in, int* differ,
                               cudaStream_t s);
+cudaError_t launch_set_state(DevParticles p, const int32_t* perm, const float* v,
+                             const float* m, const float* u, const float* rho,
+                             const float* f, const float* pressure, const float* soundspeed,
+                             const float* balsara, const int8_t* time_bin, int8_t* tbin,
+                             cudaStream_t s);
 cudaError_t launch_collect_out(DevParticles p, const int32_t* perm,
                                float* fields, int32_t* ints, cudaStream_t s);
 

@@ -15,8 +15,9 @@
  *
  * plus three engine hooks: gb300_rebuild after space_rebuild
  * (engine_rebuild, engine.c:1351), gb300_start_step before the hydro tasks
- * of a step (the active set, and the struct part fields a kick changed),
- * gb300_fetch after the force tasks (results back into struct part).
+ * of a step (the drifted positions and h, the struct part fields a kick
+ * changed, the active set), gb300_fetch after the force tasks (results back
+ * into struct part).
  *
  * Error convention: the reference's loops are void and call error()
  * (error.h:60) on fatal conditions; the library returns codes, which this
@@ -118,18 +119,27 @@ void gb300_rebuild(struct engine *e) {
   free(tb);
 }
 
-/* Before the hydro tasks of a step: the struct part fields the loops read
- * that a kick changed since the rebuild (v, mass, u), then the active set
+/* Before the hydro tasks of a step: the positions and h the drift gave
+ * since the rebuild (the particles keep their cells: the library measures
+ * dx_max_part and checks cell_need_rebuild_for_hydro_pair, cell.h:1237, the
+ * test the engine's own rebuild decision makes), the struct part fields the
+ * loops read that a kick changed (v, mass, u), then the active set
  * (active.h:349 part_is_active). */
 void gb300_start_step(struct engine *e) {
   const struct space *s = e->s;
   const size_t n = s->nr_parts;
+  double *x = gb300_malloc(3 * n * sizeof(double));
+  float *h = gb300_malloc(n * sizeof(float));
   float *v = gb300_malloc(3 * n * sizeof(float));
   float *m = gb300_malloc(n * sizeof(float));
   float *u = gb300_malloc(n * sizeof(float));
   for (size_t k = 0; k < n; k++) {
     const struct part *p = &s->parts[k];
-    for (int d = 0; d < 3; d++) v[3 * k + d] = p->v[d];
+    for (int d = 0; d < 3; d++) {
+      x[3 * k + d] = p->x[d];
+      v[3 * k + d] = p->v[d];
+    }
+    h[k] = p->h;
     m[k] = p->mass;
     u[k] = p->u;
   }
@@ -138,9 +148,12 @@ void gb300_start_step(struct engine *e) {
     pthread_mutex_unlock(&g_lock);
     error("gb300: no space; call gb300_rebuild after space_rebuild");
   }
+  GB300_CHECK(sphgpu_space_drift(g_space, x, h, NULL));
   GB300_CHECK(sphgpu_space_update(g_space, v, m, u, NULL));
   GB300_CHECK(sphgpu_set_active(g_space, e->max_active_bin));
   pthread_mutex_unlock(&g_lock);
+  free(x);
+  free(h);
   free(v);
   free(m);
   free(u);

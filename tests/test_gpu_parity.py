@@ -250,15 +250,23 @@ def test_step_host_matches_resident_step_and_checks_inputs():
         faster["v"] = box["v"] * 2.0      # velocities may change
         sp.step_host(faster, fields)
         assert not np.array_equal(fields[:, api.FIELD_COLS["ax"]], ref["ax"])
+        # positions and h may move within the tree (a drift without a
+        # rebuild, tests/test_drift.py), not beyond it
         moved = dict(box)
         moved["x"] = box["x"].copy()
-        moved["x"][7, 0] += 1e-3          # positions may not
-        with pytest.raises(api.SphGpuError):
-            sp.step_host(moved, fields)
+        moved["x"][7, 0] += 1e-3
+        sp.step_host(moved, fields)
+        far = dict(box)
+        far["x"] = box["x"].copy()
+        far["x"][7, 0] += 0.3
+        with pytest.raises(api.SphGpuError) as e:
+            sp.step_host(far, fields)
+        assert e.value.code == api.EREBUILD
         grown = dict(box)
-        grown["h"] = box["h"] * 1.01      # nor smoothing lengths
-        with pytest.raises(api.SphGpuError):
+        grown["h"] = box["h"] * 40.0
+        with pytest.raises(api.SphGpuError) as e:
             sp.step_host(grown, fields)
+        assert e.value.code == api.EREBUILD
 
 
 def test_space_update_gives_the_step_of_the_new_state():

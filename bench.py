@@ -68,7 +68,7 @@ WORKLOADS = {
     "integrate384": ("integrate", 384, None,
                      "time integration kernels (drift, kick2, timestep, kick1) over "
                      "384^3=56,623,104 particles of device-resident state; plus the "
-                     "engine sequence on a 32^3 jittered lattice"),
+                     "engine sequence on a 128^3 jittered lattice"),
     "sort128": ("sort", 128, 0.3,
                 "per-cell 13-axis sort arrays (runner_do_hydro_sort) of every cell of the "
                 "128^3=2,097,152-particle clustered box (rms 0.3 spacing): leaves sorted, "
@@ -396,8 +396,9 @@ def run_integrate(args):
     """Time integration: (1) the four integration kernels over a 384^3
     device-resident state (inputs far larger than L2), CUDA events per
     kernel on the launching stream, every particle active; (2) the engine
-    sequence (drift-all, rebuild, density -> ghost -> force, kick2, timestep,
-    kick1) on a 32^3 lattice, host clock per step."""
+    sequence (drift-all, the space drifted or rebuilt, density -> ghost ->
+    force, kick2, timestep, kick1) on a 128^3 lattice, host clock per
+    step."""
     import ctypes
 
     import numpy as np
@@ -470,16 +471,25 @@ def run_integrate(args):
         kern[k] = {"ms": 1e3 * avg, "bytes_per_particle": INTEG_BYTES[k], "GB_s": gbs,
                    "frac_of_measured_hbm": gbs / hbm}
     total = sum(statistics.mean(v) for v in ms.values()) / 1e3
-    # engine sequence on a small box (host rebuild per step)
-    box = ics.lattice(32, seed=args.seed, sigma_v=0.3)
+    # the engine sequence on a 128^3 lattice: device-resident state, the
+    # space drifted until the reference's rebuild criterion fires
+    del t, st
+    torch.cuda.empty_cache()
+    side = args.engine_side
+    box = ics.lattice(side, seed=args.seed, sigma_v=0.3)
     box["u"][::5] *= 6.0
+    t0 = time.perf_counter()
     it = Integrator(box, time_end=1.0, dt_max=0.05).init()
-    t_eng, act = [], []
-    for _ in range(4):
+    t_init = time.perf_counter() - t0
+    t_eng, act, mabs, rb = [], [], [], []
+    for _ in range(args.engine_steps):
+        r0 = it.rebuilds
         t0 = time.perf_counter()
-        it.step()
+        mabs.append(int(it.step()))
         t_eng.append(time.perf_counter() - t0)
         act.append(it.last_active)
+        rb.append(it.rebuilds - r0)
+    it.close()
     out = {
         "metric": "particle integrations/s (drift + kick2 + timestep + kick1)",
         "value": n / total, "unit": "particles/s", "n_gpus": 1, "steps": args.steps,
@@ -494,8 +504,14 @@ def run_integrate(args):
                      "traffic": None, "peak_note": "hbm_gbs of MEASURED_PEAKS.json",
                      "limiter": "FP64 pipe (81-85% busy under ncu, DRAM 4-19%): the "
                                 "reference's double-precision updates are kept bit-exact"},
-        "engine_sequence_32cubed": {"ms_per_step_host_clock": [round(1e3 * x, 2) for x in t_eng],
-                                    "active_particles": act, "particles": 32 ** 3},
+        "engine_sequence": {
+            "box": f"{side}^3={side ** 3:,} particles, jittered lattice, Gaussian velocities "
+                   "sigma 0.3, every fifth particle u x 6 (several time bins)",
+            "ms_per_step_host_clock": [round(1e3 * x, 2) for x in t_eng],
+            "ms_per_step_mean": round(1e3 * statistics.mean(t_eng), 2),
+            "active_particles": act, "max_active_bin": mabs, "rebuilds": rb,
+            "init_s": round(t_init, 2),
+            "host_copies_of_particle_state": "at rebuilds only (the step's state stays in HBM)"},
         "gpu_launches": 4 * args.steps,
         "clocks": clk,
     }
@@ -1000,6 +1016,10 @@ def main():
                     help="with --tuning: items per particle row (0: the library's default)")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default gather configuration")
+    ap.add_argument("--engine-side", type=int, default=128,
+                    help="integrate workload: lattice side of the engine-sequence box")
+    ap.add_argument("--engine-steps", type=int, default=12,
+                    help="integrate workload: engine steps timed")
     ap.add_argument("--integ-side", type=int, default=0,
                     help="integration workload: particles = side^3 (default 384)")
     ap.add_argument("--tuning", default="",

@@ -1,27 +1,30 @@
 """Time integration of a box of gas particles on the GPU: the reference's
 engine sequence (engine_init_particles, engine.c:2245; engine_step) with the
 drift-everything policy (the reference's --drift-all, engine_policy_drift_all)
-and a cell rebuild at every step.
+and a cell rebuild whenever the drifted particles need one.
 
 Per step, as the reference's task graph runs it:
     ti_old = ti_current; ti_current = ti_end_min
     max_active_bin = get_max_active_bin(ti_current)        (timeline.h:146)
     drift every particle to ti_current (drift_part + hydro_predict_extra,
-        cell_drift.c:253-332), then the periodic wrap of the rebuild
-    rebuild: a new space (cell tree, sorts, gather lists) from the drifted
-        positions; its cell assignment is made on the device
-        (sphgpu_cell_assign) and adopted by the host planner
+        cell_drift.c:253-332)
+    the space takes the drifted positions and h without a rebuild while
+        cell_need_rebuild_for_hydro_pair (cell.h:1237) holds for no pair of
+        neighbouring top-level cells (sphgpu_space_drift); otherwise the
+        positions get the rebuild's periodic wrap (space_cell_index.c:
+        113-123) and a new space is built from them: its cell assignment on
+        the device (sphgpu_cell_assign), adopted by the host planner
     density -> ghost for the active particles (time_bin <= max_active_bin)
     force for the active particles; inactive ones lend their predicted state
     kick2, timestep, kick1 for the active particles
         (runner_time_integration.c:360, :639, :87)
 
 The particle state stays in device memory (torch tensors, the caller's
-order); the kicks, the drift and the time steps are CUDA kernels of the
-library (sphgpu_integ_*).  The density / ghost / force passes run through
-:class:`swift_gb300.api.Space`: the tree comes from the device's cell
-assignment of the drifted positions, the gather lists from the host planner
-(so the particle state still makes a host round trip per step).
+order): the kicks, the drift and the time steps are CUDA kernels of the
+library (sphgpu_integ_*), and between rebuilds the space takes the drifted
+state, runs the loops and hands its results back in device memory (the
+gather lists of sparse steps planned on the device).  Only a rebuild copies
+the particle state to the host, for the planner of the new space.
 """
 from __future__ import annotations
 
@@ -95,12 +98,16 @@ class Integrator:
         }
         # grad-h term and Balsara switch: the force state an inactive
         # particle keeps from its last ghost
-        self.f = np.zeros(n, np.float32)
-        self.balsara = np.zeros(n, np.float32)
+        self.f = torch.zeros(n, **f32)
+        self.balsara = torch.zeros(n, **f32)
+        # the space's results of a step (sphgpu_download's columns)
+        self.fields = torch.zeros((n, 24), **f32)
         self.ti_current = 0
         self.ti_end_min = 0
         self.steps = 0
         self.last_active = 0
+        self.rebuilds = 0
+        self._space = None  # the space of the last rebuild, drifted since
 
     # -- device state ------------------------------------------------------
     def _state(self):
@@ -113,12 +120,20 @@ class Integrator:
         return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
 
     def state(self):
-        """The particle state as numpy arrays (the caller's order)."""
+        """The particle state as numpy arrays (the caller's order).  Between
+        rebuilds positions are not wrapped into the periodic box (the
+        reference wraps them at its rebuilds only)."""
         torch.cuda.synchronize(self.dev)
         out = {k: v.cpu().numpy() for k, v in self.t.items()}
-        out["f"] = self.f.copy()
-        out["balsara"] = self.balsara.copy()
+        out["f"] = self.f.cpu().numpy()
+        out["balsara"] = self.balsara.cpu().numpy()
         return out
+
+    def close(self):
+        """Frees the space (the device state stays)."""
+        if self._space is not None:
+            self._space.close()
+            self._space = None
 
     @property
     def time(self):
@@ -127,7 +142,12 @@ class Integrator:
     # -- snapshots and restarts ---------------------------------------------
     def save(self, path):
         """Write a snapshot (swift_gb300.snapshot: the PartType0 output
-        fields) with the state a restart needs."""
+        fields) with the state a restart needs.  The positions get the
+        rebuild's periodic wrap first and the next step rebuilds the space,
+        as an integrator restarted from the snapshot does: both continue
+        from the same cell tree."""
+        self._wrap()
+        self.close()
         st = self.state()
         fields = {k: st[k] for k in ("x", "v", "h", "u", "rho", "P")}
         fields["m"] = self.m
@@ -161,8 +181,8 @@ class Integrator:
             if k in ("f", "balsara"):
                 continue
             it.t[k].copy_(torch.as_tensor(np.ascontiguousarray(r[k]), device=it.dev))
-        it.f = np.array(r["f"], np.float32)
-        it.balsara = np.array(r["balsara"], np.float32)
+        it.f.copy_(torch.as_tensor(np.array(r["f"], np.float32), device=it.dev))
+        it.balsara.copy_(torch.as_tensor(np.array(r["balsara"], np.float32), device=it.dev))
         it.ti_current = int(r["ti_current"])
         it.ti_end_min = int(r["ti_end_min"])
         it.steps = int(r["steps"])
@@ -175,9 +195,20 @@ class Integrator:
                                        self.n, which, self.ti_current, mab, self._stream()))
 
     def _drift(self, ti_old, ti_new):
+        # no wrap: the space keeps every particle in its cell until a rebuild
         L = api.lib()
         api._check(L.sphgpu_integ_drift(ctypes.byref(self.ip), ctypes.byref(self._state()),
-                                        self.n, ti_old, ti_new, 1, self._stream()))
+                                        self.n, ti_old, ti_new, 0, self._stream()))
+
+    def _wrap(self):
+        """The rebuild's periodic wrap of the positions (space_cell_index.c:
+        113-123: one box length added or taken off, the far edge to 0)."""
+        if not self.ip.periodic:
+            return
+        x = self.t["x"]
+        D = torch.tensor(self.dim, dtype=torch.float64, device=self.dev)[None, :]
+        y = torch.where(x < 0.0, x + D, torch.where(x >= D, x - D, x))
+        x.copy_(torch.where(y == D, torch.zeros_like(y), y))
 
     def _timestep(self, mab):
         L = api.lib()
@@ -190,45 +221,64 @@ class Integrator:
                                   f"below dt_min ({self.ip.dt_min})")
         self.ti_end_min = tmin.value
 
-    def _hydro(self, mab, stages=api.STAGE_ALL):
-        """Rebuild from the current state and run density -> ghost (-> force)
-        for the particles with time_bin <= mab."""
+    def _rebuild(self, mab):
+        """A new space from the current state: the periodic wrap, the cell
+        assignment on the device from the positions in HBM, the host
+        planner on the adopted tree (the one host copy of the state)."""
+        self.close()
+        self._wrap()
         torch.cuda.synchronize(self.dev)
-        host = {k: self.t[k].cpu().numpy() for k in ("x", "v", "h", "u", "rho", "P", "c",
-                                                     "time_bin")}
+        host = {k: self.t[k].cpu().numpy() for k in ("x", "v", "h", "u", "time_bin")}
         box = dict(x=host["x"], v=host["v"], m=self.m, h=host["h"], u=host["u"],
                    time_bin=host["time_bin"], dim=self.dim, **self.box_meta)
-        act = host["time_bin"] <= mab
-        self.last_active = int(act.sum())
         assigned = None
         if self.device_rebuild:
-            # the rebuild's cell assignment on the device, from the drifted
-            # state in HBM; the space adopts it
             order, _, cells, _ = api.cell_assign(self.t["x"], self.t["h"], self.dim,
                                                  **self.space_params)
             assigned = (order, cells)
-        with api.Space(box, assigned=assigned, max_active_bin=mab, **self.space_params) as sp:
-            sp.step(api.STAGE_DENSITY | api.STAGE_GHOST)
-            g = sp.download()
-            h = np.where(act, g["h"], host["h"]).astype(np.float32)
-            rho = np.where(act, g["rho"], host["rho"]).astype(np.float32)
-            P = np.where(act, g["pressure"], host["P"]).astype(np.float32)
-            c = np.where(act, g["soundspeed"], host["c"]).astype(np.float32)
-            self.f = np.where(act, g["f"], self.f).astype(np.float32)
-            self.balsara = np.where(act, g["balsara"], self.balsara).astype(np.float32)
-            for k, arr in (("h", h), ("rho", rho), ("P", P), ("c", c)):
-                self.t[k].copy_(torch.as_tensor(arr, device=self.dev))
-            if not stages & api.STAGE_FORCE:
-                return
-            sp.force_from_state(h, rho, self.f, P, c, self.balsara)
-            o = sp.download()
-            nb = sp.min_ngb_bin()
-        ia = torch.as_tensor(np.nonzero(act)[0], device=self.dev)
-        a = np.stack([o["ax"], o["ay"], o["az"]], axis=1).astype(np.float32)
-        for k, arr in (("a", a), ("u_dt", o["u_dt"]), ("h_dt", o["h_dt"]),
-                       ("v_sig", o["v_sig"]), ("min_ngb_bin", nb)):
-            src = torch.as_tensor(np.ascontiguousarray(arr), device=self.dev)
-            self.t[k][ia] = src[ia]
+        self._space = api.Space(box, assigned=assigned, max_active_bin=mab,
+                                **self.space_params)
+        self.rebuilds += 1
+
+    def _hydro(self, mab, stages=api.STAGE_ALL):
+        """density -> ghost (-> force) for the particles with time_bin <= mab,
+        on the space of the last rebuild when the drifted state allows it
+        (sphgpu_space_drift), else on a new one.  Results stay on the
+        device."""
+        t = self.t
+        # the space works on its own stream: the drift's state must be there
+        torch.cuda.current_stream(self.dev).synchronize()
+        if self._space is not None:
+            try:
+                self._space.drift(t["x"], t["h"])
+            except api.SphGpuError as e:
+                if e.code != api.EREBUILD:
+                    raise
+                self.close()
+        if self._space is None:
+            self._rebuild(mab)
+        sp = self._space
+        # the caller's state for this step: what the kicks and the drift
+        # made of v and u, and the force inputs the inactive particles lend
+        sp.set_state(v=t["v"], u=t["u"], rho=t["rho"], f=self.f, pressure=t["P"],
+                     soundspeed=t["c"], balsara=self.balsara, time_bin=t["time_bin"])
+        sp.set_active(mab)
+        sp.step(stages)
+        F = sp.download_into(self.fields)  # complete on return
+        act = t["time_bin"] <= mab
+        self.last_active = int(act.sum())
+        for k, col in (("h", "h"), ("rho", "rho"), ("P", "pressure"), ("c", "soundspeed")):
+            t[k].copy_(torch.where(act, F[:, api.FIELD_COLS[col]], t[k]))
+        self.f.copy_(torch.where(act, F[:, api.FIELD_COLS["f"]], self.f))
+        self.balsara.copy_(torch.where(act, F[:, api.FIELD_COLS["balsara"]], self.balsara))
+        if not stages & api.STAGE_FORCE:
+            return
+        c0 = api.FIELD_COLS["ax"]
+        t["a"].copy_(torch.where(act[:, None], F[:, c0:c0 + 3], t["a"]))
+        for k in ("u_dt", "h_dt", "v_sig"):
+            t[k].copy_(torch.where(act, F[:, api.FIELD_COLS[k]], t[k]))
+        nb = F[:, api.FIELD_COLS["min_ngb_bin"]].to(torch.int8)
+        t["min_ngb_bin"].copy_(torch.where(act, nb, t["min_ngb_bin"]))
 
     # -- the engine sequence -----------------------------------------------
     def init(self):

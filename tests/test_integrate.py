@@ -219,9 +219,12 @@ def test_gpu_integrator_matches_oracle_integrator():
         assert mab_g == mab_r and gpu.ti_current == ref.ti_current, step
         g = gpu.state()
         assert np.mean(g["time_bin"] == ref.st["time_bin"]) > 0.999, step
-        for k in ("x",):
-            assert np.abs(g[k] - ref.st[k]).max() < 1e-6, (step, k)
+        # the oracle wraps every step (it rebuilds every step), the GPU
+        # integrator at its rebuilds only
+        assert np.abs(oi.box_wrap(g["x"], gpu.dim) - ref.st["x"]).max() < 1e-6, step
         for k in ("v_full", "h", "rho", "u_full"):
             scale = np.abs(ref.st[k]).max()
             assert np.abs(g[k] - ref.st[k]).max() < 2e-4 * scale, (step, k)
     assert min(active) < box["x"].shape[0], active  # some steps were partial
+    # the space was drifted between rebuilds (init builds the first one)
+    assert 1 <= gpu.rebuilds < 1 + 6, gpu.rebuilds

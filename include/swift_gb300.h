@@ -280,8 +280,8 @@ int sphgpu_density_noalloc(sphgpu_space *s, float *d_fields, int32_t *d_ngb,
 
 /* New velocities, masses and internal energies of every particle (input
  * order: v float [n][3], m, u float [n]), e.g. after the kicks of a step, for
- * the loops that follow.  Positions and h stay the space's (a drift that
- * moves particles needs a new space).  Replaces the copy of these
+ * the loops that follow.  Positions and h stay the space's (sphgpu_space_drift
+ * moves them).  Replaces the copy of these
  * struct part fields that the reference's loops read in place
  * (hydro/Minimal/hydro_part.h:103-240).  Synchronous; on a machine without
  * a GPU the host copies are updated and SPHGPU_ENODEV is returned. */
@@ -319,7 +319,8 @@ int sphgpu_step_host_wait(sphgpu_space *s);
  * would (one launch per self/pair task and loop, one ghost per top cell). */
 int sphgpu_step_plain(sphgpu_space *s, void *stream);
 
-/* Results in input order, into host or device memory.  fields float
+/* Results in input order, into host or device memory (device destinations
+ * are written in place by a kernel, with no allocation).  fields float
  * [n][24]: 0-7 raw density sums of the last density pass (rho, rho_dh,
  * wcount, wcount_dh, div_v, rot_v[3]), 8-14 after the ghost (h, rho, f,
  * pressure, soundspeed, balsara, v_sig seed), 15-20 after the force

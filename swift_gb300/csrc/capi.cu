@@ -1574,17 +1574,27 @@ int sphgpu_download(sphgpu_space* s, float* fields, int32_t* ints) {
   return guard([&]() {
     const int n = s->P.n;
     cudaStream_t st = s->stream;
+    // device destinations are written in place; host ones through a
+    // device buffer (unified addressing for the copies)
+    auto on_device = [](const void* p) {
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+      }
+      return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    };
+    const bool fdev = fields && on_device(fields), idev = ints && on_device(ints);
     DBuf<float> df;
     DBuf<int32_t> di;
-    if (fields) df.alloc(24 * (size_t)n);
-    if (ints) di.alloc(4 * (size_t)n);
+    if (fields && !fdev) df.alloc(24 * (size_t)n);
+    if (ints && !idev) di.alloc(4 * (size_t)n);
     CK(cudaStreamSynchronize(st));
-    CK(launch_collect_out(s->P, s->perm.p, fields ? df.p : nullptr,
-                          ints ? di.p : nullptr, st));
-    // host or device destinations (unified addressing)
-    if (fields)
+    CK(launch_collect_out(s->P, s->perm.p, fields ? (fdev ? fields : df.p) : nullptr,
+                          ints ? (idev ? ints : di.p) : nullptr, st));
+    if (fields && !fdev)
       CK(cudaMemcpyAsync(fields, df.p, sizeof(float) * 24 * (size_t)n, cudaMemcpyDefault, st));
-    if (ints)
+    if (ints && !idev)
       CK(cudaMemcpyAsync(ints, di.p, sizeof(int32_t) * 4 * (size_t)n, cudaMemcpyDefault, st));
     CK(cudaStreamSynchronize(st));
     return SPHGPU_OK;

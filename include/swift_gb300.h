@@ -109,6 +109,15 @@ typedef struct {
                                    16 in [64, 512]; the rows are kept only
                                    while they fit in a quarter of the free
                                    HBM */
+  int32_t tc_filter;            /* 1: the density gathers (one or two lanes
+                                   per particle, loads) test each surviving
+                                   j-block's candidates on the tensor cores
+                                   first (TF32 mma.sync of r^2 with a
+                                   margin that drops no candidate the FP32
+                                   test keeps); the candidates that pass are
+                                   classified exactly as without it (same
+                                   counts); 0: every candidate gets the
+                                   FP32 test */
 } sphgpu_tuning;
 
 int sphgpu_abi_version(void);
@@ -166,11 +175,12 @@ int sphgpu_get_tuning(const sphgpu_space *s, sphgpu_tuning *t);
  * steps per candidate after one warm-up) for every candidate configuration
  * (j-block depth x lanes per particle x tile shape), keeps the fastest and
  * returns it in *best; ms[k] receives the mean step time of candidate k (up
- * to 16 candidates, order: jtile 32/16/8 x threads_per_particle 1/2 x
+ * to 24 candidates, order: jtile 32/16/8 x threads_per_particle 1/2 x
  * block_warps 8/4, then -- when the rows are on -- the fastest of those with
- * row_widen 1.32, 1.44, 1.56, 1.69), *ncand their number. */
+ * one lane per particle and the fastest with two, each with row_widen 1.32,
+ * 1.44, 1.56, 1.69), *ncand their number. */
 int sphgpu_autotune(sphgpu_space *s, int32_t reps, sphgpu_tuning *best,
-                    float ms[16], int32_t *ncand);
+                    float ms[24], int32_t *ncand);
 
 /* Batched form: density -> ghost -> force over the whole box, one
  * persistent launch per loop, captured as one CUDA graph on the first call

@@ -53,7 +53,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [("threads_per_particle", ctypes.c_int32),
                 ("jtile", ctypes.c_int32), ("rerun_lists", ctypes.c_int32),
                 ("block_warps", ctypes.c_int32), ("bulk_stage", ctypes.c_int32),
-                ("row_widen", ctypes.c_float), ("row_cap", ctypes.c_int32)]
+                ("row_widen", ctypes.c_float), ("row_cap", ctypes.c_int32),
+                ("tc_filter", ctypes.c_int32)]
 
 
 class IntegParams(ctypes.Structure):
@@ -328,8 +329,9 @@ class Space:
 
     # -- configuration -----------------------------------------------------
     def set_tuning(self, tpp=1, jtile=16, rerun_lists=1, block_warps=8, bulk_stage=0,
-                   row_widen=0.0, row_cap=0):
-        t = Tuning(tpp, jtile, rerun_lists, block_warps, bulk_stage, row_widen, row_cap)
+                   row_widen=0.0, row_cap=0, tc_filter=0):
+        t = Tuning(tpp, jtile, rerun_lists, block_warps, bulk_stage, row_widen, row_cap,
+                   tc_filter)
         _check(lib().sphgpu_set_tuning(self._h, ctypes.byref(t)))
 
     def bulk_stage(self):
@@ -364,14 +366,17 @@ class Space:
         """Pick the fastest gather configuration for this box (native
         autotuner); returns ({jtile, block_warps, ...}, {config: ms})."""
         best = Tuning()
-        ms = np.zeros(16, np.float32)
+        ms = np.zeros(24, np.float32)
         n = ctypes.c_int32()
         _check(lib().sphgpu_autotune(self._h, int(reps), ctypes.byref(best),
                                      _ptr(ms), ctypes.byref(n)))
-        cands = [tuning_key(jt, tpp, bw) for jt in (32, 16, 8) for tpp in (1, 2)
-                 for bw in (8, 4)]
-        shape = tuning_key(best.jtile, best.threads_per_particle, best.block_warps)
-        cands += [f"{shape},row_widen={w}" for w in (1.32, 1.44, 1.56, 1.69)]
+        shapes = [(jt, tpp, bw) for jt in (32, 16, 8) for tpp in (1, 2) for bw in (8, 4)]
+        cands = [tuning_key(*sh) for sh in shapes]
+        # the fastest shape of each lane count (the first of equal times)
+        for lanes in (1, 2):
+            ks = [k for k, sh in enumerate(shapes) if sh[1] == lanes]
+            kb = min(ks, key=lambda k: (ms[k], k))
+            cands += [f"{cands[kb]},row_widen={w}" for w in (1.32, 1.44, 1.56, 1.69)]
         table = {name: float(ms[k]) for k, name in enumerate(cands[:n.value])}
         return ({"threads_per_particle": best.threads_per_particle,
                  "jtile": best.jtile, "rerun_lists": best.rerun_lists,

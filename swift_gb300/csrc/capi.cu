@@ -57,7 +57,7 @@ struct sphgpu_space {
   // list solver: [0] particles handed to the catch-up rounds, [r + 1] those
   // catch-up round r sends on
   DBuf<int> catchup;
-  sphgpu_tuning tune{1, SPH_JBLOCK, 1, 8, 0, 0.f, 0};
+  sphgpu_tuning tune{1, SPH_JBLOCK, 1, 8, 0, 0.f, 0, 0};
 
   // host plans
   Plan plan_d, plan_s, plan_f;
@@ -515,6 +515,7 @@ G2Args gargs(sphgpu_space* s, DevPlan& dp, int qslot, int mode) {
   a.nl_seg = 1;
   a.blk_of = s->blk_of.p;
   a.bulk = s->tune.bulk_stage;
+  a.tc = s->tune.tc_filter;
   a.err = s->err.p;
   a.sb_lo = s->sb_lo.p;
   a.sb_hi = s->sb_hi.p;
@@ -1383,11 +1384,12 @@ int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
       !(t->block_warps == 4 || t->block_warps == 8) ||
       !(t->bulk_stage == 0 || t->bulk_stage == 1) ||
       !(t->row_widen == 0.f || (t->row_widen >= 1.f && t->row_widen <= 4.f)) ||
-      !(t->row_cap == 0 || (t->row_cap >= 64 && t->row_cap <= 512 && t->row_cap % 16 == 0)))
+      !(t->row_cap == 0 || (t->row_cap >= 64 && t->row_cap <= 512 && t->row_cap % 16 == 0)) ||
+      !(t->tc_filter == 0 || t->tc_filter == 1))
     return fail(SPHGPU_EINVAL,
                 "tuning: threads_per_particle 1, 2 or 4, jtile 8, 16 or 32, block_warps 4 or 8, "
                 "bulk_stage 0 or 1, row_widen 0 or in [1, 4], row_cap 0 or a multiple of 16 "
-                "in [64, 512]");
+                "in [64, 512], tc_filter 0 or 1");
   return guard([&]() {
     if (s->dev) CK(cudaStreamSynchronize(s->stream));
     const bool reblock = t->jtile != s->tune.jtile;
@@ -1956,64 +1958,67 @@ int sphgpu_cell_sort(sphgpu_space* s, int32_t cell, int32_t axis, float* d, int3
   });
 }
 
-int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms[16],
+int sphgpu_autotune(sphgpu_space* s, int32_t reps, sphgpu_tuning* best, float ms[24],
                     int32_t* ncand) {
   if (!s || !best || !ms || !ncand || reps < 1)
     return fail(SPHGPU_EINVAL, "sphgpu_autotune: null argument or reps < 1");
   const int jt[3] = {32, 16, 8}, bw[2] = {8, 4};
   float best_ms = 3.4e38f;
   sphgpu_tuning bt = s->tune;
+  // the fastest shape with one and with two lanes per particle
+  float lane_ms[2] = {3.4e38f, 3.4e38f};
+  sphgpu_tuning lane_bt[2] = {s->tune, s->tune};
   int k = 0;
+  auto time_it = [&](const sphgpu_tuning& t, float* out) {
+    int rc = sphgpu_set_tuning(s, &t);
+    if (rc) return rc;
+    rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);  // plan + capture + warm
+    if (rc) return rc;
+    double sum[3];
+    int64_t n = 0;
+    sphgpu_phase_times(s, sum, &n, 1);
+    for (int r = 0; r < reps; r++) {
+      rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);
+      if (rc) return rc;
+    }
+    sphgpu_phase_times(s, sum, &n, 1);
+    *out = (float)((sum[0] + sum[1] + sum[2]) / std::max<int64_t>(1, n));
+    return (int)SPHGPU_OK;
+  };
   // j-tile outermost: only a new j-tile re-plans the blocks
   for (int a = 0; a < 3; a++)
     for (int c = 0; c < 4; c++, k++) {
       sphgpu_tuning t{1 + (c >> 1), jt[a], s->tune.rerun_lists, bw[c & 1],
-                      s->tune.bulk_stage, s->tune.row_widen, s->tune.row_cap};
-      int rc = sphgpu_set_tuning(s, &t);
+                      s->tune.bulk_stage, s->tune.row_widen, s->tune.row_cap,
+                      s->tune.tc_filter};
+      const int rc = time_it(t, &ms[k]);
       if (rc) return rc;
-      rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);  // plan + capture + warm
-      if (rc) return rc;
-      double sum[3];
-      int64_t n = 0;
-      sphgpu_phase_times(s, sum, &n, 1);
-      for (int r = 0; r < reps; r++) {
-        rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);
-        if (rc) return rc;
-      }
-      sphgpu_phase_times(s, sum, &n, 1);
-      ms[k] = (float)((sum[0] + sum[1] + sum[2]) / std::max<int64_t>(1, n));
       if (ms[k] < best_ms) {
         best_ms = ms[k];
         bt = t;
       }
+      if (ms[k] < lane_ms[c >> 1]) {
+        lane_ms[c >> 1] = ms[k];
+        lane_bt[c >> 1] = t;
+      }
     }
-  // then the rows' radius for the chosen shape: wider rows cover more of the
-  // ghost's iterates and of the force's partners on boxes where h moves far
-  // from its input, at the price of recording and reading more items
+  // then the rows' radius for the fastest shape of each lane count: wider
+  // rows cover more of the ghost's iterates and of the force's partners on
+  // boxes where h moves far from its input, at the price of recording and
+  // reading more items (and with them the cheaper lane count can change)
   if (s->lists && s->tune.rerun_lists) {
     const float widen[4] = {1.32f, 1.44f, 1.56f, 1.69f};
-    const sphgpu_tuning shape = bt;
-    for (int w = 0; w < 4 && k < 16; w++, k++) {
-      sphgpu_tuning t = shape;
-      t.row_widen = widen[w];
-      int rc = sphgpu_set_tuning(s, &t);
-      if (rc) return rc;
-      rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);
-      if (rc) return rc;
-      double sum[3];
-      int64_t n = 0;
-      sphgpu_phase_times(s, sum, &n, 1);
-      for (int r = 0; r < reps; r++) {
-        rc = sphgpu_step(s, SPHGPU_STAGE_ALL, nullptr);
+    for (int l = 0; l < 2; l++)
+      for (int w = 0; w < 4 && k < 24; w++, k++) {
+        sphgpu_tuning t = lane_bt[l];
+        t.row_widen = widen[w];
+        const int rc = time_it(t, &ms[k]);
         if (rc) return rc;
+        if (ms[k] < best_ms) {
+          best_ms = ms[k];
+          bt = t;
+        }
       }
-      sphgpu_phase_times(s, sum, &n, 1);
-      ms[k] = (float)((sum[0] + sum[1] + sum[2]) / std::max<int64_t>(1, n));
-      if (ms[k] < best_ms) {
-        best_ms = ms[k];
-        bt = t;
-      }
-    }
   }
   *ncand = k;
   const int rc = sphgpu_set_tuning(s, &bt);

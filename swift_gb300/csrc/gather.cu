@@ -23,6 +23,7 @@
 
 #include "device_sms.h"
 #include "gather_impl.cuh"
+#include "gather_tc.cuh"
 
 namespace sphgpu {
 
@@ -49,6 +50,24 @@ static cudaError_t launch_variant(const G2Args& a, int num_sms, int max_units,
   grid = std::max(1, std::min(grid, (max_units + WPB - 1) / WPB));
   gather_lanes<FORCE, OUT_STORE, WPB, MINB, LISTS, TPP, BULK><<<grid, WPB * 32, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+template <int WPB, int MINB, bool LISTS, int TPP>
+static cudaError_t launch_tc(const G2Args& a, int num_sms, int max_units, cudaStream_t s) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, gather_density_tc<OUT_STORE, WPB, MINB, LISTS, TPP>, WPB * 32, 0);
+  int grid = std::max(1, per_sm) * num_sms;
+  grid = std::max(1, std::min(grid, (max_units + WPB - 1) / WPB));
+  gather_density_tc<OUT_STORE, WPB, MINB, LISTS, TPP><<<grid, WPB * 32, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <bool LISTS, int TPP>
+static cudaError_t launch_tc_shape(const G2Args& a, int num_sms, int max_units, cudaStream_t s,
+                                   int block_warps) {
+  return block_warps == 4 ? launch_tc<4, 6, LISTS, TPP>(a, num_sms, max_units, s)
+                          : launch_tc<8, 3, LISTS, TPP>(a, num_sms, max_units, s);
 }
 
 // The bulk-copy staging (G2Args::bulk) exists for the 8-warp tile shape with
@@ -78,6 +97,13 @@ static cudaError_t launch_shape(const G2Args& a, bool force, int num_sms, int ma
 // or two lanes.
 cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_units,
                           cudaStream_t s, int block_warps, bool lists, int tpp) {
+  if (a.tc && !force && !a.bulk && (tpp == 1 || tpp == 2)) {
+    if (lists)
+      return tpp == 2 ? launch_tc_shape<true, 2>(a, num_sms, max_units, s, block_warps)
+                      : launch_tc_shape<true, 1>(a, num_sms, max_units, s, block_warps);
+    return tpp == 2 ? launch_tc_shape<false, 2>(a, num_sms, max_units, s, block_warps)
+                    : launch_tc_shape<false, 1>(a, num_sms, max_units, s, block_warps);
+  }
   if (a.bulk && block_warps == 8 && (tpp == 1 || tpp == 2))
     return tpp == 2 ? launch_bulk<2>(a, force, lists, num_sms, max_units, s)
                     : launch_bulk<1>(a, force, lists, num_sms, max_units, s);

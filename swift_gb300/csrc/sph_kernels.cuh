@@ -96,6 +96,9 @@ struct G2Args {
   // block); a run no particle of the group can reach is not tested
   const float4* sb_lo = nullptr;
   const float4* sb_hi = nullptr;
+  // density gathers: candidates pre-filtered on the tensor cores
+  // (gather_density_tc: one or two lanes per particle, loads)
+  int tc = 0;
 };
 
 // Later re-runs from the lists: particles whose list covers their new

@@ -226,8 +226,9 @@ def test_autotune_picks_a_candidate():
     with api.Space(box) as sp:
         sp.step()
         best, table = sp.autotune(reps=1)
-        # 12 tile shapes, then 4 row radii for the fastest shape
-        assert len(table) == 16 and all(v > 0 for v in table.values())
+        # 12 tile shapes, then 4 row radii for the fastest shape of each
+        # lane count
+        assert len(table) == 20 and all(v > 0 for v in table.values())
         key = api.tuning_key(best["jtile"], best["threads_per_particle"],
                              best["block_warps"])
         if best["row_widen"] > 0:

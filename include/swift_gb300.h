@@ -301,10 +301,10 @@ int sphgpu_space_update(sphgpu_space *s, const float *v, const float *m, const f
 /* Same pass through host buffers: copies x, v, m, h, u (input order) from
  * host memory, runs the step, copies the results back.  `fields` receives
  * float [n][24] in the column layout of sphgpu_download; NULL skips it.
- * v, m and u may change from step to step; x and h must be the space's own
- * (its cell tree and gather lists are built from them): they are checked on
- * the device and SPHGPU_EINVAL is returned, with no step run, when they
- * differ. */
+ * v, m and u may change from step to step; x and h are compared with the
+ * space's on the device and, where they differ, the particles are moved
+ * without a rebuild first (sphgpu_space_drift): SPHGPU_EREBUILD, with no step
+ * run, when they moved too far for the cell tree. */
 int sphgpu_step_host(sphgpu_space *s, const double *x, const float *v,
                      const float *m, const float *h, const float *u,
                      float *fields, void *stream);
@@ -316,9 +316,11 @@ int sphgpu_step_host(sphgpu_space *s, const double *x, const float *v,
  * most two steps are in flight: a call first waits for the step issued two
  * calls earlier.  A step's `fields` (required) and input buffers must stay
  * valid, and its results are complete, once a later call has waited for it
- * or sphgpu_step_host_wait returns; input differences and non-convergence
- * are reported there (by the call that waits for that step).  Pinned host
- * buffers make the copies asynchronous. */
+ * or sphgpu_step_host_wait returns.  x and h must be the space's (move
+ * particles with sphgpu_space_drift or sphgpu_step_host first): a step whose
+ * x or h differ runs on the space's own and SPHGPU_EINVAL, like
+ * non-convergence, is reported by the call that waits for that step.  Pinned host buffers make
+ * the copies asynchronous. */
 int sphgpu_step_host_async(sphgpu_space *s, const double *x, const float *v,
                            const float *m, const float *h, const float *u,
                            float *fields);

@@ -91,7 +91,10 @@ def test_gpu_sorts_match_reference_golden(path):
 @pytest.mark.gpu
 @pytest.mark.parametrize("cfg,run", [("lattice:16", {}),
                                      ("clustered:24", {"max_top_level_cells": 3}),
-                                     ("clustered:40", {})])
+                                     ("clustered:40", {}),
+                                     # top cells of ~9,700 particles: arrays longer
+                                     # than a block's shared memory
+                                     ("clustered:64", {"max_top_level_cells": 3})])
 def test_gpu_sorts_match_oracle(cfg, run, oracle_lib):
     box = ics.make(cfg, seed=12)
     ours = oracle_lib.tree_sorts(box, **run)

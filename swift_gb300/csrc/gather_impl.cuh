@@ -902,12 +902,15 @@ static __global__ void __launch_bounds__(256, 4)
               pk[u] = t < cnt ? row[t < c0 ? t : t - c0 + a.nl_cap / 2] : i;
               if ((pk[u] & 0x07ffffff) >= P.n || ((unsigned)pk[u] >> 27) > 26) pk[u] = i;
             }
+            // the partners' positions and velocities in flight together (a
+            // row recorded at another h holds many items beyond this
+            // particle's radius: a miss is evaluated beyond the kernel's
+            // support, its terms exactly zero)
 #pragma unroll
-            for (int u = 0; u < 3; u++) q[u] = P.posh[pk[u] & 0x07ffffff];
-            // a row recorded at another h holds many items beyond this
-            // particle's radius: only the partners that can be hits (r^2
-            // below the band's top) have their velocity and mass read; a
-            // miss is evaluated with zeros beyond the kernel's support
+            for (int u = 0; u < 3; u++) {
+              q[u] = P.posh[pk[u] & 0x07ffffff];
+              vm[u] = P.velm[pk[u] & 0x07ffffff];
+            }
             float dxs[3], dys[3], dzs[3], r2s[3];
 #pragma unroll
             for (int u = 0; u < 3; u++) {
@@ -922,7 +925,6 @@ static __global__ void __launch_bounds__(256, 4)
               dys[u] = pi.y - (q[u].y + fd.y);
               dzs[u] = pi.z - (q[u].z + fd.z);
               r2s[u] = dxs[u] * dxs[u] + dys[u] * dys[u] + dzs[u] * dzs[u];
-              vm[u] = r2s[u] < U2 ? P.velm[pk[u] & 0x07ffffff] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
 #pragma unroll
             for (int u = 0; u < 3; u++) {

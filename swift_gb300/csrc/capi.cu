@@ -194,13 +194,27 @@ struct sphgpu_space {
     DBuf<float> v, m, h, u, out;
     DBuf<int> dflags;                 // [0] inputs differ, [1] unconverged
     int* hflags = nullptr;            // pinned copy of dflags
+    float* fields = nullptr;          // the caller's result buffer
     cudaEvent_t in_done = nullptr, comp_done = nullptr, out_done = nullptr;
     bool busy = false;
   } slot[2];
   cudaStream_t cin = nullptr, cout = nullptr;
   int64_t async_k = 0;
+  // A batched step whose graph is launched and whose status words (particles
+  // still iterating, the force check's flag, the device plans' status) are on
+  // their way to pinned host memory: 0 none, 1 host-planned, 2 device-planned
+  // (finish_step reads them and runs what the step still needs).
+  int pending = 0;
+  int pending_slot = -1;  // the pipelined step's slot, or -1
+  int* hw = nullptr;      // [0] left, [1] changed, [2..9] device plan status
+  cudaEvent_t hw_ev = nullptr;
 
   ~sphgpu_space() {
+    if (hw_ev) {
+      cudaEventSynchronize(hw_ev);
+      cudaEventDestroy(hw_ev);
+    }
+    if (hw) cudaFreeHost(hw);
     for (auto& sl : slot) {
       if (sl.out_done) cudaEventSynchronize(sl.out_done);
       for (cudaEvent_t e : {sl.in_done, sl.comp_done, sl.out_done})
@@ -1093,7 +1107,17 @@ void enter_device_mode(sphgpu_space* s, int32_t max_active_bin) {
 // planner error hands the space back to the host planner for good; late
 // ghost rounds run here, then the force plan and the force again.
 // Returns false when the step must be run by the host-planned path.
-bool run_step_device(sphgpu_space* s, cudaStream_t st) {
+// Pinned status words and their event (launch_step_*).
+void ensure_status_words(sphgpu_space* s) {
+  if (s->hw) return;
+  CK(cudaMallocHost(&s->hw, 10 * sizeof(int)));
+  CK(cudaEventCreateWithFlags(&s->hw_ev, cudaEventDisableTiming));
+}
+
+// A device-planned step: its graph and the copies of its status words
+// (particles still iterating after the graph's rounds, the plans' status).
+void launch_step_device(sphgpu_space* s, cudaStream_t st) {
+  ensure_status_words(s);
   s->h_stale = true;
   const int rounds = std::min(kGraphRounds, s->prm.max_iter);
   CK(cudaMemcpyAsync(s->dp_bin_dev.p, &s->dp_bin, sizeof(int), cudaMemcpyHostToDevice, st));
@@ -1105,8 +1129,27 @@ bool run_step_device(sphgpu_space* s, cudaStream_t st) {
   CK(cudaGraphLaunch(s->graph[0], st));
   CK(cudaEventRecord(s->ev[3], st));
   s->step_stats[0]++;
-  int status[8] = {0};
-  int left = 0;
+  s->hw[0] = 0;
+  if (rounds < s->prm.max_iter) {
+    const int* cnt = lists_on(s) ? s->catchup.p + rounds : s->redo.p + rounds - 1;
+    CK(cudaMemcpyAsync(s->hw, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaMemcpyAsync(s->hw + 2, s->dp_status.p, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaEventRecord(s->hw_ev, st));
+  s->pending = 2;
+}
+
+// The rest of a device-planned step once its status words are in: 0 done,
+// 1 more work enqueued (late rounds, a re-run with larger plan buffers),
+// -1 the host planner took the space over (the step is still to be run).
+int finish_step_device(sphgpu_space* s, cudaStream_t st) {
+  CK(cudaEventSynchronize(s->hw_ev));
+  s->pending = 0;
+  const int rounds = std::min(kGraphRounds, s->prm.max_iter);
+  int status[8];
+  for (int k = 0; k < 8; k++) status[k] = s->hw[2 + k];
+  int left = s->hw[0];
+  int more = 0;
   auto read_back = [&]() {
     if (rounds < s->prm.max_iter) {
       const int* cnt = lists_on(s) ? s->catchup.p + rounds : s->redo.p + rounds - 1;
@@ -1115,7 +1158,6 @@ bool run_step_device(sphgpu_space* s, cudaStream_t st) {
     CK(cudaMemcpyAsync(status, s->dp_status.p, sizeof(status), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   };
-  read_back();
   for (int attempt = 0; attempt < 2 && status[0] == 1; attempt++) {
     // a plan outgrew its buffers: grow them to what it needed, run again
     for (int k = 0; k < 3; k++) {
@@ -1133,6 +1175,7 @@ bool run_step_device(sphgpu_space* s, cudaStream_t st) {
     CK(cudaEventRecord(s->pev[3], st));
     CK(cudaEventRecord(s->ev[3], st));
     read_back();
+    more = 1;
   }
   if (status[0] != 0) {
     // too deep a recursion, too many tasks on a top cell or an
@@ -1140,16 +1183,22 @@ bool run_step_device(sphgpu_space* s, cudaStream_t st) {
     s->dp_usable = false;
     leave_device_mode(s);
     host_activate(s, s->dp_bin);
-    return false;
+    return -1;
   }
   if (left > 0) {
     enqueue_ghost_rounds(s, st, rounds, s->prm.max_iter);
     enqueue_dev_force(s, st, false);
     CK(cudaEventRecord(s->ev[3], st));
     s->step_stats[2]++;
+    more = 1;
   }
   s->force_planned = true;
-  return true;
+  return more;
+}
+
+bool run_step_device(sphgpu_space* s, cudaStream_t st) {
+  launch_step_device(s, st);
+  return finish_step_device(s, st) >= 0;
 }
 
 // Staging buffers of host-side inputs (sphgpu_step_host, sphgpu_space_drift).
@@ -1235,6 +1284,11 @@ int drift_space(sphgpu_space* s, cudaStream_t st) {
 }  // namespace
 
 extern "C" {
+
+namespace {
+// Finishes a pipelined step still in flight (defined with the pipelined form).
+void settle(sphgpu_space* s);
+}  // namespace
 
 int sphgpu_abi_version(void) { return SPHGPU_ABI_VERSION; }
 
@@ -1391,6 +1445,7 @@ int sphgpu_set_tuning(sphgpu_space* s, const sphgpu_tuning* t) {
                 "bulk_stage 0 or 1, row_widen 0 or in [1, 4], row_cap 0 or a multiple of 16 "
                 "in [64, 512], tc_filter 0 or 1");
   return guard([&]() {
+    settle(s);
     if (s->dev) CK(cudaStreamSynchronize(s->stream));
     const bool reblock = t->jtile != s->tune.jtile;
     s->tune = *t;
@@ -1433,6 +1488,7 @@ int sphgpu_get_tuning(const sphgpu_space* s, sphgpu_tuning* t) {
 int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
+    settle(s);
     if (want_device_plans(s, max_active_bin)) {
       // the steps plan their own lists on the device: nothing to do here
       const auto t0 = std::chrono::steady_clock::now();
@@ -1448,16 +1504,8 @@ int sphgpu_set_active(sphgpu_space* s, int32_t max_active_bin) {
 }
 
 namespace {
-// A planned step is one CUDA graph: density, the first kGraphRounds ghost
-// rounds, the check of the force plan's decisions against the post-ghost
-// h_max, force.  Events ev[0..3] bracket the phases (ev[1], ev[2] are
-// event-record nodes inside the graph).  After it the host reads two words:
-// particles still iterating after the graph's rounds (rare: the remaining
-// rounds run here) and the check's flag (a decision of the force recursion
-// that the real h changed: the lists are re-planned on the host); either
-// way the force runs again on the host's plan, so the results are always
-// those of the force lists the post-ghost h gives.
-void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
+void launch_step_graphs(sphgpu_space* s, cudaStream_t st) {
+  ensure_status_words(s);
   s->h_stale = true;
   const int rounds = std::min(kGraphRounds, s->prm.max_iter);
   if (!s->graph[0]) {
@@ -1477,14 +1525,27 @@ void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
   CK(cudaGraphLaunch(s->graph[0], st));
   CK(cudaEventRecord(s->ev[3], st));
   s->step_stats[0]++;
-  int left = 0, changed = 0;
+  s->hw[0] = 0;
   if (rounds < s->prm.max_iter) {
     const int* cnt = lists_on(s) ? s->catchup.p + rounds : s->redo.p + rounds - 1;
-    CK(cudaMemcpyAsync(&left, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(s->hw, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
   }
-  CK(cudaMemcpyAsync(&changed, s->vflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  if (left <= 0 && !changed) return;
+  CK(cudaMemcpyAsync(s->hw + 1, s->vflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaEventRecord(s->hw_ev, st));
+  s->pending = 1;
+}
+
+// After the graph the host reads two words: particles still iterating after
+// the graph's rounds (rare: the remaining rounds run here) and the check's
+// flag (a decision of the force recursion that the real h changed: the
+// lists are re-planned on the host); either way the force runs again on the
+// host's plan.  Returns 1 when it enqueued more work.
+int finish_step_graphs(sphgpu_space* s, cudaStream_t st) {
+  CK(cudaEventSynchronize(s->hw_ev));
+  s->pending = 0;
+  const int rounds = std::min(kGraphRounds, s->prm.max_iter);
+  const int left = s->hw[0], changed = s->hw[1];
+  if (left <= 0 && !changed) return 0;
   if (left > 0) {
     enqueue_ghost_rounds(s, st, rounds, s->prm.max_iter);
     s->step_stats[2]++;
@@ -1496,6 +1557,16 @@ void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
                     std::chrono::steady_clock::now() - t0).count();
   enqueue_force(s, st);
   CK(cudaEventRecord(s->ev[3], st));
+  return 1;
+}
+
+// A planned step is one CUDA graph: density, the first kGraphRounds ghost
+// rounds, the check of the force plan's decisions against the post-ghost
+// h_max, force.  Events ev[0..3] bracket the phases (ev[1], ev[2] are
+// event-record nodes inside the graph).
+void run_step_graphs(sphgpu_space* s, cudaStream_t st) {
+  launch_step_graphs(s, st);
+  finish_step_graphs(s, st);
 }
 }  // namespace
 
@@ -1506,6 +1577,7 @@ int sphgpu_step(sphgpu_space* s, int32_t stages, void* stream) {
   if ((stages & SPHGPU_STAGE_FORCE) && !(stages & SPHGPU_STAGE_GHOST))
     return fail(SPHGPU_EINVAL, "the force stage needs the ghost stage");
   return guard([&]() {
+    settle(s);
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
     if (s->dmode && stages == SPHGPU_STAGE_ALL) {
@@ -1574,6 +1646,7 @@ int sphgpu_download(sphgpu_space* s, float* fields, int32_t* ints) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   if (!s->dev) return fail(SPHGPU_ESTATE, "no step has run on this space");
   return guard([&]() {
+    settle(s);
     const int n = s->P.n;
     cudaStream_t st = s->stream;
     // device destinations are written in place; host ones through a
@@ -1607,6 +1680,7 @@ int sphgpu_download_min_ngb_bin(sphgpu_space* s, int8_t* out) {
   if (!s || !out) return fail(SPHGPU_EINVAL, "null argument");
   if (!s->dev) return fail(SPHGPU_ESTATE, "no step has run on this space");
   return guard([&]() {
+    settle(s);
     const int n = s->P.n;
     std::vector<int8_t> st_order(n);
     CK(cudaStreamSynchronize(s->stream));
@@ -1622,6 +1696,7 @@ int sphgpu_step_host(sphgpu_space* s, const double* x, const float* v,
                      float* fields, void* stream) {
   if (!s || !x || !v || !m || !h || !u) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
+    settle(s);
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
     const int n = s->P.n;
@@ -1666,6 +1741,7 @@ int sphgpu_space_update(sphgpu_space* s, const float* v, const float* m, const f
       return fail(SPHGPU_EINVAL, "sphgpu_space_update: non-finite v or u, or mass <= 0 "
                                  "(particle " + std::to_string(k) + ")");
   return guard([&]() {
+    settle(s);
     // the host copies feed the next upload (first GPU call, re-plans)
     s->v_in.assign(v, v + 3 * (size_t)n);
     s->m_in.assign(m, m + n);
@@ -1705,6 +1781,41 @@ int finish_slot(sphgpu_space* s, int b) {
 }
 }  // namespace
 
+namespace {
+// The results of a slot's step: collected into the caller's order and
+// copied down behind it.
+void enqueue_slot_out(sphgpu_space* s, int b, cudaStream_t st) {
+  auto& S = s->slot[b];
+  CK(cudaMemcpyAsync(S.dflags.p + 1, s->redo.p + s->prm.max_iter - 1, sizeof(int),
+                     cudaMemcpyDeviceToDevice, st));
+  CK(launch_collect_out(s->P, s->perm.p, S.out.p, nullptr, st));
+  CK(cudaEventRecord(S.comp_done, st));
+  CK(cudaStreamWaitEvent(s->cout, S.comp_done, 0));
+  CK(cudaMemcpyAsync(S.fields, S.out.p, sizeof(float) * 24 * (size_t)s->P.n,
+                     cudaMemcpyDeviceToHost, s->cout));
+  CK(cudaMemcpyAsync(S.hflags, S.dflags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s->cout));
+  CK(cudaEventRecord(S.out_done, s->cout));
+}
+
+// The pipelined step still in flight: read its status words and run what
+// it still needs (late ghost rounds, a force re-planned on the host, larger
+// device-plan buffers, or the whole step on the host's plans), then copy its
+// results again.  Its slot stays the caller's until a later call or the wait
+// finishes it, so the corrected results land before anyone reads them.
+void settle(sphgpu_space* s) {
+  if (!s->pending) return;
+  cudaStream_t st = s->stream;
+  int more = s->pending == 1 ? finish_step_graphs(s, st) : finish_step_device(s, st);
+  if (more < 0) {
+    run_step_graphs(s, st);
+    more = 1;
+  }
+  const int b = s->pending_slot;
+  s->pending_slot = -1;
+  if (more && b >= 0) enqueue_slot_out(s, b, st);
+}
+}  // namespace
+
 int sphgpu_step_host_async(sphgpu_space* s, const double* x, const float* v, const float* m,
                            const float* h, const float* u, float* fields) {
   if (!s || !x || !v || !m || !h || !u || !fields) return fail(SPHGPU_EINVAL, "null argument");
@@ -1739,30 +1850,29 @@ int sphgpu_step_host_async(sphgpu_space* s, const double* x, const float* v, con
     // the step that used this slot two calls ago must be back first
     int rc = finish_slot(s, b);
     if (rc != SPHGPU_OK) return rc;
-    // inputs up (overlaps the previous step's compute)
+    // inputs up, while the previous step still computes
     CK(cudaMemcpyAsync(S.x.p, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->cin));
     CK(cudaMemcpyAsync(S.v.p, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->cin));
     CK(cudaMemcpyAsync(S.m.p, m, sizeof(float) * n, cudaMemcpyHostToDevice, s->cin));
     CK(cudaMemcpyAsync(S.h.p, h, sizeof(float) * n, cudaMemcpyHostToDevice, s->cin));
     CK(cudaMemcpyAsync(S.u.p, u, sizeof(float) * n, cudaMemcpyHostToDevice, s->cin));
     CK(cudaEventRecord(S.in_done, s->cin));
-    // the step
+    // the previous step's status (the host waits for it here, with these
+    // inputs already on their way), then this step
+    settle(s);
     cudaStream_t st = s->stream;
     CK(cudaStreamWaitEvent(st, S.in_done, 0));
     CK(cudaMemsetAsync(S.dflags.p, 0, 2 * sizeof(int), st));
     CK(launch_permute_in(s->P, s->perm.p, S.x.p, s->x_ref.p, S.v.p, S.m.p, S.h.p, S.u.p,
                          S.dflags.p, st));
-    if (!s->dmode || !run_step_device(s, st)) run_step_graphs(s, st);
-    CK(cudaMemcpyAsync(S.dflags.p + 1, s->redo.p + s->prm.max_iter - 1, sizeof(int),
-                       cudaMemcpyDeviceToDevice, st));
-    CK(launch_collect_out(s->P, s->perm.p, S.out.p, nullptr, st));
-    CK(cudaEventRecord(S.comp_done, st));
+    if (s->dmode)
+      launch_step_device(s, st);
+    else
+      launch_step_graphs(s, st);
+    s->pending_slot = b;
     // results down (overlaps the next step)
-    CK(cudaStreamWaitEvent(s->cout, S.comp_done, 0));
-    CK(cudaMemcpyAsync(fields, S.out.p, sizeof(float) * 24 * (size_t)n, cudaMemcpyDeviceToHost,
-                       s->cout));
-    CK(cudaMemcpyAsync(S.hflags, S.dflags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s->cout));
-    CK(cudaEventRecord(S.out_done, s->cout));
+    S.fields = fields;
+    enqueue_slot_out(s, b, st);
     S.busy = true;
     s->async_k++;
     return SPHGPU_OK;
@@ -1772,6 +1882,7 @@ int sphgpu_step_host_async(sphgpu_space* s, const double* x, const float* v, con
 int sphgpu_step_host_wait(sphgpu_space* s) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
+    settle(s);
     // oldest first
     const int b0 = (int)(s->async_k & 1);
     int rc = finish_slot(s, b0);
@@ -1787,6 +1898,7 @@ int sphgpu_force_from_state(sphgpu_space* s, const float* h, const float* rho,
   if (!s || !h || !rho || !f || !pressure || !soundspeed || !balsara)
     return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
+    settle(s);
     ensure_device(s);
     ensure_host_state(s);
     cudaStream_t st = pick(s, stream);
@@ -1905,6 +2017,7 @@ int sphgpu_hydro_sort(sphgpu_space* s, int32_t flags, void* stream) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   if (flags <= 0 || flags > 0x1FFF) return fail(SPHGPU_EINVAL, "flags: a non-empty set of the 13 axes");
   return guard([&]() {
+    settle(s);
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
     if (!s->sort_cells.p) build_sort_tree(s, st);
@@ -2038,6 +2151,7 @@ int sphgpu_step_stats(sphgpu_space* s, int64_t out[4], int32_t reset) {
 int sphgpu_space_drift(sphgpu_space* s, const double* x, const float* h, void* stream) {
   if (!s || !x || !h) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
+    settle(s);
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
     const int n = s->P.n;
@@ -2057,6 +2171,7 @@ int sphgpu_space_set_state(sphgpu_space* s, const float* v, const float* m, cons
   if ((rho != nullptr) != (pressure != nullptr) || (rho != nullptr) != (soundspeed != nullptr))
     return fail(SPHGPU_EINVAL, "sphgpu_space_set_state: rho, pressure and soundspeed go together");
   return guard([&]() {
+    settle(s);
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
     const int n = s->P.n;
@@ -2219,6 +2334,7 @@ int sphgpu_phase_times(sphgpu_space* s, double ms_sum[3], int64_t* steps,
 int sphgpu_count_hits(sphgpu_space* s, int64_t hits[4]) {
   if (!s || !hits) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
+    settle(s);
     ensure_device(s);
     cudaStream_t st = s->stream;
     int rc = SPHGPU_OK;
@@ -2479,6 +2595,7 @@ int sphgpu_do_end_hydro_force(sphgpu_space* s, void* stream) {
 int sphgpu_step_plain(sphgpu_space* s, void* stream) {
   if (!s) return fail(SPHGPU_EINVAL, "null argument");
   return guard([&]() {
+    settle(s);
     ensure_device(s);
     cudaStream_t st = pick(s, stream);
     int rc = sphgpu_begin_loops(s, st);

@@ -555,15 +555,23 @@ void enqueue_gather(sphgpu_space* s, cudaStream_t st, DevPlan& dp, int qslot,
   const DBuf<int>& lwb = tpp == 1 ? s->leaf_window_begin : s->leaf_window_begin_n[tpp / 4];
   const std::vector<int>& lwbh = tpp == 1 ? s->lwb_host : s->lwb_host_n[tpp / 4];
   CK(cudaMemsetAsync(s->queue.p + qslot, 0, sizeof(int), st));
+  // sparse launches (the ghost's re-runs over the particles still
+  // iterating, steps planned on the device for few active particles) over
+  // every leaf take only the non-empty windows: the gather then spends no
+  // work-queue atomic on an empty one
+  const bool compact = leaf_begin == 0 && leaf_end == nl && (mode == MODE_REDO || s->dmode);
+  int* ncompact = s->queue.p + 8 + qslot;
+  if (compact) CK(cudaMemsetAsync(ncompact, 0, sizeof(int), st));
   CK(launch_build_units(s->leaves.p + leaf_begin, leaf_end - leaf_begin, lwb.p + leaf_begin,
                         s->flags.p, need, veto, dp.lpb.p + leaf_begin, s->units.p, gate, st,
-                        32 / tpp));
-  // the groups of this leaf range occupy [w0, w1) of the window slots
+                        32 / tpp, compact ? ncompact : nullptr));
+  // the groups of this leaf range occupy [w0, w1) of the window slots (or,
+  // compacted, the first *ncompact)
   G2Args a = gargs(s, dp, qslot, mode);
   const int w0 = lwbh[leaf_begin], w1 = lwbh[leaf_end];
-  a.units = s->units.p + w0;
+  a.units = s->units.p + (compact ? 0 : w0);
   a.count = w1 - w0;
-  a.count_ptr = nullptr;
+  a.count_ptr = compact ? ncompact : nullptr;
   a.gate = gate;  // gated loops (ghost re-runs) do nothing when it reads 0
   if (lists) {
     a.nl = s->nl.p;

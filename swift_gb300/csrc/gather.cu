@@ -122,11 +122,12 @@ cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_unit
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                const int* leaf_window_begin, const uint8_t* flags,
                                int need, int veto, const int* leaf_pair_begin,
-                               int4* units, const int* gate, cudaStream_t s, int win) {
+                               int4* units, const int* gate, cudaStream_t s, int win,
+                               int* compact) {
   int g = (nleaves * 32 + 255) / 256;
   g = std::max(1, std::min(g, sm_count() * 16));
   build_units<<<g, 256, 0, s>>>(leaves, nleaves, leaf_window_begin, flags, need, veto,
-                                leaf_pair_begin, units, gate, win);
+                                leaf_pair_begin, units, gate, win, compact);
   return cudaGetLastError();
 }
 

@@ -795,12 +795,17 @@ gather_lanes(G2Args a, CallerOut co = CallerOut{nullptr, nullptr, nullptr}) {
 // leaf, in leaf order (so consecutive groups are spatial neighbours and
 // share cache lines), holding (window base, mask of the particles whose
 // flags contain `need`, candidate-list begin, end).  Windows with an empty
-// mask are skipped by the gathers.
+// mask are skipped by the gathers.  With `compact` (sparse launches: the
+// ghost's re-runs, steps with few active particles) only the windows with a
+// non-empty mask are written, one after another (in no fixed order; each
+// window's sums do not depend on it), and *compact counts them: the gather
+// then takes no unit off its work queue for an empty window.
 static __global__ void build_units(const LeafInfo* __restrict__ leaves, int nleaves,
                                    const int* __restrict__ leaf_window_begin,
                                    const uint8_t* __restrict__ flags, int need, int veto,
                                    const int* __restrict__ leaf_pair_begin,
-                                   int4* __restrict__ units, const int* gate, int win = 32) {
+                                   int4* __restrict__ units, const int* gate, int win = 32,
+                                   int* compact = nullptr) {
   if (gate && *gate == 0) return;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -814,7 +819,12 @@ static __global__ void build_units(const LeafInfo* __restrict__ leaves, int nlea
       const int f = in ? flags[first + w0 + lane] : 0;
       const bool ok = in && (f & need) == need && !(f & veto);
       const unsigned m = __ballot_sync(FULL, ok);
-      if (lane == 0) units[slot] = make_int4(first + w0, p0 == p1 ? 0 : (int)m, p0, p1);
+      if (compact) {
+        if (lane == 0 && m != 0u && p0 != p1)
+          units[atomicAdd(compact, 1)] = make_int4(first + w0, (int)m, p0, p1);
+      } else if (lane == 0) {
+        units[slot] = make_int4(first + w0, p0 == p1 ? 0 : (int)m, p0, p1);
+      }
     }
   }
 }

@@ -391,9 +391,26 @@ void Space::build_gpu_order() {
   jb_.cell_end.assign(cells_.size(), 0);
   std::vector<std::pair<uint32_t, int>> key;
   std::vector<int> leaf_block_begin(leaves_.size() + 1, 0);
+  // An adopted order follows each particle's octant path down to the levels
+  // the device cell assignment's keys hold: as many as 32-bit keys hold
+  // (top cell in the high bits, 3 bits a level) when every split cell lies
+  // above them, else as many as 64-bit keys hold.  A leaf at that depth has
+  // no path bits left below it (its particles keep their input order).
+  int adopt_levels = 1 << 30;
+  if (adopted_) {
+    const long long ntop = (long long)cdim_[0] * cdim_[1] * cdim_[2];
+    int top_bits = 1;
+    while ((1LL << top_bits) < ntop) top_bits++;
+    const int lfull = std::min(SPH_MAX_DEPTH - 1, (64 - top_bits) / 3);
+    const int lshort = std::max(1, std::min(lfull, (32 - top_bits) / 3));
+    int max_split = -1;
+    for (const Cell& c : cells_)
+      if (c.split) max_split = std::max(max_split, c.depth);
+    adopt_levels = max_split < lshort ? lshort : lfull;
+  }
   for (size_t l = 0; l < leaves_.size(); l++) {
     const Cell& c = cells_[leaves_[l]];
-    if (adopted_) {
+    if (adopted_ && c.depth < adopt_levels) {
       // an adopted order already follows each particle's octant path inside
       // its leaf (a Morton order at the split's own pivots): keep it
       for (int k = c.first; k < c.first + c.count; k++) {

@@ -143,11 +143,13 @@ cudaError_t launch_gather(const G2Args& a, bool force, int num_sms, int max_unit
                           cudaStream_t s, int block_warps = 8, bool lists = false,
                           int tpp = 1);
 // Work groups (windows of `win` particles, 32 or 16) of the particles whose
-// flags hold every bit of `need` and no bit of `veto`.
+// flags hold every bit of `need` and no bit of `veto`; with `compact` (zero
+// before the launch) only the non-empty ones, *compact of them.
 cudaError_t launch_build_units(const LeafInfo* leaves, int nleaves,
                                const int* leaf_window_begin, const uint8_t* flags,
                                int need, int veto, const int* leaf_pair_begin,
-                               int4* units, const int* gate, cudaStream_t s, int win = 32);
+                               int4* units, const int* gate, cudaStream_t s, int win = 32,
+                               int* compact = nullptr);
 // The ghost's rounds 1.. max_iter - 1 for every particle still iterating
 // after round 0, each particle on its own: density from its list (or, where
 // its h outgrew the list, from its leaf's re-run candidate blocks), then the
